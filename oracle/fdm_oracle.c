@@ -1,0 +1,897 @@
+/*
+ * fdm_oracle.c -- FP64 CPU restatement of the reference FDM LLG path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker for the CUDA engine and the
+ * timed CPU baseline. The product library never links or calls this code.
+ * Each function names the reference code it follows (paths relative to the
+ * mzrptu/fullmag tree).
+ */
+#include "fdm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+#define FO_MU0 (4.0 * M_PI * 1e-7) /* crates/fullmag-engine/src/lib.rs:37 */
+#define FO_ASYMPTOTIC_DISTANCE 40  /* crates/fullmag-fdm-demag/src/newell.rs:231 */
+
+int fo_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void fo_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* ------------------------------------------------------------------------- */
+/* Newell base functions: crates/fullmag-fdm-demag/src/newell.rs:21-131       */
+/* ------------------------------------------------------------------------- */
+
+double fo_newell_f(double x, double y, double z) {
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    const double r2 = x2 + y2 + z2;
+    if (r2 < 1e-300) return 0.0;
+    const double r = sqrt(r2);
+    double acc = (2.0 * x2 - y2 - z2) * r / 6.0;
+    const double sxz = x2 + z2;
+    if (sxz > 1e-300) {
+        const double t = 2.0 * y * (y + r) / sxz;
+        if (t > -1.0) acc += y * (z2 - x2) / 4.0 * log1p(t);
+    }
+    const double sxy = x2 + y2;
+    if (sxy > 1e-300) {
+        const double t = 2.0 * z * (z + r) / sxy;
+        if (t > -1.0) acc += z * (y2 - x2) / 4.0 * log1p(t);
+    }
+    if (fabs(x) > 1e-300) acc -= x * y * z * atan(y * z / (x * r));
+    return acc;
+}
+
+double fo_newell_g(double x, double y, double z) {
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    const double r2 = x2 + y2 + z2;
+    if (r2 < 1e-300) return 0.0;
+    const double r = sqrt(r2);
+    double acc = -x * y * r / 3.0;
+    const double sxy = x2 + y2;
+    if (sxy > 1e-300) {
+        const double t = 2.0 * z * (z + r) / sxy;
+        if (t > -1.0) acc += x * y * z * log1p(t) / 2.0;
+    }
+    const double syz = y2 + z2;
+    if (syz > 1e-300) {
+        const double t = 2.0 * x * (x + r) / syz;
+        if (t > -1.0) acc += y * (3.0 * z2 - y2) * log1p(t) / 12.0;
+    }
+    const double sxz = x2 + z2;
+    if (sxz > 1e-300) {
+        const double t = 2.0 * y * (y + r) / sxz;
+        if (t > -1.0) acc += x * (3.0 * z2 - x2) * log1p(t) / 12.0;
+    }
+    if (fabs(z) > 1e-300) acc -= z2 * z / 6.0 * atan(x * y / (z * r));
+    if (fabs(y) > 1e-300) acc -= y2 * z / 2.0 * atan(x * z / (y * r));
+    if (fabs(x) > 1e-300) acc -= x2 * z / 2.0 * atan(y * z / (x * r));
+    return acc;
+}
+
+/* Kahan-Neumaier compensated sum (newell.rs:133-149). */
+static double neumaier_sum(const double *v, int n) {
+    double s = 0.0, c = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double t = s + v[i];
+        if (fabs(s) >= fabs(v[i])) c += (s - t) + v[i];
+        else c += (v[i] - t) + s;
+        s = t;
+    }
+    return s + c;
+}
+
+/* 27-point second-difference stencil on a precomputed f or g table whose
+ * entry (a,b,c) holds the value at signed offset (a-1, b-1, c-1)
+ * (newell.rs:150-210). */
+static double stencil27(int i, int j, int k, const double *t, int sx, int sy, double vol) {
+    double terms[27];
+    int n = 0;
+    /* weight of offset (da,db,dc) with da,db,dc in {-1,0,1}:
+     * product over axes of (2 if d==0 else -1) = 8, -4, 2, -1 as in the reference */
+    for (int dc = -1; dc <= 1; ++dc)
+        for (int db = -1; db <= 1; ++db)
+            for (int da = -1; da <= 1; ++da) {
+                const double wa = da == 0 ? 2.0 : -1.0;
+                const double wb = db == 0 ? 2.0 : -1.0;
+                const double wc = dc == 0 ? 2.0 : -1.0;
+                const long idx = (long)(k + 1 + dc) * sy * sx + (long)(j + 1 + db) * sx + (i + 1 + da);
+                terms[n++] = wa * wb * wc * t[idx];
+            }
+    return neumaier_sum(terms, 27) / (4.0 * M_PI * vol);
+}
+
+/* Point-dipole asymptotics (newell.rs:212-229). */
+static double asym_diag(double x, double y, double z, double vol) {
+    const double r2 = x * x + y * y + z * z, r = sqrt(r2), r3 = r2 * r;
+    return (1.0 / r3 - 3.0 * x * x / (r3 * r2)) / (4.0 * M_PI) * vol;
+}
+static double asym_off(double x, double y, double z, double vol) {
+    const double r2 = x * x + y * y + z * z, r = sqrt(r2), r5 = r2 * r2 * r;
+    return -3.0 * x * y / (4.0 * M_PI * r5) * vol;
+}
+
+/* compute_newell_kernels (newell.rs:254-519). */
+int fo_newell_kernels(int nx, int ny, int nz, double dx, double dy, double dz, double *out) {
+    if (nx <= 0 || ny <= 0 || nz <= 0) return -1;
+    const int px = 2 * nx, py = 2 * ny, pz = 2 * nz;
+    const long plen = (long)px * py * pz;
+    const int sx = (nx < FO_ASYMPTOTIC_DISTANCE ? nx : FO_ASYMPTOTIC_DISTANCE) + 2;
+    const int sy = (ny < FO_ASYMPTOTIC_DISTANCE ? ny : FO_ASYMPTOTIC_DISTANCE) + 2;
+    const int sz = (nz < FO_ASYMPTOTIC_DISTANCE ? nz : FO_ASYMPTOTIC_DISTANCE) + 2;
+    const long flen = (long)sx * sy * sz;
+    double *tab = (double *)malloc(sizeof(double) * 6 * flen);
+    if (!tab) return -2;
+    double *fxx = tab, *fyy = tab + flen, *fzz = tab + 2 * flen;
+    double *gxy = tab + 3 * flen, *gxz = tab + 4 * flen, *gyz = tab + 5 * flen;
+
+#pragma omp parallel for schedule(dynamic)
+    for (int c = 0; c < sz; ++c)
+        for (int b = 0; b < sy; ++b)
+            for (int a = 0; a < sx; ++a) {
+                const double x = (a - 1) * dx, y = (b - 1) * dy, z = (c - 1) * dz;
+                const long id = (long)c * sy * sx + (long)b * sx + a;
+                fxx[id] = fo_newell_f(x, y, z);
+                fyy[id] = fo_newell_f(y, x, z);
+                fzz[id] = fo_newell_f(z, y, x);
+                gxy[id] = fo_newell_g(x, y, z);
+                gxz[id] = fo_newell_g(x, z, y);
+                gyz[id] = fo_newell_g(y, z, x);
+            }
+
+    memset(out, 0, sizeof(double) * 6 * plen);
+    double *nxx = out, *nyy = out + plen, *nzz = out + 2 * plen;
+    double *nxy = out + 3 * plen, *nxz = out + 4 * plen, *nyz = out + 5 * plen;
+    const double vol = dx * dy * dz;
+    const int AD = FO_ASYMPTOTIC_DISTANCE;
+
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                double vxx, vyy, vzz, vxy, vxz, vyz;
+                const long d2 = (long)i * i + (long)j * j + (long)k * k;
+                if (i >= AD || j >= AD || k >= AD || d2 >= (long)AD * AD) {
+                    const double x = i * dx, y = j * dy, z = k * dz;
+                    vxx = asym_diag(x, y, z, vol);
+                    vyy = asym_diag(y, x, z, vol);
+                    vzz = asym_diag(z, y, x, vol);
+                    vxy = asym_off(x, y, z, vol);
+                    vxz = asym_off(x, z, y, vol);
+                    vyz = asym_off(y, z, x, vol);
+                } else {
+                    vxx = stencil27(i, j, k, fxx, sx, sy, vol);
+                    vyy = stencil27(i, j, k, fyy, sx, sy, vol);
+                    vzz = stencil27(i, j, k, fzz, sx, sy, vol);
+                    vxy = stencil27(i, j, k, gxy, sx, sy, vol);
+                    vxz = stencil27(i, j, k, gxz, sx, sy, vol);
+                    vyz = stencil27(i, j, k, gyz, sx, sy, vol);
+                }
+                /* octant placement with parity signs (newell.rs:393-425) */
+                const int nxs = i == 0 ? 1 : 2, nys = j == 0 ? 1 : 2, nzs = k == 0 ? 1 : 2;
+                for (int a = 0; a < nxs; ++a) {
+                    const int ix = a == 0 ? i : px - i;
+                    const double sxg = a == 0 ? 1.0 : -1.0;
+                    for (int b = 0; b < nys; ++b) {
+                        const int iy = b == 0 ? j : py - j;
+                        const double syg = b == 0 ? 1.0 : -1.0;
+                        for (int c = 0; c < nzs; ++c) {
+                            const int iz = c == 0 ? k : pz - k;
+                            const double szg = c == 0 ? 1.0 : -1.0;
+                            const long p = (long)iz * py * px + (long)iy * px + ix;
+                            nxx[p] = vxx;
+                            nyy[p] = vyy;
+                            nzz[p] = vzz;
+                            nxy[p] = vxy * sxg * syg;
+                            nxz[p] = vxz * sxg * szg;
+                            nyz[p] = vyz * syg * szg;
+                        }
+                    }
+                }
+            }
+    free(tab);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Mixed-radix FFT (own implementation; stands in for rustfft 6.4.1)          */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    int n;
+    int nf;
+    int f[64];
+    int maxp;
+    double *w; /* w[2e], w[2e+1] = cos, -sin of 2*pi*e/n */
+} fft_plan;
+
+static int plan_init(fft_plan *P, int n) {
+    P->n = n;
+    P->nf = 0;
+    P->maxp = 4;
+    int m = n;
+    while (m % 4 == 0) { P->f[P->nf++] = 4; m /= 4; }
+    while (m % 2 == 0) { P->f[P->nf++] = 2; m /= 2; }
+    for (int q = 3; (long)q * q <= m; q += 2)
+        while (m % q == 0) { P->f[P->nf++] = q; m /= q; }
+    if (m > 1) P->f[P->nf++] = m;
+    for (int i = 0; i < P->nf; ++i)
+        if (P->f[i] > P->maxp) P->maxp = P->f[i];
+    P->w = (double *)malloc(sizeof(double) * 2 * (size_t)(n > 0 ? n : 1));
+    if (!P->w) return -1;
+    for (int e = 0; e < n; ++e) {
+        const double ang = 2.0 * M_PI * (double)e / (double)n;
+        P->w[2 * e] = cos(ang);
+        P->w[2 * e + 1] = -sin(ang);
+    }
+    return 0;
+}
+
+static void plan_free(fft_plan *P) {
+    free(P->w);
+    P->w = NULL;
+}
+
+/* Decimation in time: X[k + q m] = sum_r W_p^{rq} W_n^{rk} DFT_m(x[r::p])[k]. */
+static void fft_rec(const fft_plan *P, const double *in, long is, double *out, int n, int fi,
+                    int inv, double *tmp) {
+    if (n == 1) {
+        out[0] = in[0];
+        out[1] = in[1];
+        return;
+    }
+    const int p = P->f[fi];
+    const int m = n / p;
+    for (int r = 0; r < p; ++r) fft_rec(P, in + 2 * r * is, is * p, out + 2 * (long)r * m, m, fi + 1, inv, tmp);
+    const long N = P->n;
+    const long tws = N / n;
+    const double sg = inv ? -1.0 : 1.0; /* conjugate twiddles for the inverse */
+    for (int k = 0; k < m; ++k) {
+        for (int r = 0; r < p; ++r) {
+            const double re = out[2 * ((long)r * m + k)], im = out[2 * ((long)r * m + k) + 1];
+            const long e = ((long)r * k % n) * tws;
+            const double wr = P->w[2 * e], wi = sg * P->w[2 * e + 1];
+            tmp[2 * r] = re * wr - im * wi;
+            tmp[2 * r + 1] = re * wi + im * wr;
+        }
+        if (p == 2) {
+            out[2 * k] = tmp[0] + tmp[2];
+            out[2 * k + 1] = tmp[1] + tmp[3];
+            out[2 * (k + m)] = tmp[0] - tmp[2];
+            out[2 * (k + m) + 1] = tmp[1] - tmp[3];
+        } else if (p == 4) {
+            const double a0r = tmp[0] + tmp[4], a0i = tmp[1] + tmp[5];
+            const double a1r = tmp[0] - tmp[4], a1i = tmp[1] - tmp[5];
+            const double b0r = tmp[2] + tmp[6], b0i = tmp[3] + tmp[7];
+            const double dr = tmp[2] - tmp[6], di = tmp[3] - tmp[7];
+            /* forward: b1 = -i*d ; inverse: b1 = +i*d */
+            const double b1r = inv ? -di : di;
+            const double b1i = inv ? dr : -dr;
+            out[2 * k] = a0r + b0r;
+            out[2 * k + 1] = a0i + b0i;
+            out[2 * (k + 2 * m)] = a0r - b0r;
+            out[2 * (k + 2 * m) + 1] = a0i - b0i;
+            out[2 * (k + m)] = a1r + b1r;
+            out[2 * (k + m) + 1] = a1i + b1i;
+            out[2 * (k + 3 * m)] = a1r - b1r;
+            out[2 * (k + 3 * m) + 1] = a1i - b1i;
+        } else {
+            const long pstep = N / p;
+            for (int q = 0; q < p; ++q) {
+                double sr = 0.0, si = 0.0;
+                for (int r = 0; r < p; ++r) {
+                    const long e = ((long)r * q % p) * pstep;
+                    const double wr = P->w[2 * e], wi = sg * P->w[2 * e + 1];
+                    sr += tmp[2 * r] * wr - tmp[2 * r + 1] * wi;
+                    si += tmp[2 * r] * wi + tmp[2 * r + 1] * wr;
+                }
+                out[2 * (k + (long)q * m)] = sr;
+                out[2 * (k + (long)q * m) + 1] = si;
+            }
+        }
+    }
+}
+
+/* Transform one line gathered with a stride (in complex elements). */
+static void fft_line(const fft_plan *P, double *base, long stride, int inv, double *lin, double *lout,
+                     double *tmp) {
+    const int n = P->n;
+    for (int i = 0; i < n; ++i) {
+        lin[2 * i] = base[2 * i * stride];
+        lin[2 * i + 1] = base[2 * i * stride + 1];
+    }
+    fft_rec(P, lin, 1, lout, n, 0, inv, tmp);
+    for (int i = 0; i < n; ++i) {
+        base[2 * i * stride] = lout[2 * i];
+        base[2 * i * stride + 1] = lout[2 * i + 1];
+    }
+}
+
+int fo_fft1d(double *data, int n, int inverse) {
+    if (n <= 0) return -1;
+    fft_plan P;
+    if (plan_init(&P, n)) return -2;
+    double *buf = (double *)malloc(sizeof(double) * (4 * (size_t)n + 2 * (size_t)P.maxp));
+    if (!buf) { plan_free(&P); return -2; }
+    fft_line(&P, data, 1, inverse, buf, buf + 2 * n, buf + 4 * n);
+    free(buf);
+    plan_free(&P);
+    return 0;
+}
+
+/* x, then y, then z lines, as fft3_core (crates/fullmag-engine/src/fdm_fft.rs:445-573). */
+int fo_fft3d(double *data, int px, int py, int pz, int inverse) {
+    fft_plan Px, Py, Pz;
+    if (plan_init(&Px, px) || plan_init(&Py, py) || plan_init(&Pz, pz)) return -2;
+    int maxn = px > py ? px : py;
+    if (pz > maxn) maxn = pz;
+    int maxp = Px.maxp > Py.maxp ? Px.maxp : Py.maxp;
+    if (Pz.maxp > maxp) maxp = Pz.maxp;
+    const long sxy = (long)px * py;
+#pragma omp parallel
+    {
+        double *buf = (double *)malloc(sizeof(double) * (4 * (size_t)maxn + 2 * (size_t)maxp));
+#pragma omp for schedule(static)
+        for (long row = 0; row < (long)py * pz; ++row)
+            fft_line(&Px, data + 2 * row * px, 1, inverse, buf, buf + 2 * maxn, buf + 4 * maxn);
+#pragma omp for schedule(static)
+        for (long col = 0; col < (long)px * pz; ++col) {
+            const long z = col / px, x = col % px;
+            fft_line(&Py, data + 2 * (z * sxy + x), px, inverse, buf, buf + 2 * maxn, buf + 4 * maxn);
+        }
+        if (pz > 1) {
+#pragma omp for schedule(static)
+            for (long col = 0; col < sxy; ++col)
+                fft_line(&Pz, data + 2 * col, sxy, inverse, buf, buf + 2 * maxn, buf + 4 * maxn);
+        }
+        free(buf);
+    }
+    plan_free(&Px);
+    plan_free(&Py);
+    plan_free(&Pz);
+    return 0;
+}
+
+/* compute_newell_kernel_spectra / _thin_film_2d (fdm_fft.rs:334-437). */
+int fo_newell_spectra(int nx, int ny, int nz, double dx, double dy, double dz, int thin_film_2d,
+                      double *out) {
+    if (thin_film_2d && nz != 1) return -1;
+    const int px = 2 * nx, py = 2 * ny, pz = 2 * nz;
+    const long plen3 = (long)px * py * pz;
+    double *real = (double *)malloc(sizeof(double) * 6 * plen3);
+    if (!real) return -2;
+    int rc = fo_newell_kernels(nx, ny, nz, dx, dy, dz, real);
+    if (rc) { free(real); return rc; }
+    const long P = thin_film_2d ? (long)px * py : plen3;
+    for (int c = 0; c < 6; ++c) {
+        double *o = out + 2 * P * c;
+        const double *r = real + plen3 * c;
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < P; ++i) {
+            o[2 * i] = r[i]; /* thin film: the z = 0 plane is the first px*py values */
+            o[2 * i + 1] = 0.0;
+        }
+        rc = fo_fft3d(o, px, py, thin_film_2d ? 1 : pz, 0);
+        if (rc) break;
+    }
+    free(real);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Problem: fields, RHS, integrators                                          */
+/* ------------------------------------------------------------------------- */
+
+struct fo_problem {
+    fo_params p;
+    long n;
+    uint8_t *mask;
+    double *m; /* AoS current state */
+    double t;
+    double step;
+    int px, py, pz;
+    long P;
+    double *kern[6]; /* complex spectra (interleaved), full padded grid */
+    double *bm[3];   /* complex M */
+    double *bh[3];   /* complex H */
+    double u[3], c1[3], c2[3], c3[3];
+    /* integrator buffers (AoS) */
+    double *m0, *mst, *heff, *hscr, *k[7], *fsal;
+    int fsal_valid;
+};
+
+static inline int active(const fo_problem *pr, long i) { return pr->mask == NULL || pr->mask[i] != 0; }
+
+static void norm3(const double *a, double *o) {
+    double n = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (n < 1e-30) n = 1e-30;
+    o[0] = a[0] / n;
+    o[1] = a[1] / n;
+    o[2] = a[2] / n;
+}
+
+static double *dalloc(long n) { return (double *)calloc((size_t)n, sizeof(double)); }
+
+void fo_destroy(fo_problem *pr) {
+    if (!pr) return;
+    free(pr->mask);
+    free(pr->m);
+    for (int c = 0; c < 6; ++c) free(pr->kern[c]);
+    for (int c = 0; c < 3; ++c) { free(pr->bm[c]); free(pr->bh[c]); }
+    free(pr->m0); free(pr->mst); free(pr->heff); free(pr->hscr); free(pr->fsal);
+    for (int s = 0; s < 7; ++s) free(pr->k[s]);
+    free(pr);
+}
+
+fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
+    if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0) return NULL;
+    fo_problem *pr = (fo_problem *)calloc(1, sizeof(fo_problem));
+    if (!pr) return NULL;
+    pr->p = *p;
+    pr->p.active_mask = NULL;
+    pr->n = (long)p->nx * p->ny * p->nz;
+    const long n3 = 3 * pr->n;
+    if (p->active_mask) {
+        pr->mask = (uint8_t *)malloc((size_t)pr->n);
+        memcpy(pr->mask, p->active_mask, (size_t)pr->n);
+    }
+    pr->m = dalloc(n3);
+    pr->m0 = dalloc(n3); pr->mst = dalloc(n3); pr->heff = dalloc(n3); pr->hscr = dalloc(n3);
+    pr->fsal = dalloc(n3);
+    for (int s = 0; s < 7; ++s) pr->k[s] = dalloc(n3);
+    norm3(p->u_axis, pr->u);
+    norm3(p->c1, pr->c1);
+    norm3(p->c2, pr->c2);
+    pr->c3[0] = pr->c1[1] * pr->c2[2] - pr->c1[2] * pr->c2[1];
+    pr->c3[1] = pr->c1[2] * pr->c2[0] - pr->c1[0] * pr->c2[2];
+    pr->c3[2] = pr->c1[0] * pr->c2[1] - pr->c1[1] * pr->c2[0];
+    if (p->enable_demag) {
+        pr->px = 2 * p->nx; pr->py = 2 * p->ny; pr->pz = 2 * p->nz;
+        pr->P = (long)pr->px * pr->py * pr->pz;
+        double *sp = dalloc(12 * pr->P);
+        if (!sp || fo_newell_spectra(p->nx, p->ny, p->nz, p->dx, p->dy, p->dz, 0, sp)) {
+            free(sp);
+            fo_destroy(pr);
+            return NULL;
+        }
+        for (int c = 0; c < 6; ++c) {
+            pr->kern[c] = dalloc(2 * pr->P);
+            memcpy(pr->kern[c], sp + 2 * pr->P * c, sizeof(double) * 2 * pr->P);
+        }
+        free(sp);
+        for (int c = 0; c < 3; ++c) { pr->bm[c] = dalloc(2 * pr->P); pr->bh[c] = dalloc(2 * pr->P); }
+    }
+    if (m0_aos) fo_set_m(pr, m0_aos);
+    return pr;
+}
+
+int fo_set_m(fo_problem *pr, const double *m_aos) {
+    for (long i = 0; i < pr->n; ++i)
+        for (int c = 0; c < 3; ++c) pr->m[3 * i + c] = active(pr, i) ? m_aos[3 * i + c] : 0.0;
+    pr->fsal_valid = 0;
+    return 0;
+}
+
+int fo_get_m(const fo_problem *pr, double *m_aos) {
+    memcpy(m_aos, pr->m, sizeof(double) * 3 * pr->n);
+    return 0;
+}
+
+/* exchange_field_add_into (fdm_fields.rs:445-527), Neumann clamp (fdm_types.rs:126-132). */
+static void exchange_add(const fo_problem *pr, const double *m, double *h) {
+    const fo_params *p = &pr->p;
+    const double pref = 2.0 * p->a_ex / (FO_MU0 * p->ms);
+    const double ix2 = 1.0 / (p->dx * p->dx), iy2 = 1.0 / (p->dy * p->dy), iz2 = 1.0 / (p->dz * p->dz);
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        if (!active(pr, i)) continue;
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+        long nb[6];
+        nb[0] = i - (x > 0 ? 1 : 0);
+        nb[1] = i + (x < nx - 1 ? 1 : 0);
+        nb[2] = i - (y > 0 ? nx : 0);
+        nb[3] = i + (y < ny - 1 ? nx : 0);
+        nb[4] = i - (z > 0 ? (long)nx * ny : 0);
+        nb[5] = i + (z < nz - 1 ? (long)nx * ny : 0);
+        for (int q = 0; q < 6; ++q)
+            if (!active(pr, nb[q])) nb[q] = i;
+        for (int c = 0; c < 3; ++c) {
+            const double mc = m[3 * i + c];
+            h[3 * i + c] += pref * ((m[3 * nb[1] + c] - 2.0 * mc + m[3 * nb[0] + c]) * ix2 +
+                                    (m[3 * nb[3] + c] - 2.0 * mc + m[3 * nb[2] + c]) * iy2 +
+                                    (m[3 * nb[5] + c] - 2.0 * mc + m[3 * nb[4] + c]) * iz2);
+        }
+    }
+}
+
+/* demag_field_add_into (fdm_fields.rs:528-609). */
+static void demag_add(fo_problem *pr, const double *m, double *h) {
+    const fo_params *p = &pr->p;
+    const int nx = p->nx, ny = p->ny, nz = p->nz, px = pr->px, py = pr->py, pz = pr->pz;
+    const long P = pr->P;
+    for (int c = 0; c < 3; ++c) memset(pr->bm[c], 0, sizeof(double) * 2 * P);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+        const long d = (long)x + (long)px * (y + (long)py * z);
+        for (int c = 0; c < 3; ++c) pr->bm[c][2 * d] = active(pr, i) ? m[3 * i + c] * p->ms : 0.0;
+    }
+    for (int c = 0; c < 3; ++c) fo_fft3d(pr->bm[c], px, py, pz, 0);
+    double *const *K = pr->kern;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < P; ++i) {
+        const double mxr = pr->bm[0][2 * i], mxi = pr->bm[0][2 * i + 1];
+        const double myr = pr->bm[1][2 * i], myi = pr->bm[1][2 * i + 1];
+        const double mzr = pr->bm[2][2 * i], mzi = pr->bm[2][2 * i + 1];
+#define CMR(k, ar, ai) (K[k][2 * i] * (ar) - K[k][2 * i + 1] * (ai))
+#define CMI(k, ar, ai) (K[k][2 * i] * (ai) + K[k][2 * i + 1] * (ar))
+        /* components: 0 xx, 1 yy, 2 zz, 3 xy, 4 xz, 5 yz */
+        pr->bh[0][2 * i] = -(CMR(0, mxr, mxi) + CMR(3, myr, myi) + CMR(4, mzr, mzi));
+        pr->bh[0][2 * i + 1] = -(CMI(0, mxr, mxi) + CMI(3, myr, myi) + CMI(4, mzr, mzi));
+        pr->bh[1][2 * i] = -(CMR(3, mxr, mxi) + CMR(1, myr, myi) + CMR(5, mzr, mzi));
+        pr->bh[1][2 * i + 1] = -(CMI(3, mxr, mxi) + CMI(1, myr, myi) + CMI(5, mzr, mzi));
+        pr->bh[2][2 * i] = -(CMR(4, mxr, mxi) + CMR(5, myr, myi) + CMR(2, mzr, mzi));
+        pr->bh[2][2 * i + 1] = -(CMI(4, mxr, mxi) + CMI(5, myr, myi) + CMI(2, mzr, mzi));
+#undef CMR
+#undef CMI
+    }
+    for (int c = 0; c < 3; ++c) fo_fft3d(pr->bh[c], px, py, pz, 1);
+    const double norm = 1.0 / (double)P;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        if (!active(pr, i)) continue;
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+        const long s = (long)x + (long)px * (y + (long)py * z);
+        for (int c = 0; c < 3; ++c) h[3 * i + c] += pr->bh[c][2 * s] * norm;
+    }
+    (void)nz;
+}
+
+/* Uniaxial + cubic anisotropy field (fdm_fields.rs:648-705, 910-1047). The Kc3 term
+ * follows the CUDA reference (native/backends/fdm/src/demag_fp32.cu:295-318). */
+static void anis_field_cell(const fo_problem *pr, const double *m, double *h) {
+    const fo_params *p = &pr->p;
+    const double ms = p->ms > 1e-30 ? p->ms : 1e-30;
+    if (p->has_uniaxial) {
+        const double mu = m[0] * pr->u[0] + m[1] * pr->u[1] + m[2] * pr->u[2];
+        const double cf = 2.0 * p->ku1 / (FO_MU0 * ms) * mu + 4.0 * p->ku2 / (FO_MU0 * ms) * mu * mu * mu;
+        for (int c = 0; c < 3; ++c) h[c] += pr->u[c] * cf;
+    }
+    if (p->has_cubic) {
+        const double m1 = m[0] * pr->c1[0] + m[1] * pr->c1[1] + m[2] * pr->c1[2];
+        const double m2 = m[0] * pr->c2[0] + m[1] * pr->c2[1] + m[2] * pr->c2[2];
+        const double m3 = m[0] * pr->c3[0] + m[1] * pr->c3[1] + m[2] * pr->c3[2];
+        const double pf = 2.0 / (FO_MU0 * ms);
+        const double s1 = m1 * m1, s2 = m2 * m2, s3 = m3 * m3;
+        const double sig = s1 * s2 + s2 * s3 + s1 * s3;
+        const double p3 = -4.0 * p->kc3 / (FO_MU0 * ms);
+        const double g1 = -pf * (p->kc1 * m1 * (s2 + s3) + p->kc2 * m1 * s2 * s3) + p3 * sig * m1 * (s2 + s3);
+        const double g2 = -pf * (p->kc1 * m2 * (s1 + s3) + p->kc2 * m2 * s1 * s3) + p3 * sig * m2 * (s1 + s3);
+        const double g3 = -pf * (p->kc1 * m3 * (s1 + s2) + p->kc2 * m3 * s1 * s2) + p3 * sig * m3 * (s1 + s2);
+        for (int c = 0; c < 3; ++c) h[c] += pr->c1[c] * g1 + pr->c2[c] * g2 + pr->c3[c] * g3;
+    }
+}
+
+/* llg_rhs_from_field (fdm_fields.rs:2151-2162). */
+static void rhs_cell(const fo_params *p, const double *m, const double *h, double *k) {
+    const double gb = p->gamma / (1.0 + p->alpha * p->alpha);
+    const double pr0 = m[1] * h[2] - m[2] * h[1];
+    const double pr1 = m[2] * h[0] - m[0] * h[2];
+    const double pr2 = m[0] * h[1] - m[1] * h[0];
+    const double d0 = m[1] * pr2 - m[2] * pr1;
+    const double d1 = m[2] * pr0 - m[0] * pr2;
+    const double d2 = m[0] * pr1 - m[1] * pr0;
+    const double s = p->disable_precession ? 0.0 : 1.0;
+    k[0] = -gb * (s * pr0 + p->alpha * d0);
+    k[1] = -gb * (s * pr1 + p->alpha * d1);
+    k[2] = -gb * (s * pr2 + p->alpha * d2);
+}
+
+/* Full field evaluation: effective_field_into_ws (fdm_fields.rs:1153-1182). */
+static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h_d, double *h_eff,
+                        double *rhs) {
+    const fo_params *p = &pr->p;
+    const long n3 = 3 * pr->n;
+    memset(h_ex, 0, sizeof(double) * n3);
+    memset(h_d, 0, sizeof(double) * n3);
+    if (p->enable_exchange) exchange_add(pr, m, h_ex);
+    if (p->enable_demag) demag_add(pr, m, h_d);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        double h[3] = {h_ex[3 * i] + h_d[3 * i], h_ex[3 * i + 1] + h_d[3 * i + 1], h_ex[3 * i + 2] + h_d[3 * i + 2]};
+        if (active(pr, i)) {
+            if (p->has_external_field)
+                for (int c = 0; c < 3; ++c) h[c] += p->h_ext[c];
+            anis_field_cell(pr, m + 3 * i, h);
+        }
+        for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
+        if (rhs) rhs_cell(p, m + 3 * i, h, rhs + 3 * i);
+    }
+}
+
+int fo_fields(fo_problem *pr, const double *m_aos, double *h_ex, double *h_demag, double *h_ext,
+              double *h_eff, double *rhs) {
+    const long n3 = 3 * pr->n;
+    double *m = dalloc(n3), *a = dalloc(n3), *b = dalloc(n3), *e = dalloc(n3), *r = dalloc(n3);
+    for (long i = 0; i < pr->n; ++i)
+        for (int c = 0; c < 3; ++c) m[3 * i + c] = active(pr, i) ? m_aos[3 * i + c] : 0.0;
+    eval_fields(pr, m, a, b, e, r);
+    if (h_ex) memcpy(h_ex, a, sizeof(double) * n3);
+    if (h_demag) memcpy(h_demag, b, sizeof(double) * n3);
+    if (h_eff) memcpy(h_eff, e, sizeof(double) * n3);
+    if (rhs) memcpy(rhs, r, sizeof(double) * n3);
+    if (h_ext)
+        for (long i = 0; i < pr->n; ++i)
+            for (int c = 0; c < 3; ++c)
+                h_ext[3 * i + c] = (pr->p.has_external_field && active(pr, i)) ? pr->p.h_ext[c] : 0.0;
+    free(m); free(a); free(b); free(e); free(r);
+    return 0;
+}
+
+static double vmax_norm(const double *v, long n) {
+    double mx = 0.0;
+#pragma omp parallel for reduction(max : mx) schedule(static)
+    for (long i = 0; i < n; ++i) {
+        const double s = sqrt(v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]);
+        if (s > mx) mx = s;
+    }
+    return mx;
+}
+
+/* Energies: C ABI conventions (native/backends/fdm/src/reductions_fp64.cu:123-342,605-642)
+ * and the CPU forms (fdm_fields.rs:349-355, 2168-2273). */
+static void energies(fo_problem *pr, const double *m, const double *h_ex, const double *h_d,
+                     const double *h_eff, const double *rhs, fo_stats *st) {
+    const fo_params *p = &pr->p;
+    const double V = p->dx * p->dy * p->dz;
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const double ix2 = 1.0 / (p->dx * p->dx), iy2 = 1.0 / (p->dy * p->dy), iz2 = 1.0 / (p->dz * p->dz);
+    double epair = 0.0, exf = 0.0, ed = 0.0, eext = 0.0, euni = 0.0, ecub = 0.0, eacpu = 0.0;
+#pragma omp parallel for reduction(+ : epair, exf, ed, eext, euni, ecub, eacpu) schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        if (!active(pr, i)) continue;
+        const double *mi = m + 3 * i;
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+        if (p->enable_exchange) {
+            long nb[3] = {x + 1 < nx ? i + 1 : -1, y + 1 < ny ? i + nx : -1, z + 1 < nz ? i + (long)nx * ny : -1};
+            const double w[3] = {ix2, iy2, iz2};
+            for (int q = 0; q < 3; ++q) {
+                if (nb[q] < 0 || !active(pr, nb[q])) continue;
+                const double a = m[3 * nb[q]] - mi[0], b = m[3 * nb[q] + 1] - mi[1], c = m[3 * nb[q] + 2] - mi[2];
+                epair += p->a_ex * V * (a * a + b * b + c * c) * w[q];
+            }
+            exf += -0.5 * FO_MU0 * p->ms * V * (mi[0] * h_ex[3 * i] + mi[1] * h_ex[3 * i + 1] + mi[2] * h_ex[3 * i + 2]);
+        }
+        if (p->enable_demag)
+            ed += -0.5 * FO_MU0 * p->ms * V * (mi[0] * h_d[3 * i] + mi[1] * h_d[3 * i + 1] + mi[2] * h_d[3 * i + 2]);
+        if (p->has_external_field)
+            eext += -FO_MU0 * p->ms * V * (mi[0] * p->h_ext[0] + mi[1] * p->h_ext[1] + mi[2] * p->h_ext[2]);
+        if (p->has_uniaxial) {
+            const double mu = mi[0] * pr->u[0] + mi[1] * pr->u[1] + mi[2] * pr->u[2];
+            const double s = mu * mu;
+            euni += -V * (p->ku1 * s + p->ku2 * s * s);
+        }
+        if (p->has_cubic) {
+            const double m1 = mi[0] * pr->c1[0] + mi[1] * pr->c1[1] + mi[2] * pr->c1[2];
+            const double m2 = mi[0] * pr->c2[0] + mi[1] * pr->c2[1] + mi[2] * pr->c2[2];
+            const double m3 = mi[0] * pr->c3[0] + mi[1] * pr->c3[1] + mi[2] * pr->c3[2];
+            const double s1 = m1 * m1, s2 = m2 * m2, s3 = m3 * m3;
+            const double sig = s1 * s2 + s2 * s3 + s1 * s3;
+            ecub += V * (p->kc1 * sig + p->kc2 * s1 * s2 * s3 + p->kc3 * sig * sig);
+        }
+        if (p->has_uniaxial || p->has_cubic) {
+            double ha[3] = {0, 0, 0};
+            anis_field_cell(pr, mi, ha);
+            eacpu += -0.5 * FO_MU0 * p->ms * V * (mi[0] * ha[0] + mi[1] * ha[1] + mi[2] * ha[2]);
+        }
+    }
+    st->e_exchange = epair;
+    st->e_exchange_field = exf;
+    st->e_demag = ed;
+    st->e_external = eext;
+    st->e_uniaxial = euni;
+    st->e_cubic = ecub;
+    st->e_anis_cpu = eacpu;
+    st->e_total = epair + ed + eext + euni + ecub;
+    st->max_h_eff = vmax_norm(h_eff, pr->n);
+    st->max_h_demag = p->enable_demag ? vmax_norm(h_d, pr->n) : 0.0;
+    st->max_rhs = vmax_norm(rhs, pr->n);
+}
+
+int fo_observe(fo_problem *pr, fo_stats *st) {
+    const long n3 = 3 * pr->n;
+    double *a = dalloc(n3), *b = dalloc(n3), *r = dalloc(n3);
+    eval_fields(pr, pr->m, a, b, pr->heff, r);
+    memset(st, 0, sizeof(*st));
+    energies(pr, pr->m, a, b, pr->heff, r, st);
+    st->step = pr->step;
+    st->time = pr->t;
+    free(a); free(b); free(r);
+    return 0;
+}
+
+static void rhs_of(fo_problem *pr, const double *m, double *k) {
+    const long n3 = 3 * pr->n;
+    double *a = dalloc(n3), *b = dalloc(n3);
+    eval_fields(pr, m, a, b, pr->heff, k);
+    free(a); free(b);
+}
+
+/* out = normalize(m0 + dt * sum_j c_j k_j) (vector::normalized, zero stays zero). */
+static void stage_combine(const fo_problem *pr, double *out, const double *m0, int nk, double *const *ks,
+                          const double *cs, double dt) {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        double v[3];
+        for (int c = 0; c < 3; ++c) {
+            double acc = 0.0;
+            for (int j = 0; j < nk; ++j) acc += cs[j] * ks[j][3 * i + c];
+            v[c] = m0[3 * i + c] + acc * dt;
+        }
+        const double nn = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        const double inv = nn > 0.0 ? 1.0 / nn : 0.0;
+        for (int c = 0; c < 3; ++c) out[3 * i + c] = v[c] * inv;
+    }
+}
+
+/* Dormand-Prince 5(4) tableau (fdm_integrators.rs:441-468). */
+static const double DP_A[6][5] = {
+    {1.0 / 5.0, 0, 0, 0, 0},
+    {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0},
+    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0},
+    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0},
+    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0},
+    {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0}};
+static const double DP_B6 = 11.0 / 84.0;
+static const double DP_E[7] = {71.0 / 57600.0, 0.0, -71.0 / 16695.0, 71.0 / 1920.0, -17253.0 / 339200.0,
+                               22.0 / 525.0, -1.0 / 40.0};
+
+/* max error norm (fdm_integrators.rs:828-873; native/backends/fdm/src/llg_dp45_fp32.cu:108-128,175-184). */
+static double dp45_error(const fo_problem *pr, double dt) {
+    const fo_params *p = &pr->p;
+    double mx = 0.0;
+#pragma omp parallel for reduction(max : mx) schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        double e[3] = {0, 0, 0};
+        for (int s = 0; s < 7; ++s)
+            for (int c = 0; c < 3; ++c) e[c] += DP_E[s] * pr->k[s][3 * i + c];
+        const double en = dt * sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        double v = en;
+        if (p->dp45_norm == 1 && p->rtol > 0.0) {
+            const double *m0 = pr->m0 + 3 * i;
+            double yn = sqrt(m0[0] * m0[0] + m0[1] * m0[1] + m0[2] * m0[2]);
+            if (yn < 1e-30) yn = 1e-30;
+            v = en / (p->max_error + p->rtol * yn);
+        }
+        if (v > mx) mx = v;
+    }
+    return mx;
+}
+
+static double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+int fo_step(fo_problem *pr, double dt, fo_stats *st) {
+    const fo_params *p = &pr->p;
+    const long n3 = 3 * pr->n;
+    memcpy(pr->m0, pr->m, sizeof(double) * n3);
+    double rejected = 0.0, suggested = 0.0;
+    if (p->integrator == 1) { /* Heun: fdm_integrators.rs:87-153 */
+        rhs_of(pr, pr->m0, pr->k[0]);
+        const double c1[1] = {1.0};
+        stage_combine(pr, pr->mst, pr->m0, 1, pr->k, c1, dt);
+        rhs_of(pr, pr->mst, pr->k[1]);
+        const double c2[2] = {0.5, 0.5};
+        stage_combine(pr, pr->m, pr->m0, 2, pr->k, c2, dt);
+    } else if (p->integrator == 4) { /* RK4: fdm_integrators.rs:155-262 */
+        rhs_of(pr, pr->m0, pr->k[0]);
+        const double h[1] = {0.5}, f[1] = {1.0};
+        stage_combine(pr, pr->mst, pr->m0, 1, &pr->k[0], h, dt);
+        rhs_of(pr, pr->mst, pr->k[1]);
+        stage_combine(pr, pr->mst, pr->m0, 1, &pr->k[1], h, dt);
+        rhs_of(pr, pr->mst, pr->k[2]);
+        stage_combine(pr, pr->mst, pr->m0, 1, &pr->k[2], f, dt);
+        rhs_of(pr, pr->mst, pr->k[3]);
+        const double w[4] = {1.0 / 6.0, 2.0 / 6.0, 2.0 / 6.0, 1.0 / 6.0};
+        stage_combine(pr, pr->m, pr->m0, 4, pr->k, w, dt);
+    } else if (p->integrator == 2) { /* DP45 + FSAL: fdm_integrators.rs:429-681 (CPU norm) or
+                                        llg_dp45_fp32.cu:188-342 (ABI norm) */
+        const int cpu = p->dp45_norm == 1;
+        if (cpu) dt = clampd(dt, p->dt_min, p->dt_max);
+        for (;;) {
+            if (pr->fsal_valid) memcpy(pr->k[0], pr->fsal, sizeof(double) * n3);
+            else rhs_of(pr, pr->m0, pr->k[0]);
+            for (int s = 0; s < 5; ++s) {
+                stage_combine(pr, pr->mst, pr->m0, s + 1, pr->k, DP_A[s], dt);
+                rhs_of(pr, pr->mst, pr->k[s + 1]);
+            }
+            double bw[6] = {DP_A[5][0], DP_A[5][1], DP_A[5][2], DP_A[5][3], DP_A[5][4], DP_B6};
+            stage_combine(pr, pr->mst, pr->m0, 6, pr->k, bw, dt);
+            rhs_of(pr, pr->mst, pr->k[6]);
+            const double err = dp45_error(pr, dt);
+            const double thr = (cpu && p->rtol > 0.0) ? 1.0 : p->max_error;
+            if (err <= thr || dt <= p->dt_min) {
+                memcpy(pr->m, pr->mst, sizeof(double) * n3);
+                memcpy(pr->fsal, pr->k[6], sizeof(double) * n3);
+                pr->fsal_valid = 1;
+                if (cpu) {
+                    double ratio = p->headroom * pow(thr / (err > 1e-30 ? err : 1e-30), 0.2);
+                    ratio = clampd(ratio, p->shrink_limit, p->growth_limit);
+                    suggested = clampd(dt * ratio, p->dt_min, p->dt_max);
+                } else {
+                    suggested = err > 0.0 ? clampd(p->headroom * dt * pow(p->max_error / err, 0.2), p->dt_min, p->dt_max)
+                                          : p->dt_max;
+                }
+                break;
+            }
+            rejected += 1.0;
+            if (cpu) {
+                double ratio = clampd(p->headroom * pow(thr / err, 0.2), p->shrink_limit, p->growth_limit);
+                dt = clampd(dt * ratio, p->dt_min, p->dt_max);
+            } else {
+                dt = clampd(p->headroom * dt * pow(p->max_error / err, 0.2), p->dt_min, p->dt_max);
+            }
+            pr->fsal_valid = 0;
+        }
+    } else {
+        return -1;
+    }
+    pr->t += dt;
+    pr->step += 1.0;
+    fo_observe(pr, st);
+    st->dt_used = dt;
+    st->suggested_next_dt = suggested;
+    st->rejected_attempts = rejected;
+    return 0;
+}
+
+/* Direct real-space sum H_i = -sum_j N(r_i - r_j) Ms m_j over the padded tensor. */
+int fo_demag_direct(fo_problem *pr, const double *m_aos, double *h_demag) {
+    const fo_params *p = &pr->p;
+    const int nx = p->nx, ny = p->ny, nz = p->nz, px = 2 * nx, py = 2 * ny, pz = 2 * nz;
+    const long plen = (long)px * py * pz;
+    double *kr = dalloc(6 * plen);
+    if (!kr) return -2;
+    fo_newell_kernels(nx, ny, nz, p->dx, p->dy, p->dz, kr);
+    const long n = pr->n;
+#pragma omp parallel for schedule(dynamic)
+    for (long i = 0; i < n; ++i) {
+        double h[3] = {0, 0, 0};
+        if (active(pr, i)) {
+            const int xi = (int)(i % nx), yi = (int)((i / nx) % ny), zi = (int)(i / ((long)nx * ny));
+            for (long j = 0; j < n; ++j) {
+                if (!active(pr, j)) continue;
+                const int xj = (int)(j % nx), yj = (int)((j / nx) % ny), zj = (int)(j / ((long)nx * ny));
+                const int ddx = (xi - xj + px) % px, ddy = (yi - yj + py) % py, ddz = (zi - zj + pz) % pz;
+                const long q = (long)ddx + (long)px * (ddy + (long)py * ddz);
+                const double Mx = p->ms * m_aos[3 * j], My = p->ms * m_aos[3 * j + 1], Mz = p->ms * m_aos[3 * j + 2];
+                h[0] -= kr[q] * Mx + kr[3 * plen + q] * My + kr[4 * plen + q] * Mz;
+                h[1] -= kr[3 * plen + q] * Mx + kr[plen + q] * My + kr[5 * plen + q] * Mz;
+                h[2] -= kr[4 * plen + q] * Mx + kr[5 * plen + q] * My + kr[2 * plen + q] * Mz;
+            }
+        }
+        for (int c = 0; c < 3; ++c) h_demag[3 * i + c] = h[c];
+    }
+    free(kr);
+    return 0;
+}

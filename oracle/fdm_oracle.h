@@ -1,0 +1,97 @@
+/*
+ * fdm_oracle.h -- FP64 CPU restatement of the reference FDM LLG path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the parity checker for the CUDA
+ * engine and the timed CPU baseline; the product library never links it.
+ * It restates, in plain C with OpenMP, the algorithms of
+ *   crates/fullmag-fdm-demag/src/newell.rs      (Newell f/g, 27-point stencil, octants)
+ *   crates/fullmag-engine/src/fdm_fft.rs        (zero-padded FFT convolution)
+ *   crates/fullmag-engine/src/fdm_fields.rs     (exchange, demag, local terms, RHS, energies)
+ *   crates/fullmag-engine/src/fdm_integrators.rs (Heun, RK4, Dormand-Prince 5(4))
+ * and the step/stat semantics of native/backends/fdm (the C ABI this engine replaces).
+ * The reference's FFT comes from rustfft 6.4.1 (Cargo.lock:3647-3649), which is not
+ * in the reference tree; fo_fft1d is an own mixed-radix FFT validated against numpy.fft.
+ */
+#ifndef FDM_ORACLE_H
+#define FDM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Newell tensor ---- */
+double fo_newell_f(double x, double y, double z);
+double fo_newell_g(double x, double y, double z);
+
+/* Real-space tensors on the (2nx,2ny,2nz) padded grid, out = 6 arrays
+ * [xx, yy, zz, xy, xz, yz] of 8*nx*ny*nz doubles each. */
+int fo_newell_kernels(int nx, int ny, int nz, double dx, double dy, double dz, double *out);
+
+/* Spectra as handed to the C ABI: 6 arrays of 2*P interleaved complex values.
+ * thin_film_2d != 0 (requires nz == 1) uses P = 2nx*2ny, else P = 2nx*2ny*2nz. */
+int fo_newell_spectra(int nx, int ny, int nz, double dx, double dy, double dz,
+                      int thin_film_2d, double *out);
+
+/* ---- FFT (interleaved complex, unnormalised; inverse uses e^{+i}) ---- */
+int fo_fft1d(double *data, int n, int inverse);
+int fo_fft3d(double *data, int px, int py, int pz, int inverse);
+
+/* ---- Problem ---- */
+typedef struct {
+    int32_t nx, ny, nz;
+    int32_t integrator;          /* 1 Heun, 2 DP45, 4 RK4 (ABI values) */
+    double dx, dy, dz;
+    double ms, a_ex, alpha, gamma;
+    int32_t enable_exchange, enable_demag, has_external_field, disable_precession;
+    double h_ext[3];
+    int32_t has_uniaxial;
+    int32_t has_cubic;
+    double ku1, ku2, u_axis[3];
+    double kc1, kc2, kc3, c1[3], c2[3];
+    /* adaptive control */
+    double max_error, dt_min, dt_max, headroom;
+    double rtol, growth_limit, shrink_limit;
+    int32_t dp45_norm;           /* 0: ABI absolute max-norm, 1: CPU mixed atol/rtol norm */
+    int32_t pad0;
+    const uint8_t *active_mask;  /* optional, copied at create */
+} fo_params;
+
+typedef struct {
+    double step, time, dt_used, suggested_next_dt;
+    double e_exchange;           /* pair sum A V |dm|^2 / d^2 (equals -1/2 mu0 Ms V m.H_ex) */
+    double e_exchange_field;     /* -1/2 mu0 Ms V sum m.H_ex (CPU reference form) */
+    double e_demag;              /* -1/2 mu0 Ms V sum m.H_d */
+    double e_external;           /* -mu0 Ms V sum m.H_ext */
+    double e_uniaxial;           /* -V sum (Ku1 (m.u)^2 + Ku2 (m.u)^4)  (C ABI convention) */
+    double e_cubic;              /* V sum (Kc1 s + Kc2 p + Kc3 s^2)    (C ABI convention) */
+    double e_anis_cpu;           /* -1/2 mu0 Ms V sum m.H_anis          (CPU reference convention) */
+    double e_total;              /* e_exchange + e_demag + e_external + e_uniaxial + e_cubic */
+    double max_h_eff, max_h_demag, max_rhs;
+    double rejected_attempts;
+} fo_stats;
+
+typedef struct fo_problem fo_problem;
+
+fo_problem *fo_create(const fo_params *p, const double *m0_aos);
+void fo_destroy(fo_problem *pr);
+int fo_set_m(fo_problem *pr, const double *m_aos);
+int fo_get_m(const fo_problem *pr, double *m_aos);
+/* Fields at an arbitrary state (AoS in/out, any pointer may be NULL). */
+int fo_fields(fo_problem *pr, const double *m_aos, double *h_ex, double *h_demag,
+              double *h_ext, double *h_eff, double *rhs);
+/* Stats of the current state (fields recomputed). */
+int fo_observe(fo_problem *pr, fo_stats *st);
+/* One accepted step with the ABI semantics of the configured integrator. */
+int fo_step(fo_problem *pr, double dt, fo_stats *st);
+/* Demag field by direct O(N^2) real-space Newell sum (FFT-independent check). */
+int fo_demag_direct(fo_problem *pr, const double *m_aos, double *h_demag);
+
+int fo_num_threads(void);
+void fo_set_num_threads(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,233 @@
+"""ctypes front end of the FP64 oracle (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
+this module, as the checker.  The product path never imports it.  The C code it
+wraps restates crates/fullmag-engine (fields, integrators) and
+crates/fullmag-fdm-demag (Newell tensor) of the reference in FP64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libfdm_oracle.so"
+
+HEUN, DP45, RK4 = 1, 2, 4
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with the committed Makefile (gcc, OpenMP)."""
+    src = HERE / "fdm_oracle.c"
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("integrator", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+        ("ms", C.c_double), ("a_ex", C.c_double), ("alpha", C.c_double), ("gamma", C.c_double),
+        ("enable_exchange", C.c_int32), ("enable_demag", C.c_int32),
+        ("has_external_field", C.c_int32), ("disable_precession", C.c_int32),
+        ("h_ext", C.c_double * 3),
+        ("has_uniaxial", C.c_int32), ("has_cubic", C.c_int32),
+        ("ku1", C.c_double), ("ku2", C.c_double), ("u_axis", C.c_double * 3),
+        ("kc1", C.c_double), ("kc2", C.c_double), ("kc3", C.c_double),
+        ("c1", C.c_double * 3), ("c2", C.c_double * 3),
+        ("max_error", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double),
+        ("headroom", C.c_double), ("rtol", C.c_double), ("growth_limit", C.c_double),
+        ("shrink_limit", C.c_double),
+        ("dp45_norm", C.c_int32), ("pad0", C.c_int32),
+        ("active_mask", C.c_void_p),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "step", "time", "dt_used", "suggested_next_dt",
+        "e_exchange", "e_exchange_field", "e_demag", "e_external", "e_uniaxial", "e_cubic",
+        "e_anis_cpu", "e_total", "max_h_eff", "max_h_demag", "max_rhs", "rejected_attempts")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = C.CDLL(str(path))
+        dp = C.POINTER(C.c_double)
+        L.fo_newell_f.restype = C.c_double
+        L.fo_newell_f.argtypes = [C.c_double] * 3
+        L.fo_newell_g.restype = C.c_double
+        L.fo_newell_g.argtypes = [C.c_double] * 3
+        L.fo_newell_kernels.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [dp]
+        L.fo_newell_spectra.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int, dp]
+        L.fo_fft1d.argtypes = [dp, C.c_int, C.c_int]
+        L.fo_fft3d.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.fo_create.restype = C.c_void_p
+        L.fo_create.argtypes = [C.POINTER(Params), dp]
+        L.fo_destroy.argtypes = [C.c_void_p]
+        L.fo_set_m.argtypes = [C.c_void_p, dp]
+        L.fo_get_m.argtypes = [C.c_void_p, dp]
+        L.fo_fields.argtypes = [C.c_void_p] + [dp] * 6
+        L.fo_observe.argtypes = [C.c_void_p, C.POINTER(Stats)]
+        L.fo_step.argtypes = [C.c_void_p, C.c_double, C.POINTER(Stats)]
+        L.fo_demag_direct.argtypes = [C.c_void_p, dp, dp]
+        L.fo_num_threads.restype = C.c_int
+        L.fo_set_num_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def newell_f(x, y, z):
+    return lib().fo_newell_f(x, y, z)
+
+
+def newell_g(x, y, z):
+    return lib().fo_newell_g(x, y, z)
+
+
+def newell_kernels(nx, ny, nz, dx, dy, dz):
+    """Real-space padded tensors, shape (6, 2nz, 2ny, 2nx): xx yy zz xy xz yz."""
+    out = np.zeros(6 * 8 * nx * ny * nz)
+    rc = lib().fo_newell_kernels(nx, ny, nz, dx, dy, dz, _dp(out))
+    assert rc == 0
+    return out.reshape(6, 2 * nz, 2 * ny, 2 * nx)
+
+
+def newell_spectra(nx, ny, nz, dx, dy, dz, thin_film_2d=False):
+    """Interleaved complex spectra as the C ABI receives them: shape (6, 2P)."""
+    P = 4 * nx * ny if thin_film_2d else 8 * nx * ny * nz
+    out = np.zeros(6 * 2 * P)
+    rc = lib().fo_newell_spectra(nx, ny, nz, dx, dy, dz, int(thin_film_2d), _dp(out))
+    assert rc == 0
+    return out.reshape(6, 2 * P)
+
+
+def fft1d(x, inverse=False):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128)).copy()
+    buf = a.view(np.float64)
+    assert lib().fo_fft1d(_dp(buf), a.size, int(inverse)) == 0
+    return a
+
+
+def fft3d(x, inverse=False):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128)).copy()
+    pz, py, px = a.shape
+    assert lib().fo_fft3d(_dp(a.view(np.float64)), px, py, pz, int(inverse)) == 0
+    return a
+
+
+class Problem:
+    """FP64 oracle problem.  Arrays are AoS (n, 3)."""
+
+    def __init__(self, *, nx, ny, nz, dx, dy, dz, ms, a_ex, alpha, gamma=2.211e5,
+                 integrator=HEUN, enable_exchange=True, enable_demag=True, h_ext=None,
+                 disable_precession=False, ku1=None, ku2=0.0, u_axis=(0, 0, 1),
+                 kc1=None, kc2=0.0, kc3=0.0, c1=(1, 0, 0), c2=(0, 1, 0),
+                 max_error=1e-5, dt_min=1e-18, dt_max=1e-10, headroom=0.8, rtol=0.0,
+                 growth_limit=float("inf"), shrink_limit=0.0, dp45_norm=0,
+                 active_mask=None, m0=None):
+        p = Params()
+        p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
+        p.dx, p.dy, p.dz = dx, dy, dz
+        p.ms, p.a_ex, p.alpha, p.gamma = ms, a_ex, alpha, gamma
+        p.enable_exchange, p.enable_demag = int(enable_exchange), int(enable_demag)
+        p.has_external_field = int(h_ext is not None)
+        p.disable_precession = int(disable_precession)
+        p.h_ext[:] = list(h_ext) if h_ext is not None else [0.0, 0.0, 0.0]
+        p.has_uniaxial = int(ku1 is not None)
+        p.ku1, p.ku2 = (ku1 or 0.0), ku2
+        p.u_axis[:] = list(u_axis)
+        p.has_cubic = int(kc1 is not None)
+        p.kc1, p.kc2, p.kc3 = (kc1 or 0.0), kc2, kc3
+        p.c1[:] = list(c1)
+        p.c2[:] = list(c2)
+        p.max_error, p.dt_min, p.dt_max, p.headroom = max_error, dt_min, dt_max, headroom
+        p.rtol, p.growth_limit, p.shrink_limit = rtol, growth_limit, shrink_limit
+        p.dp45_norm = dp45_norm
+        self._mask = None
+        if active_mask is not None:
+            self._mask = np.ascontiguousarray(active_mask, dtype=np.uint8)
+            p.active_mask = self._mask.ctypes.data
+        self.n = nx * ny * nz
+        self.shape = (nz, ny, nx)
+        self.params = p
+        m0a = None if m0 is None else np.ascontiguousarray(m0, dtype=np.float64).reshape(-1)
+        self._h = lib().fo_create(C.byref(p), _dp(m0a))
+        if not self._h:
+            raise RuntimeError("oracle create failed")
+
+    def close(self):
+        if self._h:
+            lib().fo_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_m(self, m):
+        a = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
+        lib().fo_set_m(self._h, _dp(a))
+
+    def get_m(self):
+        a = np.zeros(3 * self.n)
+        lib().fo_get_m(self._h, _dp(a))
+        return a.reshape(self.n, 3)
+
+    def fields(self, m=None):
+        if m is None:
+            m = self.get_m()
+        m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
+        outs = {k: np.zeros(3 * self.n) for k in ("h_ex", "h_demag", "h_ext", "h_eff", "rhs")}
+        lib().fo_fields(self._h, _dp(m), _dp(outs["h_ex"]), _dp(outs["h_demag"]),
+                        _dp(outs["h_ext"]), _dp(outs["h_eff"]), _dp(outs["rhs"]))
+        return {k: v.reshape(self.n, 3) for k, v in outs.items()}
+
+    def observe(self):
+        st = Stats()
+        lib().fo_observe(self._h, C.byref(st))
+        return st.as_dict()
+
+    def step(self, dt):
+        st = Stats()
+        rc = lib().fo_step(self._h, dt, C.byref(st))
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed ({rc})")
+        return st.as_dict()
+
+    def demag_direct(self, m=None):
+        if m is None:
+            m = self.get_m()
+        m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
+        out = np.zeros(3 * self.n)
+        lib().fo_demag_direct(self._h, _dp(m), _dp(out))
+        return out.reshape(self.n, 3)
+
+
+def set_threads(n: int):
+    lib().fo_set_num_threads(int(n))
+
+
+def threads() -> int:
+    return lib().fo_num_threads()
