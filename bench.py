@@ -1,0 +1,331 @@
+"""Throughput of the FDM LLG step on one GB300 (cell-steps/s), one JSON line.
+
+Default workload: the large 3-D roofline volume -- 256x256x64 cells of 2 nm cubes,
+Ms = 1.4e6 A/m, A = 2.1e-11 J/m, cubic K1 = -4.8e4 J/m^3 along (100)/(010)/(001),
+alpha = 0.01, open boundaries, m0 = seeded random unit vectors smoothed by three
+6-neighbour box-filter passes and renormalised, RK4 with dt = 2e-14 s.  Inputs are
+synthetic (seeded) with exactly these shapes and parameters; the state plus the
+spectra (~0.9 GB) exceed the 129 MB L2, so no extra flush is needed between steps.
+
+value : device time (CUDA events on the engine's stream) of K steps through
+        fullmag_fdm_backend_step with the state resident in HBM.
+e2e   : the same metric, wall clock, through the C ABI with host buffers:
+        upload_magnetization_f64 (AoS host array) + K x step (stats to the host
+        every step) + copy_field_f64(M) back to the host.
+--impl reference : the FP64 C restatement of the reference CPU engine (oracle/),
+        OpenMP over all host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+MU0 = 4e-7 * np.pi
+METRIC = "cell-steps/s per GB300 (fused FP32 engine, FP64 Newell/reductions)"
+
+# Algorithmic bytes per cell-step, compulsory-traffic model v1 (fused 3-pass design):
+# T(a) = 12(1+a) + 12 + 4S + K + 12 + 12 per evaluation with a earlier stages,
+# S = 24 (nx+1)/nx, K = kernel bytes per cell; RK4 = T(0) + 3T(1) + 72.
+def model_bytes_per_cell_step(nx, ny, nz, integrator="rk4"):
+    S = 24.0 * (nx + 1) / nx
+    n = nx * ny * nz
+    if nz == 1:
+        K = 4 * 4.0 * (nx + 1) * (ny + 1) / n
+    else:
+        K = 6 * 4.0 * (nx + 1) * (ny + 1) * (nz + 1) / n
+
+    def T(a):
+        return 12 * (1 + a) + 12 + 4 * S + K + 12 + 12
+
+    if integrator == "rk4":
+        return T(0) + 3 * T(1) + 72
+    if integrator == "heun":
+        return T(0) + T(1) + 48
+    return sum(T(a) for a in (1, 2, 3, 4, 5, 5)) + 72
+
+
+WORKLOADS = {
+    "volume_256x256x64_rk4": dict(nx=256, ny=256, nz=64, d=2e-9, ms=1.4e6, a_ex=2.1e-11, alpha=0.01,
+                                  kc1=-4.8e4, dt=2e-14, integrator="rk4", seed=3),
+    "box_64x32x4_heun": dict(nx=64, ny=32, nz=4, d=4e-9, ms=8e5, a_ex=1.3e-11, alpha=0.5,
+                             b_mt=(10.0, 5.0, 0.0), dt=5e-14, integrator="heun", seed=0),
+    "film_256x64x1_rk4": dict(nx=256, ny=64, nz=1, d=4e-9, ms=8e5, a_ex=1.3e-11, alpha=0.05,
+                              b_mt=(5.0, 0.0, 0.0), dt=5e-14, integrator="rk4", seed=2),
+}
+DEFAULT_WORKLOAD = "volume_256x256x64_rk4"
+
+
+def smoothed_random_unit(nx, ny, nz, seed, passes=3):
+    rng = np.random.default_rng(seed)
+    m = rng.standard_normal((nz, ny, nx, 3))
+    m /= np.linalg.norm(m, axis=-1, keepdims=True)
+    for _ in range(passes):
+        acc = m.copy()
+        cnt = np.ones((nz, ny, nx, 1))
+        for ax in (0, 1, 2):
+            for sh in (1, -1):
+                r = np.roll(m, sh, axis=ax)
+                valid = np.ones((nz, ny, nx, 1))
+                idx = [slice(None)] * 4
+                idx[ax] = 0 if sh == 1 else -1
+                r[tuple(idx)] = 0.0
+                valid[tuple(idx)] = 0.0
+                acc += r
+                cnt += valid
+        m = acc / cnt
+        m /= np.linalg.norm(m, axis=-1, keepdims=True)
+    return m.reshape(-1, 3)
+
+
+def plan_kwargs(w):
+    from fullmag_gb300 import _abi
+    kw = dict(nx=w["nx"], ny=w["ny"], nz=w["nz"], dx=w["d"], dy=w["d"], dz=w["d"], ms=w["ms"],
+              a_ex=w["a_ex"], alpha=w["alpha"], gamma=2.211e5,
+              m0=smoothed_random_unit(w["nx"], w["ny"], w["nz"], w["seed"]))
+    if "b_mt" in w:
+        kw["h_ext"] = tuple(b * 1e-3 / MU0 for b in w["b_mt"])
+    if "kc1" in w:
+        kw.update(kc1=w["kc1"], c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0))
+    integ = {"rk4": _abi.INTEGRATOR_RK4, "heun": _abi.INTEGRATOR_HEUN}[w["integrator"]]
+    return kw, integ
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(w, threads):
+    """FP64 oracle (C restatement of the reference CPU engine) on a bounded sample:
+    one step of the same physics on a grid with 1/8 of the cells (halved per axis
+    for 3-D), after one warm-up step."""
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(threads)
+    nx, ny, nz = w["nx"], w["ny"], w["nz"]
+    if nz > 1:
+        sx, sy, sz = max(nx // 2, 1), max(ny // 2, 1), max(nz // 2, 1)
+    else:
+        sx, sy, sz = nx, ny, nz
+    ws = dict(w, nx=sx, ny=sy, nz=sz)
+    kw, _ = plan_kwargs(ws)
+    integ = {"rk4": O.RK4, "heun": O.HEUN}[w["integrator"]]
+    pr = O.Problem(**kw, integrator=integ)
+    pr.step(w["dt"])
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        pr.step(w["dt"])
+        steps += 1
+        if time.perf_counter() - t0 > 10.0 or steps >= 3:
+            break
+    el = time.perf_counter() - t0
+    pr.close()
+    return {"value": sx * sy * sz * steps / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} {w['integrator'].upper()} step(s) of {sx}x{sy}x{sz} (same physics, FP64, "
+                      f"after 1 warm-up step), wall clock"}
+
+
+def run_reference(args, w, name, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(threads)
+    nx, ny, nz = w["nx"], w["ny"], w["nz"]
+    sx, sy, sz = (max(nx // 2, 1), max(ny // 2, 1), max(nz // 2, 1)) if nz > 1 else (nx, ny, nz)
+    kw, _ = plan_kwargs(dict(w, nx=sx, ny=sy, nz=sz))
+    integ = {"rk4": O.RK4, "heun": O.HEUN}[w["integrator"]]
+    pr = O.Problem(**kw, integrator=integ)
+    for _ in range(args.warmup):
+        pr.step(w["dt"])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pr.step(w["dt"])
+    el = time.perf_counter() - t0
+    cells = sx * sy * sz
+    v = cells * args.steps / el
+    out = {"metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+           "impl": "reference",
+           "config": {"workload": name, "sample_grid": [sx, sy, sz], "threads": threads},
+           "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                            "sample": f"{args.steps} step(s) of {sx}x{sy}x{sz} per timed step set"},
+           "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w, args.workload, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    os.environ["FULLMAG_FDM_GPU_INDEX"] = str(local if world > 1 else int(os.environ.get("FULLMAG_FDM_GPU_INDEX", "0")))
+    torch.cuda.set_device(int(os.environ["FULLMAG_FDM_GPU_INDEX"]))
+
+    from fullmag_gb300 import FdmBackend, _abi
+    from fullmag_gb300.build import build
+    build()
+    kw, integ = plan_kwargs(w)
+    n = w["nx"] * w["ny"] * w["nz"]
+    dt = w["dt"]
+
+    be = FdmBackend(**kw, integrator=integ)
+    stream = torch.cuda.ExternalStream(be.stream())
+    for _ in range(args.warmup):
+        be.step(dt)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(int(os.environ["FULLMAG_FDM_GPU_INDEX"]))
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = be.launch_count()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        st = be.step(dt)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    launches = be.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    value = world * n * args.steps / (ms * 1e-3)
+
+    # ---- e2e through the C ABI with host buffers ----
+    m_host = np.ascontiguousarray(kw["m0"], dtype=np.float64)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    be.upload(m_host)
+    for _ in range(args.steps):
+        be.step(dt)
+    m_out = be.copy_field(_abi.OBSERVABLE_M)
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = world * n * args.steps / t_e2e
+    h2d = 24.0 * n / args.steps
+    d2h = 24.0 * n / args.steps + 120.0
+
+    peak, peak_kind = load_peaks()
+    bpc = model_bytes_per_cell_step(w["nx"], w["ny"], w["nz"], w["integrator"])
+    achieved = bpc * n / (ms_per_step * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "grid": [w["nx"], w["ny"], w["nz"]], "integrator": w["integrator"],
+                   "dt": dt, "padded": list(be.fft_shape()), "parallelism": "replicas" if world > 1 else "single",
+                   "l2_flush": "none needed: working set > 129 MB L2"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "note": f"whole step; model v1 {bpc:.1f} B/cell-step; peak {peak_kind}"},
+        "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "final_total_energy_J": st["total_energy_joules"],
+        "m_norm_max_dev": float(np.abs(np.linalg.norm(m_out, axis=1) - 1).max()),
+    }
+    be.close()
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,253 @@
+"""Python mirror of the reference's safe FDM wrapper.
+
+Mirrors ``NativeFdmBackend`` (crates/fullmag-runner/src/native_fdm.rs:50-970): build a
+``fullmag_fdm_plan_desc`` from plan parameters, create the backend, check
+``last_error`` on a non-NULL handle (native_fdm.rs:477-492), step with interrupt
+support (native_fdm.rs:516-569), copy fields as AoS (n, 3) arrays, upload and
+refresh (native_fdm.rs:829-857) and destroy.  Everything runs through the C ABI of
+``libfullmag_fdm.so``; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import PlanDesc, StepStats
+
+MU0 = 4.0e-7 * np.pi
+DEFAULT_GAMMA = 2.211e5
+
+_LIB = None
+
+
+class FdmError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{message} (code {code})")
+        self.code = code
+
+
+class FdmInterrupted(FdmError):
+    pass
+
+
+def library_path() -> Path:
+    env = os.environ.get("FULLMAG_FDM_LIB")
+    if env:
+        return Path(env)
+    return Path(__file__).resolve().parent / "_build" / "libfullmag_fdm.so"
+
+
+def load_library(build_if_missing: bool = True) -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not path.exists() and build_if_missing:
+            from .build import build
+            build()
+        if not path.exists():
+            raise FdmError(_abi.ERR_INTERNAL, f"libfullmag_fdm.so not found at {path}; run fullmag_gb300.build")
+        _LIB = _abi.bind(C.CDLL(str(path)))
+    return _LIB
+
+
+library = load_library
+
+
+def _dptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class FdmBackend:
+    """One FDM problem on the GPU behind the C ABI.
+
+    Parameters mirror ``FdmPlanIR`` fields the reference wrapper reads.  ``spectra`` is
+    an optional (6, 2P) array of interleaved FP64 Newell spectra (xx yy zz xy xz yz)
+    exactly as the reference computes them on the host; when omitted the engine
+    builds the tensor on the GPU.
+    """
+
+    def __init__(self, *, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
+                 ms: float, a_ex: float, alpha: float, gamma: float = DEFAULT_GAMMA,
+                 m0: np.ndarray, integrator: int = _abi.INTEGRATOR_HEUN,
+                 enable_exchange: bool = True, enable_demag: bool = True,
+                 h_ext: Optional[Sequence[float]] = None, disable_precession: bool = False,
+                 ku1: Optional[float] = None, ku2: float = 0.0, u_axis=(0.0, 0.0, 1.0),
+                 kc1: Optional[float] = None, kc2: float = 0.0, kc3: float = 0.0,
+                 c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0),
+                 active_mask: Optional[np.ndarray] = None,
+                 spectra: Optional[np.ndarray] = None,
+                 adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
+                 adaptive_dt_max: float = 0.0, adaptive_headroom: float = 0.0,
+                 precision: int = _abi.PRECISION_SINGLE):
+        self.lib = load_library()
+        self.n = nx * ny * nz
+        self.shape = (nz, ny, nx)
+        p = PlanDesc()
+        p.grid.nx, p.grid.ny, p.grid.nz = nx, ny, nz
+        p.grid.dx, p.grid.dy, p.grid.dz = dx, dy, dz
+        p.material.saturation_magnetisation = ms
+        p.material.exchange_stiffness = a_ex
+        p.material.damping = alpha
+        p.material.gyromagnetic_ratio = gamma
+        p.precision = precision
+        p.integrator = integrator
+        p.disable_precession = int(disable_precession)
+        p.enable_exchange = int(enable_exchange)
+        p.enable_demag = int(enable_demag)
+        p.has_external_field = int(h_ext is not None)
+        p.external_field_am[:] = list(h_ext) if h_ext is not None else [0.0, 0.0, 0.0]
+        p.has_uniaxial_anisotropy = int(ku1 is not None)
+        p.uniaxial_anisotropy_constant = ku1 or 0.0
+        p.uniaxial_anisotropy_k2 = ku2
+        p.anisotropy_axis[:] = list(u_axis)
+        p.has_cubic_anisotropy = int(kc1 is not None)
+        p.cubic_Kc1, p.cubic_Kc2, p.cubic_Kc3 = (kc1 or 0.0), kc2, kc3
+        p.cubic_axis1[:] = list(c1)
+        p.cubic_axis2[:] = list(c2)
+        p.sot_sigma[:] = [0.0, 0.0, 1.0]
+        p.sot_thickness = 1e-9
+        p.oersted_axis[:] = [0.0, 0.0, 1.0]
+        keep = []
+        if spectra is not None and enable_demag:
+            sp = np.ascontiguousarray(spectra, dtype=np.float64)
+            keep.append(sp)
+            rows = [sp[i] for i in range(6)]
+            (p.demag_kernel_xx_spectrum, p.demag_kernel_yy_spectrum, p.demag_kernel_zz_spectrum,
+             p.demag_kernel_xy_spectrum, p.demag_kernel_xz_spectrum,
+             p.demag_kernel_yz_spectrum) = [_dptr(r) for r in rows]
+            p.demag_kernel_spectrum_len = sp.shape[1]
+        if active_mask is not None:
+            mk = np.ascontiguousarray(active_mask, dtype=np.uint8).reshape(-1)
+            keep.append(mk)
+            p.active_mask = mk.ctypes.data_as(C.POINTER(C.c_uint8))
+            p.active_mask_len = mk.size
+        m = np.ascontiguousarray(m0, dtype=np.float64).reshape(-1)
+        keep.append(m)
+        p.initial_magnetization_xyz = _dptr(m)
+        p.initial_magnetization_len = m.size
+        p.adaptive_max_error = adaptive_max_error
+        p.adaptive_dt_min = adaptive_dt_min
+        p.adaptive_dt_max = adaptive_dt_max
+        p.adaptive_headroom = adaptive_headroom
+        self._poll = None
+        self.handle = self.lib.fullmag_fdm_backend_create(C.byref(p))
+        if not self.handle:
+            raise FdmError(_abi.ERR_INTERNAL, "fullmag_fdm_backend_create returned NULL")
+        err = self.lib.fullmag_fdm_backend_last_error(self.handle)
+        if err:
+            msg = err.decode()
+            self.lib.fullmag_fdm_backend_destroy(self.handle)
+            self.handle = None
+            raise FdmError(_abi.ERR_INVALID, msg)
+
+    # -- lifetime --
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fullmag_fdm_backend_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc == _abi.OK:
+            return
+        err = self.lib.fullmag_fdm_backend_last_error(self.handle)
+        msg = f"{what}: {err.decode() if err else 'no detail'}"
+        if rc == _abi.ERR_INTERRUPTED:
+            raise FdmInterrupted(rc, msg)
+        raise FdmError(rc, msg)
+
+    # -- stepping --
+    def step(self, dt: float) -> dict:
+        st = StepStats()
+        rc = self.lib.fullmag_fdm_backend_step(self.handle, dt, C.byref(st))
+        self._check(rc, "step")
+        return st.as_dict()
+
+    def step_many(self, dt: float, n_steps: int) -> dict:
+        st = StepStats()
+        rc = self.lib.fullmag_fdm_backend_step_many(self.handle, dt, n_steps, C.byref(st))
+        self._check(rc, "step_many")
+        return st.as_dict()
+
+    def set_interrupt_poll(self, fn):
+        """fn() -> bool, polled between device passes; True interrupts the step."""
+        if fn is None:
+            self._poll = None
+            rc = self.lib.fullmag_fdm_backend_set_interrupt_poll(self.handle, _abi.POLL_FN(), None)
+        else:
+            self._poll = _abi.POLL_FN(lambda _ud: 1 if fn() else 0)
+            rc = self.lib.fullmag_fdm_backend_set_interrupt_poll(self.handle, self._poll, None)
+        self._check(rc, "set_interrupt_poll")
+
+    def stats(self) -> dict:
+        st = StepStats()
+        self._check(self.lib.fullmag_fdm_backend_snapshot_stats(self.handle, C.byref(st)), "snapshot_stats")
+        return st.as_dict()
+
+    # -- fields --
+    def copy_field(self, observable: int, dtype=np.float64) -> np.ndarray:
+        if np.dtype(dtype) == np.float64:
+            out = np.empty(3 * self.n, dtype=np.float64)
+            rc = self.lib.fullmag_fdm_backend_copy_field_f64(self.handle, observable, _dptr(out), out.size)
+        else:
+            out = np.empty(3 * self.n, dtype=np.float32)
+            rc = self.lib.fullmag_fdm_backend_copy_field_f32(
+                self.handle, observable, out.ctypes.data_as(C.POINTER(C.c_float)), out.size)
+        self._check(rc, "copy_field")
+        return out.reshape(self.n, 3)
+
+    def magnetization(self):
+        return self.copy_field(_abi.OBSERVABLE_M)
+
+    def preview(self, observable: int, pnx: int, pny: int, pnz: int, z_origin: int = 0, z_stride: int = 1):
+        out = np.empty(3 * pnx * pny * pnz, dtype=np.float64)
+        rc = self.lib.fullmag_fdm_backend_copy_field_preview_f64(
+            self.handle, observable, pnx, pny, pnz, z_origin, z_stride, _dptr(out), out.size)
+        self._check(rc, "copy_field_preview")
+        return out.reshape(-1, 3)
+
+    def upload(self, m: np.ndarray):
+        a = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
+        self._check(self.lib.fullmag_fdm_backend_upload_magnetization_f64(self.handle, _dptr(a), a.size),
+                    "upload_magnetization")
+
+    def refresh(self):
+        self._check(self.lib.fullmag_fdm_backend_refresh_observables(self.handle), "refresh_observables")
+
+    def device_info(self) -> dict:
+        info = _abi.DeviceInfo()
+        self._check(self.lib.fullmag_fdm_backend_get_device_info(self.handle, C.byref(info)), "get_device_info")
+        return {"name": info.name.decode(), "cc": (info.compute_capability_major, info.compute_capability_minor),
+                "driver": info.driver_version, "runtime": info.runtime_version}
+
+    def fft_shape(self):
+        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._check(self.lib.fullmag_fdm_backend_fft_shape(self.handle, C.byref(a), C.byref(b), C.byref(c)),
+                    "fft_shape")
+        return a.value, b.value, c.value
+
+    def launch_count(self) -> int:
+        c = C.c_uint64()
+        self._check(self.lib.fullmag_fdm_backend_launch_count(self.handle, C.byref(c)), "launch_count")
+        return c.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.fullmag_fdm_backend_stream(self.handle, C.byref(s)), "stream")
+        return s.value or 0

@@ -1,0 +1,69 @@
+"""In-tree build of libfullmag_fdm.so for sm_103a (nvcc, no cmake).
+
+Each translation unit compiles in its own nvcc process (in parallel), then one
+link step produces fullmag_gb300/_build/libfullmag_fdm.so.  The library links only
+the CUDA runtime; no torch types cross its C ABI.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+SRC = PKG / "csrc"
+OUT = PKG / "_build"
+LIB = OUT / "libfullmag_fdm.so"
+SOURCES = ["kernels.cu", "engine.cu", "newell.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
+
+
+def nvcc() -> str:
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libfullmag_fdm.so")
+    return p
+
+
+def _stale() -> bool:
+    if not LIB.exists():
+        return True
+    t = LIB.stat().st_mtime
+    deps = [SRC / s for s in SOURCES if (SRC / s).exists()]
+    deps += list(SRC.glob("*.cuh")) + list(SRC.glob("*.h")) + [PKG.parent / "include" / "fullmag_fdm.h"]
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    if not force and not _stale():
+        return LIB
+    OUT.mkdir(parents=True, exist_ok=True)
+    cc = nvcc()
+    srcs = [s for s in SOURCES if (SRC / s).exists()]
+
+    def compile_one(s: str) -> Path:
+        obj = OUT / (Path(s).stem + ".o")
+        cmd = [cc, *FLAGS, *ARCH, "-c", str(SRC / s), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {s}:\n{r.stderr}")
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = OUT / "libfullmag_fdm.so.tmp"
+    cmd = [cc, "-shared", *ARCH, *map(str, objs), "-o", str(tmp), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,1187 @@
+// engine.cu -- host side of the GB300 FDM engine and the C ABI of include/fullmag_fdm.h.
+//
+// One handle = one problem on one GPU, one CUDA stream, one device arena.
+// Semantics follow the reference C ABI (native/backends/fdm/src/api.cpp:151-1070,
+// context.cu:934-1060, llg_fp32.cu:267-389, llg_rk4_fp32.cu, llg_dp45_fp32.cu:188-342):
+// create returns a handle even on validation failure with last_error set, step
+// advances one accepted step and reports post-step statistics, observables are
+// AoS on the host.  Internally the step is a chain of fused passes (see
+// kernels.cu); the field evaluation at the new state that every step reports
+// statistics for doubles as the first stage of the next step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fullmag_fdm.h"
+#include "engine.h"
+
+namespace fm {
+
+static constexpr double kMu0 = 4.0 * M_PI * 1e-7;
+
+bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
+                         std::string &err);
+
+// Device conversions between the ABI's AoS host layout and SoA device state.
+__global__ void aos_to_soa_kernel(const double *__restrict__ in_d, const float *__restrict__ in_f, float *__restrict__ out,
+                                  const uint8_t *__restrict__ mask, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const bool act = mask == nullptr || mask[i] != 0;
+        for (int c = 0; c < 3; ++c) {
+            const float v = in_d ? (float)in_d[3 * i + c] : in_f[3 * i + c];
+            out[c * n + i] = act ? v : 0.f;
+        }
+    }
+}
+__global__ void soa_to_aos_kernel(const float *__restrict__ in, double *__restrict__ out_d, float *__restrict__ out_f,
+                                  long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        for (int c = 0; c < 3; ++c) {
+            const float v = in[c * n + i];
+            if (out_d) out_d[3 * i + c] = (double)v;
+            else out_f[3 * i + c] = v;
+        }
+    }
+}
+
+struct Engine {
+    // ---- configuration ----
+    Grid g{};
+    Material mat{};
+    int integrator = FULLMAG_FDM_INTEGRATOR_HEUN;
+    bool demag = false;
+    double dx = 0, dy = 0, dz = 0, ms = 0, a_ex = 0, alpha = 0, gamma = 0;
+    bool has_ext = false, has_uni = false, has_cub = false, exchange = false;
+    double hext[3] = {0, 0, 0};
+    double max_error = 1e-5, dt_min = 1e-18, dt_max = 1e-10, headroom = 0.8;
+    std::vector<uint8_t> mask_host;
+    bool has_mask = false;
+
+    // ---- device state ----
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    float *S[2] = {nullptr, nullptr};
+    float *A[2] = {nullptr, nullptr};
+    float *K[7] = {};
+    int nk = 0;
+    float *h_ex = nullptr, *h_d = nullptr, *h_eff = nullptr;
+    float2 *X = nullptr, *Y = nullptr;
+    float *kern = nullptr;
+    uint8_t *mask = nullptr;
+    double *partials = nullptr;
+    double *dstats = nullptr;
+    double *hstats = nullptr;  // pinned
+    float2 *twid = nullptr;
+    float2 *xpost = nullptr;
+    FftPlan plan_x{}, plan_y{}, plan_z{};
+    void *staging = nullptr;  // lazily allocated 3n doubles for host transfers
+    int row_rows = 1;
+    int max_row_blocks = 1;
+
+    // ---- dynamic state ----
+    int cur = 0;
+    bool k1_valid = false, fields_valid = false, stats_valid = false;
+    uint64_t step_count = 0;
+    double time = 0.0;
+    double stat_raw[kNumStats] = {};
+    fullmag_fdm_step_stats cur_stats{};
+
+    fullmag_fdm_interrupt_poll_fn poll = nullptr;
+    void *poll_user = nullptr;
+    bool interrupted = false;
+    uint64_t launches = 0;  // kernels this handle has launched
+    fullmag_fdm_device_info info{};
+    bool info_valid = false;
+    std::string last_error;
+
+    ~Engine() { release(); }
+
+    void release() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (arena) cudaFree(arena);
+        arena = nullptr;
+        if (staging) cudaFree(staging);
+        staging = nullptr;
+        if (hstats) cudaFreeHost(hstats);
+        hstats = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+
+    bool cuda_fail(const char *what, cudaError_t e) {
+        if (e == cudaSuccess) return false;
+        last_error = std::string(what) + ": " + cudaGetErrorString(e);
+        return true;
+    }
+
+    bool poll_hit() {
+        if (poll && poll(poll_user) != 0) {
+            interrupted = true;
+            return true;
+        }
+        return false;
+    }
+
+    // ---------------- setup ----------------
+    static void factorize(int n, std::vector<int> &r) {
+        int m = n;
+        while (m % 8 == 0) { r.push_back(8); m /= 8; }
+        while (m % 4 == 0) { r.push_back(4); m /= 4; }
+        while (m % 2 == 0) { r.push_back(2); m /= 2; }
+        for (int q = 3; q * q <= m; q += 2)
+            while (m % q == 0) { r.push_back(q); m /= q; }
+        if (m > 1) r.push_back(m);
+    }
+
+    bool make_plan(FftPlan &p, int n, std::vector<float2> &host_tw, std::vector<size_t> &offs) {
+        std::vector<int> r;
+        factorize(n, r);
+        if ((int)r.size() > kMaxStages) {
+            last_error = "FFT length " + std::to_string(n) + " has too many factors";
+            return false;
+        }
+        for (int x : r)
+            if (x > 8 && x > kMaxGenericRadix) {
+                last_error = "FFT length " + std::to_string(n) + " has a prime factor above 64 (" + std::to_string(x) + ")";
+                return false;
+            }
+        p.n = n;
+        p.nstages = (int)r.size();
+        for (int i = 0; i < p.nstages; ++i) p.radix[i] = r[i];
+        offs.push_back(host_tw.size());
+        for (int e = 0; e < n; ++e) {
+            const double ang = 2.0 * M_PI * (double)e / (double)n;
+            host_tw.push_back(make_float2((float)cos(ang), (float)-sin(ang)));
+        }
+        return true;
+    }
+
+    bool use_gpu_newell = false;
+
+    // largest prime factor <= 7 for the fast radix kernels; up to 64 still works
+    static bool smooth_enough(int n) {
+        int m = n;
+        for (int q : {2, 3, 5, 7}) while (m % q == 0) m /= q;
+        return m == 1;
+    }
+    static int next_smooth(int n, bool even) {
+        for (int m = std::max(n, 1);; ++m) {
+            if (even && (m & 1)) continue;
+            if (smooth_enough(m)) return m;
+        }
+    }
+
+    bool setup(const fullmag_fdm_plan_desc *plan);
+    bool upload_spectra(const fullmag_fdm_plan_desc *plan, bool thin_from_len);
+
+    // ---------------- passes ----------------
+    RowPass row_base() const {
+        RowPass p{};
+        p.g = g;
+        p.mat = mat;
+        p.mask = mask;
+        p.xplan = plan_x;
+        p.xpost = xpost;
+        p.rows = row_rows;
+        return p;
+    }
+
+    bool run_row(RowPass &p) {
+        if (!demag) {
+            p.x_in = nullptr;
+            p.x_out = nullptr;
+        }
+        launches += 1;
+        return !cuda_fail("row pass", launch_row_pass(p, stream));
+    }
+
+    bool run_columns() {
+        if (!demag) return true;
+        ColPass c{};
+        c.g = g;
+        c.kern = kern;
+        if (g.thin) {
+            c.plan = plan_y;
+            c.tx = col_tile(g, 3, g.py);
+            c.in = X;
+            c.out = X;
+            launches += 1;
+            return !cuda_fail("y convolve", launch_y_convolve_2d(c, stream));
+        }
+        c.plan = plan_y;
+        c.tx = col_tile(g, 1, g.py);
+        c.in = X;
+        c.out = Y;
+        if (cuda_fail("y forward", launch_y_forward(c, stream))) return false;
+        c.plan = plan_z;
+        c.tx = col_tile(g, 3, g.pz);
+        c.in = Y;
+        c.out = Y;
+        if (cuda_fail("z convolve", launch_z_convolve(c, stream))) return false;
+        c.plan = plan_y;
+        c.tx = col_tile(g, 1, g.py);
+        c.in = Y;
+        c.out = X;
+        launches += 3;
+        return !cuda_fail("y inverse", launch_y_inverse(c, stream));
+    }
+
+    // forward x-transform of a state (no combination)
+    bool pass_forward(const float *m) {
+        if (!demag) return true;
+        RowPass p = row_base();
+        p.m_fwd = m;
+        p.x_out = X;
+        return run_row(p) && run_columns();
+    }
+
+    bool read_stats() {
+        launches += 1;
+        if (cuda_fail("finalize", launch_finalize_stats(partials, max_row_blocks, dstats, stream))) return false;
+        if (cuda_fail("stats copy", cudaMemcpyAsync(hstats, dstats, sizeof(double) * kNumStats, cudaMemcpyDeviceToHost, stream)))
+            return false;
+        if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return false;
+        return true;
+    }
+
+    void fill_stats(const double *d, fullmag_fdm_step_stats &st) const {
+        const double V = dx * dy * dz;
+        st.exchange_energy_joules = exchange ? a_ex * V * d[0] : 0.0;
+        st.demag_energy_joules = demag ? -0.5 * kMu0 * ms * V * d[1] : 0.0;
+        st.external_energy_joules = has_ext ? -kMu0 * ms * V * d[2] : 0.0;
+        st.anisotropy_energy_joules = has_uni ? -V * d[3] : 0.0;
+        st.cubic_energy_joules = has_cub ? V * d[4] : 0.0;
+        st.dmi_energy_joules = 0.0;
+        st.total_energy_joules = st.exchange_energy_joules + st.demag_energy_joules + st.external_energy_joules +
+                                 st.anisotropy_energy_joules + st.cubic_energy_joules + st.dmi_energy_joules;
+        st.max_effective_field_amplitude = sqrt(d[5]);
+        st.max_demag_field_amplitude = demag ? sqrt(d[6]) : 0.0;
+        st.max_rhs_amplitude = sqrt(d[7]);
+    }
+
+    // RHS at the committed state -> K[0], statistics, optionally observables.
+    bool eval_state(bool write_fields) {
+        if (!pass_forward(S[cur])) return false;
+        RowPass p = row_base();
+        p.x_in = X;
+        p.m_in = S[cur];
+        p.k_out = K[0];
+        p.partials = partials;
+        if (write_fields) {
+            p.h_ex_out = h_ex;
+            p.h_d_out = h_d;
+            p.h_eff_out = h_eff;
+        }
+        if (!run_row(p)) return false;
+        if (!read_stats()) return false;
+        memcpy(stat_raw, hstats, sizeof(stat_raw));
+        k1_valid = true;
+        stats_valid = true;
+        if (write_fields) fields_valid = true;
+        fill_stats(stat_raw, cur_stats);
+        cur_stats.step = step_count;
+        cur_stats.time_seconds = time;
+        return true;
+    }
+
+    // One pass: RHS at m_in (stored to k_out when non-null), combination into m_next.
+    bool stage(const float *m_in, float *k_out, int ncomb, const int *kidx, const double *coef, double dt, float *m_next) {
+        RowPass p = row_base();
+        p.x_in = m_in ? X : nullptr;
+        p.m_in = m_in;
+        p.k_out = k_out;
+        p.m0 = S[cur];
+        p.m_next = m_next;
+        p.n_comb = ncomb;
+        for (int t = 0; t < ncomb; ++t) {
+            p.comb_k[t] = kidx[t] < 0 ? nullptr : K[kidx[t]];
+            p.comb_c[t] = (float)coef[t];
+        }
+        p.dt = (float)dt;
+        p.x_out = X;
+        return run_row(p) && run_columns();
+    }
+
+    // Final RHS of an attempt (at the proposed state) with statistics and optional error terms.
+    bool final_eval(const float *m_in, float *k_out, int nerr, const int *kidx, const double *coef, double dt) {
+        RowPass p = row_base();
+        p.x_in = X;
+        p.m_in = m_in;
+        p.k_out = k_out;
+        p.partials = partials;
+        p.n_err = nerr;
+        for (int t = 0; t < nerr; ++t) {
+            p.err_k[t] = kidx[t] < 0 ? nullptr : K[kidx[t]];
+            p.err_c[t] = coef[t];
+        }
+        p.err_dt = dt;
+        return run_row(p) && read_stats();
+    }
+
+    bool ensure_k1() { return k1_valid || eval_state(false); }
+
+    void commit(double dt, const double *raw) {
+        cur = 1 - cur;
+        memcpy(stat_raw, raw, sizeof(stat_raw));
+        step_count += 1;
+        time += dt;
+        k1_valid = true;
+        stats_valid = true;
+        fields_valid = false;
+        fill_stats(stat_raw, cur_stats);
+        cur_stats.step = step_count;
+        cur_stats.time_seconds = time;
+        cur_stats.dt_seconds = dt;
+        cur_stats.suggested_next_dt = 0.0;
+    }
+
+    // ---- integrators: return 0 ok, 1 interrupted, -1 error ----
+    int step_heun(double dt) {
+        if (!ensure_k1()) return -1;
+        if (poll_hit()) return 1;
+        const int nxt = 1 - cur;
+        {
+            const int k[1] = {0};
+            const double c[1] = {1.0};
+            if (!stage(nullptr, nullptr, 1, k, c, dt, A[0])) return -1;
+        }
+        if (poll_hit()) return 1;
+        {
+            const int k[2] = {0, -1};
+            const double c[2] = {0.5, 0.5};
+            if (!stage(A[0], nullptr, 2, k, c, dt, S[nxt])) return -1;
+        }
+        if (!final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt)) return -1;
+        commit(dt, hstats);
+        return 0;
+    }
+
+    int step_rk4(double dt) {
+        if (!ensure_k1()) return -1;
+        if (poll_hit()) return 1;
+        const int nxt = 1 - cur;
+        const int self[1] = {-1};
+        const double h[1] = {0.5}, one[1] = {1.0};
+        {
+            const int k[1] = {0};
+            if (!stage(nullptr, nullptr, 1, k, h, dt, A[0])) return -1;
+        }
+        if (poll_hit()) return 1;
+        if (!stage(A[0], K[1], 1, self, h, dt, A[1])) return -1;
+        if (poll_hit()) return 1;
+        if (!stage(A[1], K[2], 1, self, one, dt, A[0])) return -1;
+        if (poll_hit()) return 1;
+        {
+            const int k[4] = {0, 1, 2, -1};
+            const double c[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+            if (!stage(A[0], nullptr, 4, k, c, dt, S[nxt])) return -1;
+        }
+        if (!final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt)) return -1;
+        commit(dt, hstats);
+        return 0;
+    }
+
+    int step_dp45(double dt) {
+        static const double a21 = 1.0 / 5.0;
+        static const double a3[2] = {3.0 / 40.0, 9.0 / 40.0};
+        static const double a4[3] = {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0};
+        static const double a5[4] = {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0};
+        static const double a6[5] = {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0};
+        static const double b[5] = {35.0 / 384.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0};
+        static const double e[6] = {71.0 / 57600.0, -71.0 / 16695.0, 71.0 / 1920.0, -17253.0 / 339200.0, 22.0 / 525.0,
+                                    -1.0 / 40.0};
+        if (!ensure_k1()) return -1;
+        const int nxt = 1 - cur;
+        for (;;) {
+            if (poll_hit()) return 1;
+            {
+                const int k[1] = {0};
+                const double c[1] = {a21};
+                if (!stage(nullptr, nullptr, 1, k, c, dt, A[0])) return -1;
+            }
+            if (poll_hit()) return 1;
+            {
+                const int k[2] = {0, -1};
+                if (!stage(A[0], K[1], 2, k, a3, dt, A[1])) return -1;
+            }
+            if (poll_hit()) return 1;
+            {
+                const int k[3] = {0, 1, -1};
+                if (!stage(A[1], K[2], 3, k, a4, dt, A[0])) return -1;
+            }
+            if (poll_hit()) return 1;
+            {
+                const int k[4] = {0, 1, 2, -1};
+                if (!stage(A[0], K[3], 4, k, a5, dt, A[1])) return -1;
+            }
+            if (poll_hit()) return 1;
+            {
+                const int k[5] = {0, 1, 2, 3, -1};
+                if (!stage(A[1], K[4], 5, k, a6, dt, A[0])) return -1;
+            }
+            if (poll_hit()) return 1;
+            {
+                const int k[5] = {0, 2, 3, 4, -1};
+                if (!stage(A[0], K[5], 5, k, b, dt, S[nxt])) return -1;
+            }
+            if (poll_hit()) return 1;
+            {
+                const int k[6] = {0, 2, 3, 4, 5, -1};
+                if (!final_eval(S[nxt], K[6], 6, k, e, dt)) return -1;
+            }
+            const double err = sqrt(hstats[8]);
+            if (err <= max_error || dt <= dt_min) {
+                double dt_next = dt_max;
+                if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+                std::swap(K[0], K[6]);  // first-same-as-last
+                commit(dt, hstats);
+                cur_stats.suggested_next_dt = dt_next;
+                return 0;
+            }
+            dt = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+        }
+    }
+
+    int step(double dt) {
+        interrupted = false;
+        switch (integrator) {
+            case FULLMAG_FDM_INTEGRATOR_RK4: return step_rk4(dt);
+            case FULLMAG_FDM_INTEGRATOR_DP45: return step_dp45(dt);
+            default: return step_heun(dt);
+        }
+    }
+
+    // ---------------- transfers ----------------
+    bool ensure_staging() {
+        if (staging) return true;
+        return !cuda_fail("cudaMalloc(staging)", cudaMalloc(&staging, sizeof(double) * 3 * (size_t)g.n));
+    }
+
+    template <typename T>
+    bool upload(const T *m_xyz) {
+        if (!ensure_staging()) return false;
+        const size_t bytes = sizeof(T) * 3 * (size_t)g.n;
+        if (cuda_fail("cudaMemcpy(m)", cudaMemcpyAsync(staging, m_xyz, bytes, cudaMemcpyHostToDevice, stream))) return false;
+        const bool isd = sizeof(T) == 8;
+        aos_to_soa_kernel<<<std::min<long long>((g.n + 255) / 256, 4096), 256, 0, stream>>>(
+            isd ? (const double *)staging : nullptr, isd ? nullptr : (const float *)staging, S[cur], mask, g.n);
+        if (cuda_fail("upload convert", cudaGetLastError())) return false;
+        if (cuda_fail("upload sync", cudaStreamSynchronize(stream))) return false;
+        k1_valid = false;
+        fields_valid = false;
+        stats_valid = false;
+        return true;
+    }
+
+    const float *field_ptr(int obs) {
+        switch (obs) {
+            case FULLMAG_FDM_OBSERVABLE_M: return S[cur];
+            case FULLMAG_FDM_OBSERVABLE_H_EX: return h_ex;
+            case FULLMAG_FDM_OBSERVABLE_H_DEMAG: return h_d;
+            case FULLMAG_FDM_OBSERVABLE_H_EFF: return h_eff;
+            default: return nullptr;
+        }
+    }
+
+    template <typename T>
+    bool download(int obs, T *out) {
+        const long long n = g.n;
+        if (obs == FULLMAG_FDM_OBSERVABLE_H_EXT) {
+            for (long long i = 0; i < n; ++i) {
+                const bool act = !has_mask || mask_host[i] != 0;
+                for (int c = 0; c < 3; ++c) out[3 * i + c] = (T)((has_ext && act) ? hext[c] : 0.0);
+            }
+            return true;
+        }
+        if (obs < FULLMAG_FDM_OBSERVABLE_M || obs > FULLMAG_FDM_OBSERVABLE_H_EFF) {
+            last_error = "unknown observable " + std::to_string(obs);
+            return false;
+        }
+        if (obs != FULLMAG_FDM_OBSERVABLE_M && !fields_valid) {
+            if (!eval_state(true)) return false;
+        }
+        const float *src = field_ptr(obs);
+        if (!ensure_staging()) return false;
+        const bool isd = sizeof(T) == 8;
+        soa_to_aos_kernel<<<std::min<long long>((n + 255) / 256, 4096), 256, 0, stream>>>(
+            src, isd ? (double *)staging : nullptr, isd ? nullptr : (float *)staging, n);
+        if (cuda_fail("download convert", cudaGetLastError())) return false;
+        if (cuda_fail("cudaMemcpy(field)",
+                      cudaMemcpyAsync(out, staging, sizeof(T) * 3 * (size_t)n, cudaMemcpyDeviceToHost, stream)))
+            return false;
+        return !cuda_fail("download sync", cudaStreamSynchronize(stream));
+    }
+
+    template <typename T>
+    bool preview(int obs, uint32_t pnx, uint32_t pny, uint32_t pnz, uint32_t z0, uint32_t zs, T *out) {
+        if (z0 >= (uint32_t)g.nz) {
+            last_error = "preview z_origin out of range";
+            return false;
+        }
+        std::vector<double> full(3 * (size_t)g.n);
+        if (!download<double>(obs, full.data())) return false;
+        const uint32_t fx = g.nx, fy = g.ny, fz = g.nz;
+        for (uint32_t pz = 0; pz < pnz; ++pz) {
+            uint32_t zs0 = z0 + pz * zs;
+            if (zs0 >= fz) zs0 = fz - 1;
+            uint32_t ze = z0 + (pz + 1) * zs;
+            if (ze <= zs0) ze = zs0 + 1;
+            if (ze > fz) ze = fz;
+            for (uint32_t py = 0; py < pny; ++py) {
+                uint32_t ys = (uint32_t)(((uint64_t)py * fy) / pny), ye = (uint32_t)(((uint64_t)(py + 1) * fy) / pny);
+                if (ye <= ys) ye = ys + 1;
+                if (ye > fy) ye = fy;
+                for (uint32_t px = 0; px < pnx; ++px) {
+                    uint32_t xs = (uint32_t)(((uint64_t)px * fx) / pnx), xe = (uint32_t)(((uint64_t)(px + 1) * fx) / pnx);
+                    if (xe <= xs) xe = xs + 1;
+                    if (xe > fx) xe = fx;
+                    double a[3] = {0, 0, 0}, cnt = 0;
+                    for (uint32_t z = zs0; z < ze; ++z)
+                        for (uint32_t y = ys; y < ye; ++y)
+                            for (uint32_t x = xs; x < xe; ++x) {
+                                const size_t i = ((size_t)z * fy + y) * fx + x;
+                                for (int c = 0; c < 3; ++c) a[c] += full[3 * i + c];
+                                cnt += 1.0;
+                            }
+                    const size_t o = ((size_t)pz * pny + py) * pnx + px;
+                    for (int c = 0; c < 3; ++c) out[3 * o + c] = (T)(a[c] / cnt);
+                }
+            }
+        }
+        return true;
+    }
+};
+
+// ---------------- setup ----------------
+
+static bool unsupported(Engine &e, bool cond, const char *what) {
+    if (cond) e.last_error = std::string("not supported by the GB300 engine: ") + what;
+    return cond;
+}
+
+bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
+    g.nx = (int)plan->grid.nx;
+    g.ny = (int)plan->grid.ny;
+    g.nz = (int)plan->grid.nz;
+    g.n = (long long)g.nx * g.ny * g.nz;
+    dx = plan->grid.dx;
+    dy = plan->grid.dy;
+    dz = plan->grid.dz;
+    ms = plan->material.saturation_magnetisation;
+    a_ex = plan->material.exchange_stiffness;
+    alpha = plan->material.damping;
+    gamma = plan->material.gyromagnetic_ratio;
+    integrator = plan->integrator;
+    exchange = plan->enable_exchange != 0;
+    demag = plan->enable_demag != 0;
+    has_ext = plan->has_external_field != 0;
+    has_uni = plan->has_uniaxial_anisotropy != 0;
+    has_cub = plan->has_cubic_anisotropy != 0;
+    for (int c = 0; c < 3; ++c) hext[c] = has_ext ? plan->external_field_am[c] : 0.0;
+    max_error = plan->adaptive_max_error > 0 ? plan->adaptive_max_error : 1e-5;
+    dt_min = plan->adaptive_dt_min > 0 ? plan->adaptive_dt_min : 1e-18;
+    dt_max = plan->adaptive_dt_max > 0 ? plan->adaptive_dt_max : 1e-10;
+    headroom = plan->adaptive_headroom > 0 ? plan->adaptive_headroom : 0.8;
+
+    // ---- validation (reference api.cpp:324-395) ----
+    if (g.n == 0) {
+        last_error = "grid has zero cells";
+        return false;
+    }
+    if (plan->initial_magnetization_xyz == nullptr || plan->initial_magnetization_len != 3 * (uint64_t)g.n) {
+        last_error = "initial_magnetization_len mismatch: expected " + std::to_string(3 * (uint64_t)g.n) + ", got " +
+                     std::to_string(plan->initial_magnetization_len);
+        return false;
+    }
+    if (plan->active_mask && plan->active_mask_len != (uint64_t)g.n) {
+        last_error = "active_mask_len mismatch: expected " + std::to_string(g.n) + ", got " +
+                     std::to_string(plan->active_mask_len);
+        return false;
+    }
+    if (!(dx > 0 && dy > 0 && dz > 0)) {
+        last_error = "cell sizes must be positive";
+        return false;
+    }
+    if (!(ms > 0)) {
+        last_error = "saturation_magnetisation must be positive";
+        return false;
+    }
+    if (unsupported(*this, plan->precision == FULLMAG_FDM_PRECISION_DOUBLE, "double precision state (use SINGLE)") ||
+        unsupported(*this, integrator != FULLMAG_FDM_INTEGRATOR_HEUN && integrator != FULLMAG_FDM_INTEGRATOR_RK4 &&
+                               integrator != FULLMAG_FDM_INTEGRATOR_DP45,
+                    "integrators other than HEUN, RK4, DP45") ||
+        unsupported(*this, plan->has_interfacial_dmi || plan->has_bulk_dmi, "DMI") ||
+        unsupported(*this, plan->has_magnetoelastic != 0, "magnetoelastic coupling") ||
+        unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
+        unsupported(*this, plan->current_density_x != 0 || plan->current_density_y != 0 || plan->current_density_z != 0,
+                    "spin-transfer torque") ||
+        unsupported(*this, plan->has_sot != 0, "spin-orbit torque") ||
+        unsupported(*this, plan->has_oersted_cylinder != 0, "Oersted field") ||
+        unsupported(*this, plan->region_mask != nullptr, "region masks / exchange LUT") ||
+        unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers") ||
+        unsupported(*this, plan->ku1_field || plan->ku2_field || plan->kc1_field || plan->kc2_field || plan->kc3_field,
+                    "per-cell anisotropy maps"))
+        return false;
+
+    if (plan->active_mask) {
+        has_mask = true;
+        mask_host.assign(plan->active_mask, plan->active_mask + g.n);
+    }
+
+    // ---- padded geometry ----
+    // With caller spectra the padded grid is the reference's (2nx, 2ny, 2nz) or, for
+    // nz == 1 and 2-D spectra, (2nx, 2ny).  When the engine builds the tensor itself
+    // any extent p >= 2n - 1 keeps the circular convolution exact on the physical
+    // cells, so awkward sizes are rounded up to 2,3,5,7-smooth FFT lengths.
+    bool thin = false;
+    use_gpu_newell = false;
+    g.px = 2 * g.nx;
+    g.py = 2 * g.ny;
+    if (demag) {
+        const uint64_t len3 = 2ull * (uint64_t)(2 * g.nx) * (2 * g.ny) * (2 * g.nz);
+        const uint64_t len2 = 2ull * (uint64_t)(2 * g.nx) * (2 * g.ny);
+        if (plan->demag_kernel_spectrum_len == 0) {
+            use_gpu_newell = true;
+            thin = g.nz == 1;
+        } else {
+            if (!plan->demag_kernel_xx_spectrum || !plan->demag_kernel_yy_spectrum || !plan->demag_kernel_zz_spectrum ||
+                !plan->demag_kernel_xy_spectrum || !plan->demag_kernel_xz_spectrum || !plan->demag_kernel_yz_spectrum) {
+                last_error = "demag kernel spectra pointers must all be present when demag_kernel_spectrum_len is set";
+                return false;
+            }
+            if (g.nz == 1 && plan->demag_kernel_spectrum_len == len2) thin = true;
+            else if (plan->demag_kernel_spectrum_len != len3) {
+                last_error = "demag_kernel_spectrum_len mismatch: expected " + std::to_string(len3) + " (3D)" +
+                             (g.nz == 1 ? " or " + std::to_string(len2) + " (thin-film 2D)" : std::string()) + ", got " +
+                             std::to_string(plan->demag_kernel_spectrum_len);
+                return false;
+            }
+            // the given spectra fix P = 2n; lengths with a prime factor the shared-memory
+            // FFT does not handle are rebuilt on the GPU at smooth extents instead
+            if (!smooth_enough(2 * g.nx) || !smooth_enough(2 * g.ny) || (!thin && !smooth_enough(2 * g.nz)))
+                use_gpu_newell = true;
+        }
+        if (use_gpu_newell) {
+            g.px = next_smooth(2 * g.nx - 1, true);
+            g.py = next_smooth(2 * g.ny - 1, false);
+        }
+    }
+    g.thin = thin ? 1 : 0;
+    g.pz = thin ? 1 : (use_gpu_newell ? next_smooth(2 * g.nz - 1, false) : 2 * g.nz);
+    if (g.px < 2) g.px = 2;
+    g.half = g.px / 2;
+    g.nkx = g.half + 1;
+    g.nky = g.py / 2 + 1;
+    g.nkz = g.pz / 2 + 1;
+
+    // ---- material constants ----
+    const double mu0ms = kMu0 * ms;
+    mat.ex_pref = exchange ? (float)(2.0 * a_ex / mu0ms) : 0.f;
+    mat.idx2 = (float)(1.0 / (dx * dx));
+    mat.idy2 = (float)(1.0 / (dy * dy));
+    mat.idz2 = (float)(1.0 / (dz * dz));
+    mat.has_ext = has_ext;
+    for (int c = 0; c < 3; ++c) mat.hext[c] = (float)hext[c];
+    auto unit = [](const double *v, double *o) {
+        double nn = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (nn < 1e-30) nn = 1e-30;
+        for (int c = 0; c < 3; ++c) o[c] = v[c] / nn;
+    };
+    mat.has_uni = has_uni;
+    if (has_uni) {
+        double u[3];
+        unit(plan->anisotropy_axis, u);
+        for (int c = 0; c < 3; ++c) mat.u[c] = (float)u[c];
+        mat.ku1c = (float)(2.0 * plan->uniaxial_anisotropy_constant / mu0ms);
+        mat.ku2c = (float)(4.0 * plan->uniaxial_anisotropy_k2 / mu0ms);
+        mat.ku1 = plan->uniaxial_anisotropy_constant;
+        mat.ku2 = plan->uniaxial_anisotropy_k2;
+    }
+    mat.has_cub = has_cub;
+    if (has_cub) {
+        double c1[3], c2[3];
+        unit(plan->cubic_axis1, c1);
+        unit(plan->cubic_axis2, c2);
+        const double c3[3] = {c1[1] * c2[2] - c1[2] * c2[1], c1[2] * c2[0] - c1[0] * c2[2], c1[0] * c2[1] - c1[1] * c2[0]};
+        for (int c = 0; c < 3; ++c) {
+            mat.c1[c] = (float)c1[c];
+            mat.c2[c] = (float)c2[c];
+            mat.c3[c] = (float)c3[c];
+        }
+        mat.kc1c = (float)(-2.0 * plan->cubic_Kc1 / mu0ms);
+        mat.kc2c = (float)(-2.0 * plan->cubic_Kc2 / mu0ms);
+        mat.kc3c = (float)(-4.0 * plan->cubic_Kc3 / mu0ms);
+        mat.kc1 = plan->cubic_Kc1;
+        mat.kc2 = plan->cubic_Kc2;
+        mat.kc3 = plan->cubic_Kc3;
+    }
+    mat.gbar = (float)(gamma / (1.0 + alpha * alpha));
+    mat.alpha = (float)alpha;
+    mat.prec = plan->disable_precession ? 0.f : 1.f;
+
+    // ---- device and stream ----
+    if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;
+    if (cuda_fail("cudaStreamCreate", cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking))) return false;
+
+    // ---- FFT plans ----
+    std::vector<float2> tw;
+    std::vector<size_t> offs;
+    if (demag) {
+        if (!make_plan(plan_x, g.half, tw, offs) || !make_plan(plan_y, g.py, tw, offs) || !make_plan(plan_z, g.pz, tw, offs))
+            return false;
+    }
+    const size_t xpost_off = tw.size();
+    for (int k = 0; k <= g.half; ++k) {
+        const double ang = 2.0 * M_PI * (double)k / (double)g.px;
+        tw.push_back(make_float2((float)cos(ang), (float)-sin(ang)));
+    }
+
+    // ---- arena ----
+    nk = integrator == FULLMAG_FDM_INTEGRATOR_DP45 ? 7 : (integrator == FULLMAG_FDM_INTEGRATOR_RK4 ? 3 : 1);
+    row_rows = std::max(1, std::min(16, 256 / std::max(1, g.nx)));
+    max_row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
+    const size_t vec = sizeof(float) * 3 * (size_t)g.n;
+    const size_t xlen = demag ? sizeof(float2) * 3 * (size_t)g.nz * g.ny * g.nkx : 0;
+    const size_t ylen = (demag && !thin) ? sizeof(float2) * 3 * (size_t)g.nz * g.py * g.nkx : 0;
+    const size_t klen = demag ? sizeof(float) * (thin ? 4 : 6) * (size_t)g.nkz * g.nky * g.nkx : 0;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t off = 0;
+    std::vector<size_t> o;
+    auto take = [&](size_t b) {
+        o.push_back(off);
+        off += al(b);
+    };
+    take(vec); take(vec); take(vec); take(vec);            // S0 S1 A0 A1
+    for (int i = 0; i < nk; ++i) take(vec);                 // K
+    take(vec); take(vec); take(vec);                        // observables
+    take(xlen); take(ylen); take(klen);                     // spectra + kernel
+    take(has_mask ? (size_t)g.n : 0);                       // mask
+    take(sizeof(double) * kNumStats * (size_t)max_row_blocks);
+    take(sizeof(double) * kNumStats);
+    take(sizeof(float2) * tw.size());
+    arena_bytes = off;
+    if (cuda_fail("cudaMalloc(arena)", cudaMalloc((void **)&arena, arena_bytes))) return false;
+    if (cuda_fail("cudaMemset(arena)", cudaMemsetAsync(arena, 0, arena_bytes, stream))) return false;
+    int q = 0;
+    S[0] = (float *)(arena + o[q++]);
+    S[1] = (float *)(arena + o[q++]);
+    A[0] = (float *)(arena + o[q++]);
+    A[1] = (float *)(arena + o[q++]);
+    for (int i = 0; i < nk; ++i) K[i] = (float *)(arena + o[q++]);
+    h_ex = (float *)(arena + o[q++]);
+    h_d = (float *)(arena + o[q++]);
+    h_eff = (float *)(arena + o[q++]);
+    X = demag ? (float2 *)(arena + o[q]) : nullptr;
+    q++;
+    Y = ylen ? (float2 *)(arena + o[q]) : nullptr;
+    q++;
+    kern = demag ? (float *)(arena + o[q]) : nullptr;
+    q++;
+    mask = has_mask ? (uint8_t *)(arena + o[q]) : nullptr;
+    q++;
+    partials = (double *)(arena + o[q++]);
+    dstats = (double *)(arena + o[q++]);
+    twid = (float2 *)(arena + o[q++]);
+    if (cuda_fail("cudaMallocHost(stats)", cudaMallocHost((void **)&hstats, sizeof(double) * kNumStats))) return false;
+
+    if (cuda_fail("cudaMemcpy(twiddles)", cudaMemcpyAsync(twid, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, stream)))
+        return false;
+    if (demag) {
+        plan_x.tw = twid + offs[0];
+        plan_y.tw = twid + offs[1];
+        plan_z.tw = twid + offs[2];
+    }
+    xpost = twid + xpost_off;
+    if (has_mask && cuda_fail("cudaMemcpy(mask)", cudaMemcpyAsync(mask, mask_host.data(), (size_t)g.n, cudaMemcpyHostToDevice, stream)))
+        return false;
+    if (demag) {
+        if (use_gpu_newell) {
+            std::string err;
+            if (!newell_spectrum_gpu(g, dx, dy, dz, ms, kern, stream, err)) {
+                last_error = err;
+                return false;
+            }
+        } else if (!upload_spectra(plan, thin)) {
+            return false;
+        }
+    }
+    if (cuda_fail("setup sync", cudaStreamSynchronize(stream))) return false;
+    return true;
+}
+
+// Real, octant-unique part of the given FP64 spectra, scaled by Ms/P (the
+// FFT normalisation and M = Ms m folded into the kernel), converted to FP32.
+bool Engine::upload_spectra(const fullmag_fdm_plan_desc *plan, bool thin) {
+    const double *src[6] = {plan->demag_kernel_xx_spectrum, plan->demag_kernel_yy_spectrum, plan->demag_kernel_zz_spectrum,
+                            plan->demag_kernel_xy_spectrum, plan->demag_kernel_xz_spectrum, plan->demag_kernel_yz_spectrum};
+    const int ncomp = thin ? 4 : 6;
+    const double P = (double)g.px * g.py * (thin ? 1 : g.pz);
+    const double scale = ms / P;
+    const size_t per = (size_t)g.nkz * g.nky * g.nkx;
+    std::vector<float> h((size_t)ncomp * per);
+    for (int c = 0; c < ncomp; ++c)
+        for (int kz = 0; kz < g.nkz; ++kz)
+            for (int ky = 0; ky < g.nky; ++ky)
+                for (int kx = 0; kx < g.nkx; ++kx) {
+                    const size_t s = (size_t)kx + (size_t)g.px * (ky + (size_t)g.py * kz);
+                    h[(size_t)c * per + ((size_t)kz * g.nky + ky) * g.nkx + kx] = (float)(src[c][2 * s] * scale);
+                }
+    if (cuda_fail("cudaMemcpy(kernel)", cudaMemcpyAsync(kern, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice, stream)))
+        return false;
+    return !cuda_fail("kernel sync", cudaStreamSynchronize(stream));
+}
+
+}  // namespace fm
+
+// =====================================================================
+// C ABI
+// =====================================================================
+
+using fm::Engine;
+
+static Engine *eng(fullmag_fdm_backend *h) { return reinterpret_cast<Engine *>(h); }
+
+static int device_from_env() {
+    const char *a = std::getenv("FULLMAG_FDM_GPU_INDEX");
+    const char *b = std::getenv("FULLMAG_CUDA_DEVICE_INDEX");
+    const char *raw = a ? a : b;
+    if (!raw || !*raw) return -1;
+    char *end = nullptr;
+    long v = std::strtol(raw, &end, 10);
+    if (end == raw || *end != '\0' || v < 0) return -1;
+    return (int)v;
+}
+
+template <typename T>
+static int preview_impl(fullmag_fdm_backend *handle, fullmag_fdm_observable obs, uint32_t pnx, uint32_t pny, uint32_t pnz,
+                        uint32_t z0, uint32_t zs, T *out, uint64_t out_len) {
+    Engine *e = eng(handle);
+    if (!e || !out || pnx == 0 || pny == 0 || pnz == 0 || zs == 0 || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (out_len != (uint64_t)pnx * pny * pnz * 3) {
+        e->last_error = "preview out_len mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->preview<T>(obs, pnx, pny, pnz, z0, zs, out) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+// Snapshots: the payload is produced at begin time into memory owned by the
+// snapshot (component-major SoA for field snapshots, AoS for previews), so
+// wait never touches the backend and may run on another thread.
+struct SnapshotPayload {
+    std::vector<unsigned char> bytes;
+    fullmag_fdm_snapshot_desc desc{};
+    bool ok = false;
+};
+
+static int snap_wait(SnapshotPayload *s, const void **out_data, uint64_t *out_len, fullmag_fdm_snapshot_desc *out_desc) {
+    if (!s || !out_data || !out_len || !out_desc) return FULLMAG_FDM_ERR_INVALID;
+    if (!s->ok) return FULLMAG_FDM_ERR_CUDA;
+    *out_data = s->bytes.data();
+    *out_len = s->bytes.size();
+    *out_desc = s->desc;
+    return FULLMAG_FDM_OK;
+}
+
+extern "C" {
+
+int fullmag_fdm_is_available(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return 0;
+    const int sel = device_from_env();
+    if (sel >= 0 && sel >= count) return 0;
+    return 1;
+}
+
+fullmag_fdm_backend *fullmag_fdm_backend_create(const fullmag_fdm_plan_desc *plan) {
+    if (!plan) return nullptr;
+    Engine *e = new (std::nothrow) Engine();
+    if (!e) return nullptr;
+    const int sel = device_from_env();
+    if (sel >= 0) {
+        cudaError_t err = cudaSetDevice(sel);
+        if (err != cudaSuccess) {
+            e->last_error = std::string("cudaSetDevice: ") + cudaGetErrorString(err);
+            return reinterpret_cast<fullmag_fdm_backend *>(e);
+        }
+    }
+    if (!e->setup(plan)) return reinterpret_cast<fullmag_fdm_backend *>(e);
+    if (!e->upload<double>(plan->initial_magnetization_xyz)) return reinterpret_cast<fullmag_fdm_backend *>(e);
+    if (!e->eval_state(true)) return reinterpret_cast<fullmag_fdm_backend *>(e);
+    return reinterpret_cast<fullmag_fdm_backend *>(e);
+}
+
+int fullmag_fdm_backend_step(fullmag_fdm_backend *handle, double dt_seconds, fullmag_fdm_step_stats *out_stats) {
+    Engine *e = eng(handle);
+    if (!e || !out_stats) return FULLMAG_FDM_ERR_INVALID;
+    if (!e->arena) return FULLMAG_FDM_ERR_INVALID;
+    e->last_error.clear();
+    if (!(dt_seconds > 0.0) || !std::isfinite(dt_seconds)) {
+        e->last_error = "dt_seconds must be positive and finite";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = e->step(dt_seconds);
+    if (rc < 0) return FULLMAG_FDM_ERR_CUDA;
+    if (rc == 1) {
+        if (!e->stats_valid && !e->eval_state(false)) return FULLMAG_FDM_ERR_CUDA;
+        *out_stats = e->cur_stats;
+        out_stats->dt_seconds = 0.0;
+        return FULLMAG_FDM_ERR_INTERRUPTED;
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    *out_stats = e->cur_stats;
+    out_stats->wall_time_ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count();
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_step_many(fullmag_fdm_backend *handle, double dt_seconds, uint64_t n_steps,
+                                  fullmag_fdm_step_stats *out_stats) {
+    Engine *e = eng(handle);
+    if (!e || !out_stats || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    e->last_error.clear();
+    if (e->integrator == FULLMAG_FDM_INTEGRATOR_DP45) {
+        e->last_error = "step_many supports fixed-step integrators only";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    for (uint64_t s = 0; s < n_steps; ++s) {
+        const int rc = fullmag_fdm_backend_step(handle, dt_seconds, out_stats);
+        if (rc != FULLMAG_FDM_OK) return rc;
+    }
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_set_interrupt_poll(fullmag_fdm_backend *handle, fullmag_fdm_interrupt_poll_fn poll_fn, void *user_data) {
+    Engine *e = eng(handle);
+    if (!e) return FULLMAG_FDM_ERR_INVALID;
+    e->poll = poll_fn;
+    e->poll_user = user_data;
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_copy_field_f64(fullmag_fdm_backend *handle, fullmag_fdm_observable observable, double *out_xyz,
+                                       uint64_t out_len) {
+    Engine *e = eng(handle);
+    if (!e || !out_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (out_len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "out_len mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    if (observable < FULLMAG_FDM_OBSERVABLE_M || observable > FULLMAG_FDM_OBSERVABLE_H_EFF) {
+        e->last_error = "unknown observable";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->download<double>(observable, out_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_copy_field_f32(fullmag_fdm_backend *handle, fullmag_fdm_observable observable, float *out_xyz,
+                                       uint64_t out_len) {
+    Engine *e = eng(handle);
+    if (!e || !out_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (out_len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "out_len mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    if (observable < FULLMAG_FDM_OBSERVABLE_M || observable > FULLMAG_FDM_OBSERVABLE_H_EFF) {
+        e->last_error = "unknown observable";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->download<float>(observable, out_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_copy_field_preview_f64(fullmag_fdm_backend *handle, fullmag_fdm_observable observable,
+                                               uint32_t preview_nx, uint32_t preview_ny, uint32_t preview_nz,
+                                               uint32_t z_origin, uint32_t z_stride, double *out_xyz, uint64_t out_len) {
+    return preview_impl<double>(handle, observable, preview_nx, preview_ny, preview_nz, z_origin, z_stride, out_xyz, out_len);
+}
+
+int fullmag_fdm_backend_copy_field_preview_f32(fullmag_fdm_backend *handle, fullmag_fdm_observable observable,
+                                               uint32_t preview_nx, uint32_t preview_ny, uint32_t preview_nz,
+                                               uint32_t z_origin, uint32_t z_stride, float *out_xyz, uint64_t out_len) {
+    return preview_impl<float>(handle, observable, preview_nx, preview_ny, preview_nz, z_origin, z_stride, out_xyz, out_len);
+}
+
+fullmag_fdm_field_snapshot *fullmag_fdm_backend_begin_field_snapshot(fullmag_fdm_backend *handle,
+                                                                     fullmag_fdm_observable observable) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena) return nullptr;
+    auto *s = new (std::nothrow) SnapshotPayload();
+    if (!s) return nullptr;
+    const size_t n = (size_t)e->g.n;
+    std::vector<float> aos(3 * n);
+    if (!e->download<float>(observable, aos.data())) {
+        delete s;
+        return nullptr;
+    }
+    s->bytes.resize(sizeof(float) * 3 * n);
+    float *soa = reinterpret_cast<float *>(s->bytes.data());
+    for (size_t i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c) soa[c * n + i] = aos[3 * i + c];
+    s->desc.cell_count = n;
+    s->desc.component_count = 3;
+    s->desc.scalar_bytes = 4;
+    s->desc.scalar_type = FULLMAG_FDM_SNAPSHOT_SCALAR_F32;
+    s->ok = true;
+    return reinterpret_cast<fullmag_fdm_field_snapshot *>(s);
+}
+
+fullmag_fdm_preview_snapshot *fullmag_fdm_backend_begin_preview_snapshot(fullmag_fdm_backend *handle,
+                                                                         fullmag_fdm_observable observable,
+                                                                         uint32_t preview_nx, uint32_t preview_ny,
+                                                                         uint32_t preview_nz, uint32_t z_origin,
+                                                                         uint32_t z_stride) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena || preview_nx == 0 || preview_ny == 0 || preview_nz == 0 || z_stride == 0) return nullptr;
+    auto *s = new (std::nothrow) SnapshotPayload();
+    if (!s) return nullptr;
+    const size_t n = (size_t)preview_nx * preview_ny * preview_nz;
+    s->bytes.resize(sizeof(float) * 3 * n);
+    if (!e->preview<float>(observable, preview_nx, preview_ny, preview_nz, z_origin, z_stride,
+                           reinterpret_cast<float *>(s->bytes.data()))) {
+        delete s;
+        return nullptr;
+    }
+    s->desc.cell_count = n;
+    s->desc.component_count = 3;
+    s->desc.scalar_bytes = 4;
+    s->desc.scalar_type = FULLMAG_FDM_SNAPSHOT_SCALAR_F32;
+    s->ok = true;
+    return reinterpret_cast<fullmag_fdm_preview_snapshot *>(s);
+}
+
+int fullmag_fdm_field_snapshot_wait(fullmag_fdm_field_snapshot *snapshot, const void **out_data, uint64_t *out_len_bytes,
+                                    fullmag_fdm_snapshot_desc *out_desc) {
+    return snap_wait(reinterpret_cast<SnapshotPayload *>(snapshot), out_data, out_len_bytes, out_desc);
+}
+
+int fullmag_fdm_preview_snapshot_wait(fullmag_fdm_preview_snapshot *snapshot, const void **out_data, uint64_t *out_len_bytes,
+                                      fullmag_fdm_snapshot_desc *out_desc) {
+    return snap_wait(reinterpret_cast<SnapshotPayload *>(snapshot), out_data, out_len_bytes, out_desc);
+}
+
+void fullmag_fdm_field_snapshot_destroy(fullmag_fdm_field_snapshot *snapshot) {
+    delete reinterpret_cast<SnapshotPayload *>(snapshot);
+}
+
+void fullmag_fdm_preview_snapshot_destroy(fullmag_fdm_preview_snapshot *snapshot) {
+    delete reinterpret_cast<SnapshotPayload *>(snapshot);
+}
+
+int fullmag_fdm_backend_upload_magnetization_f64(fullmag_fdm_backend *handle, const double *m_xyz, uint64_t len) {
+    Engine *e = eng(handle);
+    if (!e || !m_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "magnetization length mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->upload<double>(m_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_upload_magnetization_f32(fullmag_fdm_backend *handle, const float *m_xyz, uint64_t len) {
+    Engine *e = eng(handle);
+    if (!e || !m_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "magnetization length mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->upload<float>(m_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_refresh_observables(fullmag_fdm_backend *handle) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    return e->eval_state(true) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_refresh_demag_observable(fullmag_fdm_backend *handle) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    return e->eval_state(true) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_snapshot_stats(fullmag_fdm_backend *handle, fullmag_fdm_step_stats *out_stats) {
+    Engine *e = eng(handle);
+    if (!e || !out_stats || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (!e->stats_valid && !e->eval_state(false)) return FULLMAG_FDM_ERR_CUDA;
+    *out_stats = e->cur_stats;
+    out_stats->step = e->step_count;
+    out_stats->time_seconds = e->time;
+    out_stats->dt_seconds = 0.0;
+    out_stats->suggested_next_dt = 0.0;
+    out_stats->wall_time_ns = 0;
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_get_device_info(fullmag_fdm_backend *handle, fullmag_fdm_device_info *out_info) {
+    Engine *e = eng(handle);
+    if (!e || !out_info) return FULLMAG_FDM_ERR_INVALID;
+    if (!e->info_valid) {
+        cudaDeviceProp prop;
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+            e->last_error = "cudaGetDeviceProperties failed";
+            return FULLMAG_FDM_ERR_CUDA;
+        }
+        std::memset(&e->info, 0, sizeof(e->info));
+        std::strncpy(e->info.name, prop.name, sizeof(e->info.name) - 1);
+        e->info.compute_capability_major = prop.major;
+        e->info.compute_capability_minor = prop.minor;
+        cudaDriverGetVersion(&e->info.driver_version);
+        cudaRuntimeGetVersion(&e->info.runtime_version);
+        e->info_valid = true;
+    }
+    *out_info = e->info;
+    return FULLMAG_FDM_OK;
+}
+
+const char *fullmag_fdm_backend_last_error(fullmag_fdm_backend *handle) {
+    if (!handle) return "null handle";
+    Engine *e = eng(handle);
+    return e->last_error.empty() ? nullptr : e->last_error.c_str();
+}
+
+void fullmag_fdm_backend_destroy(fullmag_fdm_backend *handle) { delete eng(handle); }
+
+int fullmag_fdm_backend_device_magnetization(fullmag_fdm_backend *handle, void **out_mx, void **out_my, void **out_mz) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena || !out_mx || !out_my || !out_mz) return FULLMAG_FDM_ERR_INVALID;
+    float *m = e->S[e->cur];
+    *out_mx = m;
+    *out_my = m + e->g.n;
+    *out_mz = m + 2 * e->g.n;
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_stream(fullmag_fdm_backend *handle, void **out_stream) {
+    Engine *e = eng(handle);
+    if (!e || !out_stream) return FULLMAG_FDM_ERR_INVALID;
+    *out_stream = (void *)e->stream;
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_count) {
+    Engine *e = eng(handle);
+    if (!e || !out_count) return FULLMAG_FDM_ERR_INVALID;
+    *out_count = e->launches;
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px, uint32_t *out_py, uint32_t *out_pz) {
+    Engine *e = eng(handle);
+    if (!e || !out_px || !out_py || !out_pz) return FULLMAG_FDM_ERR_INVALID;
+    *out_px = e->g.px;
+    *out_py = e->g.py;
+    *out_pz = e->g.pz;
+    return FULLMAG_FDM_OK;
+}
+
+}  // extern "C"

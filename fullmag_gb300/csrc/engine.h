@@ -1,0 +1,109 @@
+// engine.h -- device-side data layout and pass descriptors of the GB300 FDM engine.
+//
+// Layout in HBM (one allocation per buffer class, all 256-byte aligned):
+//   vector fields : SoA float, component c of cell i at base[c*n + i],
+//                   cell i = x + nx*(y + ny*z)
+//   X spectrum    : x-transformed half spectrum, float2 X[c][z][y][kx],
+//                   kx in [0, px/2], rows only for y < ny, z < nz (zero rows pruned)
+//   Y spectrum    : (3-D only) y-transformed, float2 Y[c][z][ky][kx], ky in [0, py)
+//   demag kernel  : real, octant-unique, pre-scaled by Ms/P:
+//                   3-D K[6][pz/2+1][py/2+1][kx]   (xx yy zz xy xz yz)
+//                   2-D K[4][py/2+1][kx]           (xx yy zz xy)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_smem.cuh"
+
+namespace fm {
+
+constexpr int kNumStats = 9;  // e_ex e_d e_ext e_uni e_cub | max|Heff|^2 max|Hd|^2 max|k|^2 max err^2
+constexpr int kMaxTerms = 8;
+
+struct Material {
+    float ex_pref;              // 2A/(mu0 Ms)
+    float idx2, idy2, idz2;     // 1/d^2
+    int has_ext;
+    float hext[3];
+    int has_uni;
+    float ku1c, ku2c;           // 2Ku1/(mu0 Ms), 4Ku2/(mu0 Ms)
+    float u[3];
+    int has_cub;
+    float kc1c, kc2c, kc3c;     // -2Kc1/(mu0 Ms), -2Kc2/(mu0 Ms), -4Kc3/(mu0 Ms)
+    float c1[3], c2[3], c3[3];
+    float gbar;                 // gamma/(1+alpha^2)
+    float alpha;
+    float prec;                 // 1 precession on, 0 damping only
+    // energy coefficients (FP64 reductions)
+    double ku1, ku2, kc1, kc2, kc3;
+};
+
+struct Grid {
+    int nx, ny, nz;
+    long long n;
+    int px, py, pz;  // padded extents (pz == 1 on the thin-film path)
+    int nkx;         // px/2 + 1
+    int half;        // px/2
+    int nky, nkz;    // py/2+1, pz/2+1 (kernel octant extents)
+    int thin;        // 1: 2-D transform (nz == 1, pz == 1)
+};
+
+// Fused row pass: one CTA owns `rows` consecutive x-rows.  Depending on the
+// flags it (1) inverts the x-transform of the demag spectrum, (2) evaluates
+// exchange + Zeeman + anisotropy + torque, (3) accumulates FP64 statistics,
+// (4) forms the next stage input normalize(m0 + dt*sum c_j k_j), and
+// (5) forward-transforms that input along x for the next evaluation.
+struct RowPass {
+    Grid g;
+    Material mat;
+    const uint8_t *mask;
+    // (1)
+    const float2 *x_in;      // NULL: no demag
+    FftPlan xplan;           // length px/2
+    const float2 *xpost;     // e^{-2 pi i k / px}, k in [0, px/2]
+    // (2)
+    const float *m_in;       // stage input (SoA); NULL: no right-hand side in this pass
+    float *k_out;            // NULL: keep the right-hand side in registers only
+    // (3)
+    double *partials;        // NULL: no statistics; else gridDim.x * kNumStats doubles
+    int n_err;               // DP45 error terms (0: none); NULL pointer = current k
+    const float *err_k[kMaxTerms];
+    double err_c[kMaxTerms];
+    double err_dt;
+    // (4)
+    const float *m0;         // NULL: no stage combination (forward pass of m_fwd)
+    float *m_next;
+    int n_comb;
+    const float *comb_k[kMaxTerms];  // NULL entry = current k
+    float comb_c[kMaxTerms];
+    float dt;
+    // (5)
+    float2 *x_out;           // NULL: no forward transform
+    const float *m_fwd;      // forward-transform source when m0 == NULL
+    // observables
+    float *h_ex_out, *h_d_out, *h_eff_out;  // NULL: not written
+    int rows;                // rows per CTA
+};
+
+struct ColPass {
+    Grid g;
+    FftPlan plan;
+    int tx;                  // kx columns per CTA
+    const float2 *in;
+    float2 *out;
+    const float *kern;       // demag kernel (multiply passes)
+    int inverse;
+};
+
+// Launchers (kernels.cu)
+size_t row_pass_smem(const RowPass &p);
+cudaError_t launch_row_pass(const RowPass &p, cudaStream_t s);
+cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s);     // X -> Y  (3-D)
+cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s);    // Y -> Y  (3-D, z FFT, multiply, inverse)
+cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (3-D)
+cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
+cudaError_t launch_finalize_stats(const double *partials, int nblocks, double *out, cudaStream_t s);
+int row_pass_blocks(const RowPass &p);
+int col_tile(const Grid &g, int lines_per_col, int len);
+
+}  // namespace fm

@@ -1,0 +1,265 @@
+// newell.cu -- FP64 Newell demagnetisation tensor and its spectrum, built on the GPU.
+//
+// Follows the algorithm of crates/fullmag-fdm-demag/src/newell.rs:
+//   f, g base functions with log1p/atan forms            newell.rs:21-131
+//   Kahan-Neumaier 27-point second difference / (4 pi V) newell.rs:133-210
+//   point-dipole asymptotics beyond 40 cells             newell.rs:212-231, 356-373
+//   octant placement with even/odd parity                newell.rs:393-425
+// and the spectrum of crates/fullmag-engine/src/fdm_fft.rs:334-437 (2-D thin-film
+// variant: the z = 0 plane of the nz = 1 tensor).  The reference's CUDA version
+// (native/backends/fdm/src/newell_gpu_fp64.cu:384-484) computed the tensor and then
+// discarded it; here it becomes the engine's kernel.
+//
+// Because each placed component is even or odd along every axis, its DFT is real
+// and separable: along an even axis sum_i w_i N(i) cos(2 pi k i / p) with w_0 = 1,
+// w_i = 2; along an odd axis -i * sum_i 2 N(i) sin(2 pi k i / p).  Two odd axes give
+// the overall factor -1 of the off-diagonal components.  Evaluating these direct
+// real transforms in FP64 for the octant k in [0, p/2] yields exactly the stored
+// kernel, with no padded complex array and no FP64 FFT.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace fm {
+
+namespace {
+
+constexpr int kAsym = 40;
+
+__device__ double newell_f(double x, double y, double z) {
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    const double r2 = x2 + y2 + z2;
+    if (r2 < 1e-300) return 0.0;
+    const double r = sqrt(r2);
+    double acc = (2.0 * x2 - y2 - z2) * r / 6.0;
+    const double sxz = x2 + z2;
+    if (sxz > 1e-300) {
+        const double t = 2.0 * y * (y + r) / sxz;
+        if (t > -1.0) acc += y * (z2 - x2) / 4.0 * log1p(t);
+    }
+    const double sxy = x2 + y2;
+    if (sxy > 1e-300) {
+        const double t = 2.0 * z * (z + r) / sxy;
+        if (t > -1.0) acc += z * (y2 - x2) / 4.0 * log1p(t);
+    }
+    if (fabs(x) > 1e-300) acc -= x * y * z * atan(y * z / (x * r));
+    return acc;
+}
+
+__device__ double newell_g(double x, double y, double z) {
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    const double r2 = x2 + y2 + z2;
+    if (r2 < 1e-300) return 0.0;
+    const double r = sqrt(r2);
+    double acc = -x * y * r / 3.0;
+    const double sxy = x2 + y2;
+    if (sxy > 1e-300) {
+        const double t = 2.0 * z * (z + r) / sxy;
+        if (t > -1.0) acc += x * y * z * log1p(t) / 2.0;
+    }
+    const double syz = y2 + z2;
+    if (syz > 1e-300) {
+        const double t = 2.0 * x * (x + r) / syz;
+        if (t > -1.0) acc += y * (3.0 * z2 - y2) * log1p(t) / 12.0;
+    }
+    const double sxz = x2 + z2;
+    if (sxz > 1e-300) {
+        const double t = 2.0 * y * (y + r) / sxz;
+        if (t > -1.0) acc += x * (3.0 * z2 - x2) * log1p(t) / 12.0;
+    }
+    if (fabs(z) > 1e-300) acc -= z2 * z / 6.0 * atan(x * y / (z * r));
+    if (fabs(y) > 1e-300) acc -= y2 * z / 2.0 * atan(x * z / (y * r));
+    if (fabs(x) > 1e-300) acc -= x2 * z / 2.0 * atan(y * z / (x * r));
+    return acc;
+}
+
+// T[f][c][b][a]: f in {fxx, fyy, fzz, gxy, gxz, gyz} at signed offsets (a-1, b-1, c-1) cells.
+__global__ void fg_table_kernel(double *T, int sx, int sy, int sz, double dx, double dy, double dz) {
+    const long long len = (long long)sx * sy * sz;
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < len; id += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(id % sx);
+        const int b = (int)((id / sx) % sy);
+        const int c = (int)(id / ((long long)sx * sy));
+        const double x = (a - 1) * dx, y = (b - 1) * dy, z = (c - 1) * dz;
+        T[0 * len + id] = newell_f(x, y, z);
+        T[1 * len + id] = newell_f(y, x, z);
+        T[2 * len + id] = newell_f(z, y, x);
+        T[3 * len + id] = newell_g(x, y, z);
+        T[4 * len + id] = newell_g(x, z, y);
+        T[5 * len + id] = newell_g(y, z, x);
+    }
+}
+
+__device__ double stencil27(const double *t, int i, int j, int k, int sx, int sy, double inv4piv) {
+    double s = 0.0, comp = 0.0;
+    for (int dc = -1; dc <= 1; ++dc)
+        for (int db = -1; db <= 1; ++db)
+            for (int da = -1; da <= 1; ++da) {
+                const double w = (da == 0 ? 2.0 : -1.0) * (db == 0 ? 2.0 : -1.0) * (dc == 0 ? 2.0 : -1.0);
+                const double v = w * t[(long long)(k + 1 + dc) * sy * sx + (long long)(j + 1 + db) * sx + (i + 1 + da)];
+                const double u = s + v;
+                if (fabs(s) >= fabs(v)) comp += (s - u) + v;
+                else comp += (v - u) + s;
+                s = u;
+            }
+    return (s + comp) * inv4piv;
+}
+
+__device__ double asym_diag(double x, double y, double z, double vol) {
+    const double r2 = x * x + y * y + z * z, r = sqrt(r2), r3 = r2 * r;
+    return (1.0 / r3 - 3.0 * x * x / (r3 * r2)) / (4.0 * M_PI) * vol;
+}
+__device__ double asym_off(double x, double y, double z, double vol) {
+    const double r2 = x * x + y * y + z * z, r = sqrt(r2), r5 = r2 * r2 * r;
+    return -3.0 * x * y / (4.0 * M_PI * r5) * vol;
+}
+
+// First-octant tensor R[c][k][j][i], i < nx, j < ny, k < nz.
+__global__ void tensor_kernel(double *R, const double *T, int nx, int ny, int nz, int sx, int sy, int sz, double dx,
+                              double dy, double dz) {
+    const long long n = (long long)nx * ny * nz;
+    const long long tl = (long long)sx * sy * sz;
+    const double vol = dx * dy * dz;
+    const double inv = 1.0 / (4.0 * M_PI * vol);
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < n; id += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(id % nx);
+        const int j = (int)((id / nx) % ny);
+        const int k = (int)(id / ((long long)nx * ny));
+        const long long d2 = (long long)i * i + (long long)j * j + (long long)k * k;
+        double v[6];
+        if (i >= kAsym || j >= kAsym || k >= kAsym || d2 >= (long long)kAsym * kAsym) {
+            const double x = i * dx, y = j * dy, z = k * dz;
+            v[0] = asym_diag(x, y, z, vol);
+            v[1] = asym_diag(y, x, z, vol);
+            v[2] = asym_diag(z, y, x, vol);
+            v[3] = asym_off(x, y, z, vol);
+            v[4] = asym_off(x, z, y, vol);
+            v[5] = asym_off(y, z, x, vol);
+        } else {
+#pragma unroll 1
+            for (int c = 0; c < 6; ++c) v[c] = stencil27(T + c * tl, i, j, k, sx, sy, inv);
+        }
+        for (int c = 0; c < 6; ++c) R[c * n + id] = v[c];
+    }
+}
+
+// Direct real transform along one axis of layout [comp][outer][axis][inner]:
+// out[c][o][kk][b] = sum_i w_i trig(kk*i) in[c][o][i][b]; the odd flag of each
+// component selects sine (i >= 1) instead of cosine.  tw holds cos/sin of 2 pi e / p.
+__global__ void axis_transform_kernel(const double *__restrict__ in, double *__restrict__ out, int ncomp, int outer,
+                                      int nin, int nout, int inner, int p, const double2 *__restrict__ tw,
+                                      unsigned odd_mask) {
+    const long long per_out = (long long)outer * nout * inner;
+    const long long total = per_out * ncomp;
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(id / per_out);
+        long long r = id - c * per_out;
+        const int b = (int)(r % inner);
+        r /= inner;
+        const int kk = (int)(r % nout);
+        const int o = (int)(r / nout);
+        const double *src = in + (((long long)c * outer + o) * nin) * inner + b;
+        const bool odd = (odd_mask >> c) & 1u;
+        double acc = odd ? 0.0 : src[0];
+        int e = 0;  // (kk * i) mod p, advanced incrementally
+        for (int i = 1; i < nin; ++i) {
+            e += kk;
+            if (e >= p) e -= p;
+            const double2 w = tw[e];
+            acc += 2.0 * (odd ? w.y : w.x) * src[(long long)i * inner];
+        }
+        out[(((long long)c * outer + o) * nout + kk) * inner + b] = acc;
+    }
+}
+
+__global__ void to_float_kernel(const double *__restrict__ in, float *__restrict__ out, long long per, int ncomp,
+                                double scale, unsigned neg_mask) {
+    const long long total = per * ncomp;
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(id / per);
+        const double s = ((neg_mask >> c) & 1u) ? -scale : scale;
+        out[id] = (float)(in[id] * s);
+    }
+}
+
+unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152LL * 64); }
+
+}  // namespace
+
+static bool ck(cudaError_t e, const char *what, std::string &err) {
+    if (e == cudaSuccess) return true;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+// Builds the octant kernel (layout of engine.h) scaled by ms / P into `kern`.
+bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
+                         std::string &err) {
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int sx = std::min(nx, kAsym) + 2, sy = std::min(ny, kAsym) + 2, sz = std::min(nz, kAsym) + 2;
+    const long long tl = (long long)sx * sy * sz;
+    const long long n = (long long)nx * ny * nz;
+    const int ncomp = g.thin ? 4 : 6;
+    // parity bits per component (xx yy zz xy xz yz)
+    const unsigned oddx = (1u << 3) | (1u << 4), oddy = (1u << 3) | (1u << 5), oddz = (1u << 4) | (1u << 5);
+    const unsigned neg = (1u << 3) | (1u << 4) | (1u << 5);
+
+    std::vector<double2> tw;
+    std::vector<size_t> off;
+    for (int p : {g.px, g.py, g.pz}) {
+        off.push_back(tw.size());
+        for (int e = 0; e < p; ++e) {
+            const double a = 2.0 * M_PI * (double)e / (double)p;
+            tw.push_back(make_double2(cos(a), sin(a)));
+        }
+    }
+    const long long sizeA = 6LL * nz * ny * g.nkx;
+    const long long sizeB = 6LL * nz * g.nky * g.nkx;
+    const long long sizeC = 6LL * g.nkz * g.nky * g.nkx;
+    double *T = nullptr, *R = nullptr, *Ab = nullptr, *Bb = nullptr, *Cb = nullptr;
+    double2 *dtw = nullptr;
+    bool ok = ck(cudaMalloc(&T, sizeof(double) * 6 * tl), "cudaMalloc(newell table)", err) &&
+              ck(cudaMalloc(&R, sizeof(double) * 6 * n), "cudaMalloc(newell tensor)", err) &&
+              ck(cudaMalloc(&Ab, sizeof(double) * sizeA), "cudaMalloc(newell x)", err) &&
+              ck(cudaMalloc(&Bb, sizeof(double) * sizeB), "cudaMalloc(newell y)", err) &&
+              ck(cudaMalloc(&Cb, sizeof(double) * sizeC), "cudaMalloc(newell z)", err) &&
+              ck(cudaMalloc(&dtw, sizeof(double2) * tw.size()), "cudaMalloc(newell twiddles)", err);
+    if (ok) ok = ck(cudaMemcpyAsync(dtw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice, s), "twiddle copy", err);
+    if (ok) {
+        fg_table_kernel<<<grid_for(tl), 256, 0, s>>>(T, sx, sy, sz, dx, dy, dz);
+        tensor_kernel<<<grid_for(n), 256, 0, s>>>(R, T, nx, ny, nz, sx, sy, sz, dx, dy, dz);
+        // x: [c][(k,j)][i] -> [c][(k,j)][kx]
+        axis_transform_kernel<<<grid_for(sizeA), 256, 0, s>>>(R, Ab, 6, nz * ny, nx, g.nkx, 1, g.px, dtw + off[0], oddx);
+        // y: [c][k][j][kx] -> [c][k][ky][kx]
+        axis_transform_kernel<<<grid_for(sizeB), 256, 0, s>>>(Ab, Bb, 6, nz, ny, g.nky, g.nkx, g.py, dtw + off[1], oddy);
+        if (g.thin) {
+            // thin film: the k = 0 plane of (xx, yy, zz, xy); P = px * py
+            const long long per = (long long)g.nky * g.nkx;
+            const double scale = ms / ((double)g.px * g.py);
+            // components 0..3 of Bb are contiguous blocks of nz*nky*nkx = per (nz == 1)
+            to_float_kernel<<<grid_for(per * 4), 256, 0, s>>>(Bb, kern, per, 4, scale, 1u << 3);
+        } else {
+            // z: [c][k][(ky,kx)] -> [c][kz][(ky,kx)]
+            axis_transform_kernel<<<grid_for(sizeC), 256, 0, s>>>(Bb, Cb, 6, 1, nz, g.nkz, g.nky * g.nkx, g.pz, dtw + off[2],
+                                                                  oddz);
+            const long long per = (long long)g.nkz * g.nky * g.nkx;
+            const double scale = ms / ((double)g.px * g.py * g.pz);
+            to_float_kernel<<<grid_for(per * 6), 256, 0, s>>>(Cb, kern, per, 6, scale, neg);
+        }
+        ok = ck(cudaGetLastError(), "newell kernels", err) && ck(cudaStreamSynchronize(s), "newell sync", err);
+    }
+    (void)ncomp;
+    cudaFree(T);
+    cudaFree(R);
+    cudaFree(Ab);
+    cudaFree(Bb);
+    cudaFree(Cb);
+    cudaFree(dtw);
+    return ok;
+}
+
+}  // namespace fm

@@ -364,6 +364,9 @@ int fullmag_fdm_backend_device_magnetization(fullmag_fdm_backend *handle,
 /* The CUDA stream every kernel of this handle is launched on. */
 int fullmag_fdm_backend_stream(fullmag_fdm_backend *handle, void **out_stream);
 
+/* Number of kernels this handle has launched so far (instrumentation). */
+int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_count);
+
 /* Padded FFT extents the engine chose (px, py, pz; pz == 1 for the thin-film path). */
 int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
                                   uint32_t *out_py, uint32_t *out_pz);
