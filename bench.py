@@ -224,6 +224,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="timed steps only: no e2e leg, no CPU baseline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -281,6 +282,10 @@ def main():
     value = world * n * args.steps / (ms * 1e-3)
 
     # ---- e2e through the C ABI with host buffers ----
+    if args.profile:
+        be.close()
+        print(json.dumps({"profile_ms_per_step": ms_per_step, "gpu_launches": launches}), flush=True)
+        return
     m_host = np.ascontiguousarray(kw["m0"], dtype=np.float64)
     if dist:
         dist.barrier()
