@@ -1,0 +1,288 @@
+// columns.cu -- y/z transforms of the demag convolution and the tensor multiply,
+// plus the deterministic final reduction of the per-block statistics.
+//
+// Reference behaviour restated (paths in mzrptu/fullmag):
+//   tensor multiply H(k) = -N(k) M(k)          native/backends/fdm/src/demag_fp32.cu:138-164
+//                                              crates/fullmag-engine/src/fdm_fields.rs:560-588
+//   multi-pass FP64 reductions                 native/backends/fdm/src/reductions_fp64.cu:30-84,354-393
+// Here the kernel is real and octant-unique (6 floats per octant frequency), the
+// multiply sits between the forward and inverse z (3-D) or y (thin film)
+// transforms of one CTA, and the y-frequencies ky and py-ky share one CTA so
+// every octant kernel value is read from HBM once per evaluation.
+#include "engine.h"
+
+namespace fm {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void kernel_mirror(int k, int p, int &km, float &sg) {
+    if (k > p / 2) {
+        km = p - k;
+        sg = -1.f;
+    } else {
+        km = k;
+        sg = 1.f;
+    }
+}
+
+// X[c][z][y<ny][kx] -> Y[c][z][ky<py][kx] (forward along y, zero rows pruned)
+__global__ void __launch_bounds__(kThreads) y_forward_kernel(const ColPass p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int z = blockIdx.y, c = blockIdx.z;
+    const int ls = skewed_len(g.py);
+    float2 *a = reinterpret_cast<float2 *>(smem);
+    float2 *b = a + tx * ls;
+    const float2 *src = p.in + ((size_t)c * g.nz + z) * g.ny * g.nkx;
+    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
+        const int y = p.fd_tx.div(idx), col = idx - y * tx;
+        a[col * ls + sk(y)] = (y < g.ny && col < ncol) ? src[(size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *r = fft_lines(a, b, tx, ls, p.plan, false);
+    float2 *dst = p.out + ((size_t)c * g.nz + z) * g.py * g.nkx;
+    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
+        const int y = p.fd_tx.div(idx), col = idx - y * tx;
+        if (col < ncol) dst[(size_t)y * g.nkx + kx0 + col] = r[col * ls + sk(y)];
+    }
+}
+
+// Y[c][z][ky][kx] -> X[c][z][y<ny][kx] (inverse along y, only physical rows kept)
+__global__ void __launch_bounds__(kThreads) y_inverse_kernel(const ColPass p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int z = blockIdx.y, c = blockIdx.z;
+    const int ls = skewed_len(g.py);
+    float2 *a = reinterpret_cast<float2 *>(smem);
+    float2 *b = a + tx * ls;
+    const float2 *src = p.in + ((size_t)c * g.nz + z) * g.py * g.nkx;
+    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
+        const int y = p.fd_tx.div(idx), col = idx - y * tx;
+        a[col * ls + sk(y)] = col < ncol ? src[(size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *r = fft_lines(a, b, tx, ls, p.plan, true);
+    float2 *dst = p.out + ((size_t)c * g.nz + z) * g.ny * g.nkx;
+    for (int idx = threadIdx.x; idx < g.ny * tx; idx += blockDim.x) {
+        const int y = p.fd_tx.div(idx), col = idx - y * tx;
+        if (col < ncol) dst[(size_t)y * g.nkx + kx0 + col] = r[col * ls + sk(y)];
+    }
+}
+
+// Number of y-frequencies a CTA handles: ky and py - ky (1 for ky = 0 and the Nyquist row).
+__device__ __forceinline__ int ky_pair(int kya, int py, int &kyb) {
+    kyb = py - kya;
+    return (kya == 0 || kyb == kya) ? 1 : 2;
+}
+
+// 3-D: for y-frequencies (ky, py-ky) and a tile of kx, forward z-transform of the
+// nz physical planes (zero-padded to pz), multiply by -N(k), inverse, keep nz planes.
+__global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int kya = blockIdx.y;
+    int kyb;
+    const int np = ky_pair(kya, g.py, kyb);
+    const int ls = skewed_len(g.pz);
+    const int nl = np * 3 * tx;  // line (q, c, col) at ((q*3 + c)*tx + col)
+    float2 *a = reinterpret_cast<float2 *>(smem);
+    float2 *b = a + (size_t)2 * 3 * tx * ls;
+    const size_t cstride = (size_t)g.nz * g.py * g.nkx;  // component stride of Y
+    const size_t zstride = (size_t)g.py * g.nkx;
+    for (int idx = threadIdx.x; idx < np * 3 * g.pz * tx; idx += blockDim.x) {
+        const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+        const int r2 = g.fd_pz.div(r1), z = r1 - r2 * g.pz;
+        const int q = r2 / 3, c = r2 - 3 * q;
+        const int ky = q ? kyb : kya;
+        a[((q * 3 + c) * tx + col) * ls + sk(z)] =
+            (z < g.nz && col < ncol) ? p.in[c * cstride + z * zstride + (size_t)ky * g.nkx + kx0 + col]
+                                     : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *r = fft_lines(a, b, nl, ls, p.plan, false);
+    float2 *o = (r == a) ? b : a;
+    const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
+    for (int idx = threadIdx.x; idx < g.pz * tx; idx += blockDim.x) {
+        const int kz = p.fd_tx.div(idx), col = idx - kz * tx;
+        const int kx = min(kx0 + col, g.nkx - 1);
+        int kzm;
+        float sz;
+        kernel_mirror(kz, g.pz, kzm, sz);
+        const float *K = p.kern + ((size_t)kzm * g.nky + kya) * g.nkx + kx;
+        const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
+        const float kxy0 = __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz0 = sz * __ldg(K + 5 * kc);
+        for (int q = 0; q < np; ++q) {
+            // the second frequency of the pair is the y-mirror: odd-in-y components flip sign
+            const float sy = q ? -1.f : 1.f;
+            const float kxy = sy * kxy0, kyz = sy * kyz0;
+            float2 *lx = r + ((q * 3 + 0) * tx + col) * ls + sk(kz);
+            float2 *ly = r + ((q * 3 + 1) * tx + col) * ls + sk(kz);
+            float2 *lz = r + ((q * 3 + 2) * tx + col) * ls + sk(kz);
+            const float2 mx = *lx, my = *ly, mz = *lz;
+            *lx = make_float2(-(kxx * mx.x + kxy * my.x + kxz * mz.x), -(kxx * mx.y + kxy * my.y + kxz * mz.y));
+            *ly = make_float2(-(kxy * mx.x + kyy * my.x + kyz * mz.x), -(kxy * mx.y + kyy * my.y + kyz * mz.y));
+            *lz = make_float2(-(kxz * mx.x + kyz * my.x + kzz * mz.x), -(kxz * mx.y + kyz * my.y + kzz * mz.y));
+        }
+    }
+    __syncthreads();
+    float2 *qb = fft_lines(r, o, nl, ls, p.plan, true);
+    for (int idx = threadIdx.x; idx < np * 3 * g.nz * tx; idx += blockDim.x) {
+        const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+        const int r2 = g.fd_nz.div(r1), z = r1 - r2 * g.nz;
+        const int q = r2 / 3, c = r2 - 3 * q;
+        const int ky = q ? kyb : kya;
+        if (col < ncol)
+            p.out[c * cstride + z * zstride + (size_t)ky * g.nkx + kx0 + col] = qb[((q * 3 + c) * tx + col) * ls + sk(z)];
+    }
+}
+
+// Thin film: forward y-transform of ny physical rows (zero-padded to py), multiply by
+// the 2-D kernel, inverse, keep ny rows.  X -> X in place.
+__global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int ls = skewed_len(g.py);
+    const int nl = 3 * tx;
+    float2 *a = reinterpret_cast<float2 *>(smem);
+    float2 *b = a + nl * ls;
+    const size_t cstride = (size_t)g.ny * g.nkx;
+    for (int idx = threadIdx.x; idx < 3 * g.py * tx; idx += blockDim.x) {
+        const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+        const int c = g.fd_py.div(r1), y = r1 - c * g.py;
+        a[(c * tx + col) * ls + sk(y)] =
+            (y < g.ny && col < ncol) ? p.in[c * cstride + (size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *r = fft_lines(a, b, nl, ls, p.plan, false);
+    float2 *o = (r == a) ? b : a;
+    const size_t kc = (size_t)g.nky * g.nkx;
+    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
+        const int ky = p.fd_tx.div(idx), col = idx - ky * tx;
+        const int kx = min(kx0 + col, g.nkx - 1);
+        int kym;
+        float sy;
+        kernel_mirror(ky, g.py, kym, sy);
+        const float *K = p.kern + (size_t)kym * g.nkx + kx;
+        const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc), kxy = sy * __ldg(K + 3 * kc);
+        float2 *lx = r + (0 * tx + col) * ls + sk(ky);
+        float2 *ly = r + (1 * tx + col) * ls + sk(ky);
+        float2 *lz = r + (2 * tx + col) * ls + sk(ky);
+        const float2 mx = *lx, my = *ly, mz = *lz;
+        *lx = make_float2(-(kxx * mx.x + kxy * my.x), -(kxx * mx.y + kxy * my.y));
+        *ly = make_float2(-(kxy * mx.x + kyy * my.x), -(kxy * mx.y + kyy * my.y));
+        *lz = make_float2(-(kzz * mz.x), -(kzz * mz.y));
+    }
+    __syncthreads();
+    float2 *q = fft_lines(r, o, nl, ls, p.plan, true);
+    for (int idx = threadIdx.x; idx < 3 * g.ny * tx; idx += blockDim.x) {
+        const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+        const int c = g.fd_ny.div(r1), y = r1 - c * g.ny;
+        if (col < ncol) p.out[c * cstride + (size_t)y * g.nkx + kx0 + col] = q[(c * tx + col) * ls + sk(y)];
+    }
+}
+
+// Deterministic final reduction of the per-block partials (layout [stat][block] of
+// float-float pairs): 1024 threads stride over the blocks with compensated TwoSum
+// accumulation for the energies and max for the norms, then a fixed-order tree
+// combines the threads.  GB300's FP64 rate is a small fraction of its FP32 rate, so
+// the compensation runs on FP32 pipes; only the final hi + lo is formed in FP64.
+constexpr int kFinThreads = 1024;
+
+__global__ void __launch_bounds__(kFinThreads) finalize_stats_kernel(const float2 *__restrict__ partials, int nblocks,
+                                                                     double *__restrict__ out) {
+    __shared__ float2 sh[kFinThreads];
+    for (int s = 0; s < kNumStats; ++s) {
+        const bool is_sum = s < 5;
+        const float2 *src = partials + (size_t)s * nblocks;
+        float h = 0.f, l = 0.f;
+        for (int b = threadIdx.x; b < nblocks; b += kFinThreads) {
+            const float2 v = src[b];
+            if (is_sum) {
+                ff_add(h, l, v.x);
+                l += v.y;
+            } else {
+                h = fmaxf(h, v.x);
+            }
+        }
+        sh[threadIdx.x] = make_float2(h, l);
+        __syncthreads();
+        for (int w = kFinThreads / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) {
+                float2 a = sh[threadIdx.x];
+                const float2 b = sh[threadIdx.x + w];
+                if (is_sum) {
+                    ff_add(a.x, a.y, b.x);
+                    a.y += b.y;
+                } else {
+                    a.x = fmaxf(a.x, b.x);
+                }
+                sh[threadIdx.x] = a;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[s] = (double)sh[0].x + (double)sh[0].y;
+        __syncthreads();
+    }
+}
+
+cudaError_t ensure_smem(const void *fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+unsigned tiles(const ColPass &p) { return (unsigned)((p.g.nkx + p.tx - 1) / p.tx); }
+
+}  // namespace
+
+int col_tile(const Grid &g, int lines_per_col, int len) {
+    // largest tile (<= 8 kx columns) whose two ping-pong buffers fit in 200 KB
+    int tx = 8;
+    while (tx > 1 && (size_t)2 * lines_per_col * tx * skewed_len(len) * sizeof(float2) > 200u * 1024u) tx >>= 1;
+    return tx;
+}
+
+cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s) {
+    const size_t sm = 2 * sizeof(float2) * (size_t)p.tx * skewed_len(p.g.py);
+    cudaError_t e = ensure_smem((const void *)y_forward_kernel, sm);
+    if (e != cudaSuccess) return e;
+    y_forward_kernel<<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s) {
+    const size_t sm = 2 * sizeof(float2) * (size_t)p.tx * skewed_len(p.g.py);
+    cudaError_t e = ensure_smem((const void *)y_inverse_kernel, sm);
+    if (e != cudaSuccess) return e;
+    y_inverse_kernel<<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
+    // room for a y-frequency pair: 2 x 3 lines per kx column, two ping-pong buffers
+    const size_t sm = 2 * sizeof(float2) * (size_t)2 * 3 * p.tx * skewed_len(p.g.pz);
+    cudaError_t e = ensure_smem((const void *)z_convolve_kernel, sm);
+    if (e != cudaSuccess) return e;
+    z_convolve_kernel<<<dim3(tiles(p), p.g.nky), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s) {
+    const size_t sm = 2 * sizeof(float2) * (size_t)3 * p.tx * skewed_len(p.g.py);
+    cudaError_t e = ensure_smem((const void *)y_convolve_2d_kernel, sm);
+    if (e != cudaSuccess) return e;
+    y_convolve_2d_kernel<<<tiles(p), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s) {
+    finalize_stats_kernel<<<1, kFinThreads, 0, s>>>(partials, nblocks, out);
+    return cudaGetLastError();
+}
+
+}  // namespace fm

@@ -78,7 +78,7 @@ struct Engine {
     float2 *X = nullptr, *Y = nullptr;
     float *kern = nullptr;
     uint8_t *mask = nullptr;
-    double *partials = nullptr;
+    float2 *partials = nullptr;  // [kNumStats][row blocks] float-float partial sums
     double *dstats = nullptr;
     double *hstats = nullptr;  // pinned
     float2 *twid = nullptr;
@@ -108,6 +108,7 @@ struct Engine {
 
     void release() {
         if (stream) cudaStreamSynchronize(stream);
+        drop_graphs();
         if (arena) cudaFree(arena);
         arena = nullptr;
         if (staging) cudaFree(staging);
@@ -157,6 +158,12 @@ struct Engine {
             }
         p.n = n;
         p.nstages = (int)r.size();
+        p.log2n = -1;
+        if (n >= 2 && (n & (n - 1)) == 0) {
+            int l = 0;
+            while ((1 << l) < n) ++l;
+            p.log2n = l;
+        }
         for (int i = 0; i < p.nstages; ++i) p.radix[i] = r[i];
         offs.push_back(host_tw.size());
         for (int e = 0; e < n; ++e) {
@@ -213,6 +220,7 @@ struct Engine {
         if (g.thin) {
             c.plan = plan_y;
             c.tx = col_tile(g, 3, g.py);
+            c.fd_tx = FastDiv((uint32_t)c.tx);
             c.in = X;
             c.out = X;
             launches += 1;
@@ -220,16 +228,19 @@ struct Engine {
         }
         c.plan = plan_y;
         c.tx = col_tile(g, 1, g.py);
+        c.fd_tx = FastDiv((uint32_t)c.tx);
         c.in = X;
         c.out = Y;
         if (cuda_fail("y forward", launch_y_forward(c, stream))) return false;
         c.plan = plan_z;
-        c.tx = col_tile(g, 3, g.pz);
+        c.tx = col_tile(g, 6, g.pz);
+        c.fd_tx = FastDiv((uint32_t)c.tx);
         c.in = Y;
         c.out = Y;
         if (cuda_fail("z convolve", launch_z_convolve(c, stream))) return false;
         c.plan = plan_y;
         c.tx = col_tile(g, 1, g.py);
+        c.fd_tx = FastDiv((uint32_t)c.tx);
         c.in = Y;
         c.out = X;
         launches += 3;
@@ -245,14 +256,14 @@ struct Engine {
         return run_row(p) && run_columns();
     }
 
-    bool read_stats() {
+    bool enqueue_stats() {
         launches += 1;
         if (cuda_fail("finalize", launch_finalize_stats(partials, max_row_blocks, dstats, stream))) return false;
-        if (cuda_fail("stats copy", cudaMemcpyAsync(hstats, dstats, sizeof(double) * kNumStats, cudaMemcpyDeviceToHost, stream)))
-            return false;
-        if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return false;
-        return true;
+        return !cuda_fail("stats copy",
+                          cudaMemcpyAsync(hstats, dstats, sizeof(double) * kNumStats, cudaMemcpyDeviceToHost, stream));
     }
+
+    bool read_stats() { return enqueue_stats() && !cuda_fail("stream sync", cudaStreamSynchronize(stream)); }
 
     void fill_stats(const double *d, fullmag_fdm_step_stats &st) const {
         const double V = dx * dy * dz;
@@ -313,7 +324,8 @@ struct Engine {
     }
 
     // Final RHS of an attempt (at the proposed state) with statistics and optional error terms.
-    bool final_eval(const float *m_in, float *k_out, int nerr, const int *kidx, const double *coef, double dt) {
+    bool final_eval(const float *m_in, float *k_out, int nerr, const int *kidx, const double *coef, double dt,
+                    bool sync = true) {
         RowPass p = row_base();
         p.x_in = X;
         p.m_in = m_in;
@@ -325,7 +337,104 @@ struct Engine {
             p.err_c[t] = coef[t];
         }
         p.err_dt = dt;
-        return run_row(p) && read_stats();
+        return run_row(p) && (sync ? read_stats() : enqueue_stats());
+    }
+
+    // ---- fixed-step integrators: the whole step as one CUDA graph ----
+    // One executable per state parity (the committed state alternates between
+    // S[0] and S[1]); re-captured when dt changes.  With an interrupt poll
+    // installed the step runs pass by pass instead, polling in between.
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    double gdt[2] = {0.0, 0.0};
+    uint64_t gkernels[2] = {0, 0};
+    bool use_graphs = true;
+
+    void drop_graphs() {
+        for (int c = 0; c < 2; ++c) {
+            if (gexec[c]) cudaGraphExecDestroy(gexec[c]);
+            gexec[c] = nullptr;
+        }
+    }
+
+    // Enqueues a Heun or RK4 step from S[cur] into S[1-cur]; `poll_between`
+    // checks the interrupt callback between passes (eager mode only).
+    int enqueue_fixed_step(double dt, bool poll_between) {
+        const int nxt = 1 - cur;
+        if (integrator == FULLMAG_FDM_INTEGRATOR_RK4) {
+            const int self[1] = {-1};
+            const double h[1] = {0.5}, one[1] = {1.0};
+            const int k0[1] = {0};
+            if (!stage(nullptr, nullptr, 1, k0, h, dt, A[0])) return -1;
+            if (poll_between && poll_hit()) return 1;
+            if (!stage(A[0], K[1], 1, self, h, dt, A[1])) return -1;
+            if (poll_between && poll_hit()) return 1;
+            if (!stage(A[1], K[2], 1, self, one, dt, A[0])) return -1;
+            if (poll_between && poll_hit()) return 1;
+            const int k[4] = {0, 1, 2, -1};
+            const double c[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+            if (!stage(A[0], nullptr, 4, k, c, dt, S[nxt])) return -1;
+        } else {
+            const int k0[1] = {0};
+            const double c1[1] = {1.0};
+            if (!stage(nullptr, nullptr, 1, k0, c1, dt, A[0])) return -1;
+            if (poll_between && poll_hit()) return 1;
+            const int k[2] = {0, -1};
+            const double c[2] = {0.5, 0.5};
+            if (!stage(A[0], nullptr, 2, k, c, dt, S[nxt])) return -1;
+        }
+        return final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt, poll_between) ? 0 : -1;
+    }
+
+    bool capture_step(double dt) {
+        if (gexec[cur]) {
+            cudaGraphExecDestroy(gexec[cur]);
+            gexec[cur] = nullptr;
+        }
+        const uint64_t l0 = launches;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+        const int rc = enqueue_fixed_step(dt, false);
+        const cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        launches = l0;
+        if (rc != 0 || e != cudaSuccess || graph == nullptr) {
+            if (graph) cudaGraphDestroy(graph);
+            return false;
+        }
+        size_t nnodes = 0;
+        cudaGraphGetNodes(graph, nullptr, &nnodes);
+        const cudaError_t ie = cudaGraphInstantiate(&gexec[cur], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            gexec[cur] = nullptr;
+            return false;
+        }
+        gkernels[cur] = nnodes > 0 ? nnodes - 1 : 0;  // every node but the stats copy is a kernel
+        gdt[cur] = dt;
+        return true;
+    }
+
+    int step_fixed(double dt) {
+        if (!ensure_k1()) return -1;
+        if (poll_hit()) return 1;
+        if (poll == nullptr && use_graphs) {
+            if ((!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
+                // capture unavailable: clear the sticky state and fall back to eager launches
+                cudaGetLastError();
+                use_graphs = false;
+                last_error.clear();
+            }
+            if (use_graphs) {
+                if (cuda_fail("graph launch", cudaGraphLaunch(gexec[cur], stream))) return -1;
+                launches += gkernels[cur];
+                if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
+                commit(dt, hstats);
+                return 0;
+            }
+        }
+        const int rc = enqueue_fixed_step(dt, true);
+        if (rc != 0) return rc;
+        commit(dt, hstats);
+        return 0;
     }
 
     bool ensure_k1() { return k1_valid || eval_state(false); }
@@ -346,51 +455,6 @@ struct Engine {
     }
 
     // ---- integrators: return 0 ok, 1 interrupted, -1 error ----
-    int step_heun(double dt) {
-        if (!ensure_k1()) return -1;
-        if (poll_hit()) return 1;
-        const int nxt = 1 - cur;
-        {
-            const int k[1] = {0};
-            const double c[1] = {1.0};
-            if (!stage(nullptr, nullptr, 1, k, c, dt, A[0])) return -1;
-        }
-        if (poll_hit()) return 1;
-        {
-            const int k[2] = {0, -1};
-            const double c[2] = {0.5, 0.5};
-            if (!stage(A[0], nullptr, 2, k, c, dt, S[nxt])) return -1;
-        }
-        if (!final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt)) return -1;
-        commit(dt, hstats);
-        return 0;
-    }
-
-    int step_rk4(double dt) {
-        if (!ensure_k1()) return -1;
-        if (poll_hit()) return 1;
-        const int nxt = 1 - cur;
-        const int self[1] = {-1};
-        const double h[1] = {0.5}, one[1] = {1.0};
-        {
-            const int k[1] = {0};
-            if (!stage(nullptr, nullptr, 1, k, h, dt, A[0])) return -1;
-        }
-        if (poll_hit()) return 1;
-        if (!stage(A[0], K[1], 1, self, h, dt, A[1])) return -1;
-        if (poll_hit()) return 1;
-        if (!stage(A[1], K[2], 1, self, one, dt, A[0])) return -1;
-        if (poll_hit()) return 1;
-        {
-            const int k[4] = {0, 1, 2, -1};
-            const double c[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
-            if (!stage(A[0], nullptr, 4, k, c, dt, S[nxt])) return -1;
-        }
-        if (!final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt)) return -1;
-        commit(dt, hstats);
-        return 0;
-    }
-
     int step_dp45(double dt) {
         static const double a21 = 1.0 / 5.0;
         static const double a3[2] = {3.0 / 40.0, 9.0 / 40.0};
@@ -455,9 +519,9 @@ struct Engine {
     int step(double dt) {
         interrupted = false;
         switch (integrator) {
-            case FULLMAG_FDM_INTEGRATOR_RK4: return step_rk4(dt);
+            case FULLMAG_FDM_INTEGRATOR_RK4: return step_fixed(dt);
             case FULLMAG_FDM_INTEGRATOR_DP45: return step_dp45(dt);
-            default: return step_heun(dt);
+            default: return step_fixed(dt);
         }
     }
 
@@ -683,6 +747,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     g.nkx = g.half + 1;
     g.nky = g.py / 2 + 1;
     g.nkz = g.pz / 2 + 1;
+    grid_dividers(g);
 
     // ---- material constants ----
     const double mu0ms = kMu0 * ms;
@@ -704,8 +769,8 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         for (int c = 0; c < 3; ++c) mat.u[c] = (float)u[c];
         mat.ku1c = (float)(2.0 * plan->uniaxial_anisotropy_constant / mu0ms);
         mat.ku2c = (float)(4.0 * plan->uniaxial_anisotropy_k2 / mu0ms);
-        mat.ku1 = plan->uniaxial_anisotropy_constant;
-        mat.ku2 = plan->uniaxial_anisotropy_k2;
+        mat.ku1f = (float)plan->uniaxial_anisotropy_constant;
+        mat.ku2f = (float)plan->uniaxial_anisotropy_k2;
     }
     mat.has_cub = has_cub;
     if (has_cub) {
@@ -721,9 +786,9 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         mat.kc1c = (float)(-2.0 * plan->cubic_Kc1 / mu0ms);
         mat.kc2c = (float)(-2.0 * plan->cubic_Kc2 / mu0ms);
         mat.kc3c = (float)(-4.0 * plan->cubic_Kc3 / mu0ms);
-        mat.kc1 = plan->cubic_Kc1;
-        mat.kc2 = plan->cubic_Kc2;
-        mat.kc3 = plan->cubic_Kc3;
+        mat.kc1f = (float)plan->cubic_Kc1;
+        mat.kc2f = (float)plan->cubic_Kc2;
+        mat.kc3f = (float)plan->cubic_Kc3;
     }
     mat.gbar = (float)(gamma / (1.0 + alpha * alpha));
     mat.alpha = (float)alpha;
@@ -748,7 +813,8 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
 
     // ---- arena ----
     nk = integrator == FULLMAG_FDM_INTEGRATOR_DP45 ? 7 : (integrator == FULLMAG_FDM_INTEGRATOR_RK4 ? 3 : 1);
-    row_rows = std::max(1, std::min(16, 256 / std::max(1, g.nx)));
+    const char *rr_env = std::getenv("FULLMAG_FDM_ROWS_PER_CTA");
+    row_rows = rr_env ? std::max(1, std::atoi(rr_env)) : std::max(1, std::min(16, 512 / std::max(1, g.nx)));
     max_row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
     const size_t vec = sizeof(float) * 3 * (size_t)g.n;
     const size_t xlen = demag ? sizeof(float2) * 3 * (size_t)g.nz * g.ny * g.nkx : 0;
@@ -766,7 +832,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     take(vec); take(vec); take(vec);                        // observables
     take(xlen); take(ylen); take(klen);                     // spectra + kernel
     take(has_mask ? (size_t)g.n : 0);                       // mask
-    take(sizeof(double) * kNumStats * (size_t)max_row_blocks);
+    take(sizeof(float2) * kNumStats * (size_t)max_row_blocks);
     take(sizeof(double) * kNumStats);
     take(sizeof(float2) * tw.size());
     arena_bytes = off;
@@ -789,7 +855,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     q++;
     mask = has_mask ? (uint8_t *)(arena + o[q]) : nullptr;
     q++;
-    partials = (double *)(arena + o[q++]);
+    partials = (float2 *)(arena + o[q++]);
     dstats = (double *)(arena + o[q++]);
     twid = (float2 *)(arena + o[q++]);
     if (cuda_fail("cudaMallocHost(stats)", cudaMallocHost((void **)&hstats, sizeof(double) * kNumStats))) return false;

@@ -34,8 +34,8 @@ struct Material {
     float gbar;                 // gamma/(1+alpha^2)
     float alpha;
     float prec;                 // 1 precession on, 0 damping only
-    // energy coefficients (FP64 reductions)
-    double ku1, ku2, kc1, kc2, kc3;
+    // energy densities (raw Ku, Kc in J/m^3) for the float-float reductions
+    float ku1f, ku2f, kc1f, kc2f, kc3f;
 };
 
 struct Grid {
@@ -46,7 +46,20 @@ struct Grid {
     int half;        // px/2
     int nky, nkz;    // py/2+1, pz/2+1 (kernel octant extents)
     int thin;        // 1: 2-D transform (nz == 1, pz == 1)
+    // dividers for the index arithmetic of the passes
+    FastDiv fd_nx, fd_ny, fd_nz, fd_half, fd_nkx, fd_py, fd_pz, fd_padw;
 };
+
+inline void grid_dividers(Grid &g) {
+    g.fd_nx = FastDiv((uint32_t)g.nx);
+    g.fd_ny = FastDiv((uint32_t)g.ny);
+    g.fd_nz = FastDiv((uint32_t)g.nz);
+    g.fd_half = FastDiv((uint32_t)g.half);
+    g.fd_nkx = FastDiv((uint32_t)g.nkx);
+    g.fd_py = FastDiv((uint32_t)g.py);
+    g.fd_pz = FastDiv((uint32_t)g.pz);
+    g.fd_padw = FastDiv((uint32_t)(2 * g.half - g.nx > 0 ? 2 * g.half - g.nx : 1));
+}
 
 // Fused row pass: one CTA owns `rows` consecutive x-rows.  Depending on the
 // flags it (1) inverts the x-transform of the demag spectrum, (2) evaluates
@@ -65,7 +78,7 @@ struct RowPass {
     const float *m_in;       // stage input (SoA); NULL: no right-hand side in this pass
     float *k_out;            // NULL: keep the right-hand side in registers only
     // (3)
-    double *partials;        // NULL: no statistics; else gridDim.x * kNumStats doubles
+    float2 *partials;        // NULL: no statistics; else [kNumStats][gridDim.x] (hi, lo) pairs
     int n_err;               // DP45 error terms (0: none); NULL pointer = current k
     const float *err_k[kMaxTerms];
     double err_c[kMaxTerms];
@@ -89,6 +102,7 @@ struct ColPass {
     Grid g;
     FftPlan plan;
     int tx;                  // kx columns per CTA
+    FastDiv fd_tx;
     const float2 *in;
     float2 *out;
     const float *kern;       // demag kernel (multiply passes)
@@ -102,7 +116,7 @@ cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s);     // X -> Y  (
 cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s);    // Y -> Y  (3-D, z FFT, multiply, inverse)
 cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (3-D)
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
-cudaError_t launch_finalize_stats(const double *partials, int nblocks, double *out, cudaStream_t s);
+cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s);
 int row_pass_blocks(const RowPass &p);
 int col_tile(const Grid &g, int lines_per_col, int len);
 

@@ -1,0 +1,393 @@
+// row_pass.cu -- the fused per-row pass: inverse x-transform of the demag
+// spectrum, exchange + Zeeman + anisotropy + LLG torque, FP64 statistics,
+// next-stage combination and forward x-transform.
+//
+// Reference behaviour restated here (paths in mzrptu/fullmag):
+//   exchange stencil, Neumann clamp, mask      native/backends/fdm/src/exchange_fp32.cu:21-122
+//                                              crates/fullmag-engine/src/fdm_fields.rs:445-527
+//   zero-padded tensor convolution             native/backends/fdm/src/demag_fp32.cu:50-199,406-502
+//                                              crates/fullmag-engine/src/fdm_fields.rs:528-609
+//   Zeeman + uniaxial + cubic local terms      native/backends/fdm/src/demag_fp32.cu:201-318
+//   LLG right-hand side                        native/backends/fdm/src/llg_fp32.cu:32-60
+//                                              crates/fullmag-engine/src/fdm_fields.rs:2151-2162
+//   stage combination with normalisation      native/backends/fdm/src/llg_fp32.cu:204-261,
+//                                              llg_rk4_fp32.cu:37-80, llg_dp45_fp32.cu:37-106
+//   energies and max norms (FP64 accumulate)   native/backends/fdm/src/reductions_fp64.cu:123-342,605-642
+//   DP45 error norm                            native/backends/fdm/src/llg_dp45_fp32.cu:108-128,175-184
+// The structure is new: the x-transforms live inside the per-row pass, the
+// y/z transforms and the tensor multiply live in column passes, and no
+// padded real-space array or cuFFT plan exists.
+#include "engine.h"
+
+#include <cfloat>
+
+namespace fm {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// a / (2i) = -i a / 2
+__device__ __forceinline__ float2 div2i(float2 a) { return make_float2(0.5f * a.y, -0.5f * a.x); }
+__device__ __forceinline__ float2 mul_i(float2 a) { return make_float2(-a.y, a.x); }
+
+__device__ __forceinline__ bool cell_active(const uint8_t *mask, long long i) { return mask == nullptr || mask[i] != 0; }
+
+// butterfly all-reduce of a float-float value; every lane ends with the same bits
+// because each level combines the pair in lane order
+__device__ __forceinline__ void warp_ff_sum(float &h, float &l) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+        const bool low = (threadIdx.x & o) == 0;
+        float ah = low ? h : oh, al = low ? l : ol;
+        const float bh = low ? oh : h, bl = low ? ol : l;
+        ff_add(ah, al, bh);
+        h = ah;
+        l = al + bl;
+    }
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int nx = g.nx, half = g.half, nkx = g.nkx;
+    const long long n = g.n;
+    const int nrows = g.ny * g.nz;
+    const int row0 = blockIdx.x * p.rows;
+    const int rows = min(p.rows, nrows - row0);
+    const bool use_fft = (p.x_in != nullptr) || (p.x_out != nullptr);
+    const int lsx = skewed_len(half);  // line stride of the x-transform buffers
+    const int flen = p.rows * 3 * lsx;
+    float2 *fa = reinterpret_cast<float2 *>(smem);
+    float2 *fb = fa + (use_fft ? flen : 0);
+    float2 *red = fb + (use_fft ? flen : 0);  // per-warp statistics
+
+    // ---- (1) inverse x-transform of the demag spectrum ----
+    float2 *hd = nullptr;
+    if (p.x_in) {
+        for (int idx = threadIdx.x; idx < rows * 3 * half; idx += blockDim.x) {
+            const int r1 = g.fd_half.div(idx), k = idx - r1 * half;
+            const int rr = r1 / 3, c = r1 - 3 * rr;
+            const float2 *X = p.x_in + ((size_t)c * nrows + row0 + rr) * nkx;
+            const float2 a = X[k];
+            const float2 b = cconj(X[half - k]);
+            const float2 E = cadd(a, b);
+            const float2 O = cmul(csub(a, b), cconj(__ldg(p.xpost + k)));
+            fa[(rr * 3 + c) * lsx + sk(k)] = cadd(E, mul_i(O));
+        }
+        __syncthreads();
+        hd = fft_lines(fa, fb, rows * 3, lsx, p.xplan, true);
+    }
+    float2 *pack = (hd == fb) ? fa : fb;  // free buffer for the forward transform input
+
+    // ---- (2)-(4) per-cell work ----
+    // statistics: compensated float-float sums (TwoSum) for the energies, FP32 maxima
+    // of squared norms; FP64 only for the per-cell DP45 error combination
+    float sum_hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sum_lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    float mx2[4] = {0.f, 0.f, 0.f, 0.f};
+    const Material &M = p.mat;
+    for (int idx = threadIdx.x; idx < rows * nx; idx += blockDim.x) {
+        const int rr = g.fd_nx.div(idx);
+        const int x = idx - rr * nx;
+        const int row = row0 + rr;
+        const int z = g.fd_ny.div(row);
+        const int y = row - z * g.ny;
+        const long long i = (long long)row * nx + x;
+        const bool act = cell_active(p.mask, i);
+        float kx_ = 0.f, ky_ = 0.f, kz_ = 0.f;
+        if (p.m_in) {
+            const float *mi = p.m_in;
+            const float m0x = mi[i], m0y = mi[n + i], m0z = mi[2 * n + i];
+            float hx = 0.f, hy = 0.f, hz = 0.f;      // effective field
+            float ex = 0.f, ey = 0.f, ez = 0.f;      // exchange
+            float dx_ = 0.f, dy_ = 0.f, dz_ = 0.f;   // demag
+            float e_pair = 0.f;
+            if (act) {
+                if (M.ex_pref != 0.f) {
+                    long long nb[6];
+                    nb[0] = x > 0 ? i - 1 : i;
+                    nb[1] = x < nx - 1 ? i + 1 : i;
+                    nb[2] = y > 0 ? i - nx : i;
+                    nb[3] = y < g.ny - 1 ? i + nx : i;
+                    nb[4] = z > 0 ? i - (long long)nx * g.ny : i;
+                    nb[5] = z < g.nz - 1 ? i + (long long)nx * g.ny : i;
+                    if (p.mask) {
+#pragma unroll
+                        for (int q = 0; q < 6; ++q)
+                            if (p.mask[nb[q]] == 0) nb[q] = i;
+                    }
+                    float v[6][3];
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        v[q][0] = mi[nb[q]];
+                        v[q][1] = mi[n + nb[q]];
+                        v[q][2] = mi[2 * n + nb[q]];
+                    }
+                    const float c0[3] = {m0x, m0y, m0z};
+                    float e3[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        e3[c] = M.ex_pref * ((v[1][c] - 2.f * c0[c] + v[0][c]) * M.idx2 +
+                                             (v[3][c] - 2.f * c0[c] + v[2][c]) * M.idy2 +
+                                             (v[5][c] - 2.f * c0[c] + v[4][c]) * M.idz2);
+                    ex = e3[0];
+                    ey = e3[1];
+                    ez = e3[2];
+                    if (p.partials) {
+                        // forward pairs only (x+1, y+1, z+1), each active pair once
+                        const float w[3] = {M.idx2, M.idy2, M.idz2};
+                        const bool has[3] = {x < nx - 1, y < g.ny - 1, z < g.nz - 1};
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            const int q = 2 * a + 1;
+                            if (has[a] && nb[q] != i) {
+                                const float d0 = v[q][0] - m0x, d1 = v[q][1] - m0y, d2 = v[q][2] - m0z;
+                                e_pair += (d0 * d0 + d1 * d1 + d2 * d2) * w[a];
+                            }
+                        }
+                    }
+                }
+                if (hd) {
+                    const float2 a = hd[(rr * 3 + 0) * lsx + sk(x >> 1)];
+                    const float2 b = hd[(rr * 3 + 1) * lsx + sk(x >> 1)];
+                    const float2 c = hd[(rr * 3 + 2) * lsx + sk(x >> 1)];
+                    dx_ = (x & 1) ? a.y : a.x;
+                    dy_ = (x & 1) ? b.y : b.x;
+                    dz_ = (x & 1) ? c.y : c.x;
+                }
+                hx = ex + dx_;
+                hy = ey + dy_;
+                hz = ez + dz_;
+                if (M.has_ext) {
+                    hx += M.hext[0];
+                    hy += M.hext[1];
+                    hz += M.hext[2];
+                }
+                float e_uni = 0.f, e_cub = 0.f;
+                if (M.has_uni) {
+                    const float mu = m0x * M.u[0] + m0y * M.u[1] + m0z * M.u[2];
+                    const float cf = M.ku1c * mu + M.ku2c * mu * mu * mu;
+                    hx += cf * M.u[0];
+                    hy += cf * M.u[1];
+                    hz += cf * M.u[2];
+                    const float s = mu * mu;
+                    e_uni = M.ku1f * s + M.ku2f * s * s;
+                }
+                if (M.has_cub) {
+                    const float a1 = m0x * M.c1[0] + m0y * M.c1[1] + m0z * M.c1[2];
+                    const float a2 = m0x * M.c2[0] + m0y * M.c2[1] + m0z * M.c2[2];
+                    const float a3 = m0x * M.c3[0] + m0y * M.c3[1] + m0z * M.c3[2];
+                    const float s1 = a1 * a1, s2 = a2 * a2, s3 = a3 * a3;
+                    const float sig = s1 * s2 + s2 * s3 + s1 * s3;
+                    const float g1 = M.kc1c * a1 * (s2 + s3) + M.kc2c * a1 * s2 * s3 + M.kc3c * sig * a1 * (s2 + s3);
+                    const float g2 = M.kc1c * a2 * (s1 + s3) + M.kc2c * a2 * s1 * s3 + M.kc3c * sig * a2 * (s1 + s3);
+                    const float g3 = M.kc1c * a3 * (s1 + s2) + M.kc2c * a3 * s1 * s2 + M.kc3c * sig * a3 * (s1 + s2);
+                    hx += g1 * M.c1[0] + g2 * M.c2[0] + g3 * M.c3[0];
+                    hy += g1 * M.c1[1] + g2 * M.c2[1] + g3 * M.c3[1];
+                    hz += g1 * M.c1[2] + g2 * M.c2[2] + g3 * M.c3[2];
+                    e_cub = M.kc1f * sig + M.kc2f * s1 * s2 * s3 + M.kc3f * sig * sig;
+                }
+                // LLG: k = -gbar (m x H + alpha m x (m x H))
+                const float px_ = m0y * hz - m0z * hy;
+                const float py_ = m0z * hx - m0x * hz;
+                const float pz_ = m0x * hy - m0y * hx;
+                const float qx = m0y * pz_ - m0z * py_;
+                const float qy = m0z * px_ - m0x * pz_;
+                const float qz = m0x * py_ - m0y * px_;
+                kx_ = -M.gbar * (M.prec * px_ + M.alpha * qx);
+                ky_ = -M.gbar * (M.prec * py_ + M.alpha * qy);
+                kz_ = -M.gbar * (M.prec * pz_ + M.alpha * qz);
+                if (p.partials) {
+                    ff_add(sum_hi[0], sum_lo[0], e_pair);
+                    ff_add(sum_hi[1], sum_lo[1], m0x * dx_ + m0y * dy_ + m0z * dz_);
+                    if (M.has_ext) ff_add(sum_hi[2], sum_lo[2], m0x * M.hext[0] + m0y * M.hext[1] + m0z * M.hext[2]);
+                    ff_add(sum_hi[3], sum_lo[3], e_uni);
+                    ff_add(sum_hi[4], sum_lo[4], e_cub);
+                    mx2[0] = fmaxf(mx2[0], hx * hx + hy * hy + hz * hz);
+                    mx2[1] = fmaxf(mx2[1], dx_ * dx_ + dy_ * dy_ + dz_ * dz_);
+                    mx2[2] = fmaxf(mx2[2], kx_ * kx_ + ky_ * ky_ + kz_ * kz_);
+                }
+            }
+            if (p.partials && p.n_err > 0) {
+                double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+                for (int t = 0; t < p.n_err; ++t) {
+                    const float *kk = p.err_k[t];
+                    const double w = p.err_c[t];
+                    if (kk) {
+                        e0 += w * (double)kk[i];
+                        e1 += w * (double)kk[n + i];
+                        e2 += w * (double)kk[2 * n + i];
+                    } else {
+                        e0 += w * (double)kx_;
+                        e1 += w * (double)ky_;
+                        e2 += w * (double)kz_;
+                    }
+                }
+                e0 *= p.err_dt;
+                e1 *= p.err_dt;
+                e2 *= p.err_dt;
+                mx2[3] = fmaxf(mx2[3], (float)(e0 * e0 + e1 * e1 + e2 * e2));
+            }
+            if (p.k_out) {
+                p.k_out[i] = kx_;
+                p.k_out[n + i] = ky_;
+                p.k_out[2 * n + i] = kz_;
+            }
+            if (p.h_eff_out) {
+                p.h_eff_out[i] = hx;
+                p.h_eff_out[n + i] = hy;
+                p.h_eff_out[2 * n + i] = hz;
+            }
+            if (p.h_ex_out) {
+                p.h_ex_out[i] = ex;
+                p.h_ex_out[n + i] = ey;
+                p.h_ex_out[2 * n + i] = ez;
+            }
+            if (p.h_d_out) {
+                p.h_d_out[i] = dx_;
+                p.h_d_out[n + i] = dy_;
+                p.h_d_out[2 * n + i] = dz_;
+            }
+        }
+        // ---- (4) next stage input ----
+        float nxv = 0.f, nyv = 0.f, nzv = 0.f;
+        if (p.m0) {
+            float sx = 0.f, sy = 0.f, sz = 0.f;
+            for (int t = 0; t < p.n_comb; ++t) {
+                const float *kk = p.comb_k[t];
+                const float w = p.comb_c[t];
+                if (kk) {
+                    sx += w * kk[i];
+                    sy += w * kk[n + i];
+                    sz += w * kk[2 * n + i];
+                } else {
+                    sx += w * kx_;
+                    sy += w * ky_;
+                    sz += w * kz_;
+                }
+            }
+            const float vx = p.m0[i] + p.dt * sx;
+            const float vy = p.m0[n + i] + p.dt * sy;
+            const float vz = p.m0[2 * n + i] + p.dt * sz;
+            const float nn = sqrtf(vx * vx + vy * vy + vz * vz);
+            const float inv = nn > 0.f ? 1.0f / nn : 0.f;
+            nxv = vx * inv;
+            nyv = vy * inv;
+            nzv = vz * inv;
+            p.m_next[i] = nxv;
+            p.m_next[n + i] = nyv;
+            p.m_next[2 * n + i] = nzv;
+        } else if (p.m_fwd) {
+            nxv = p.m_fwd[i];
+            nyv = p.m_fwd[n + i];
+            nzv = p.m_fwd[2 * n + i];
+        }
+        if (p.x_out) {
+            float *pk = reinterpret_cast<float *>(pack);
+            // real sample x of line L lives at float index 2*(L*lsx + sk(x/2)) + (x&1)
+            const int base = 2 * ((rr * 3) * lsx + sk(x >> 1)) + (x & 1);
+            pk[base] = nxv;
+            pk[base + 2 * lsx] = nyv;
+            pk[base + 4 * lsx] = nzv;
+        }
+    }
+
+    // ---- (3) block statistics ----
+    if (p.partials) {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+            float h = sum_hi[s], l = sum_lo[s];
+            warp_ff_sum(h, l);
+            if (lane == 0) red[wid * kNumStats + s] = make_float2(h, l);
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const float v = warp_maxf(mx2[s]);
+            if (lane == 0) red[wid * kNumStats + 5 + s] = make_float2(v, 0.f);
+        }
+        __syncthreads();
+        if (threadIdx.x < kNumStats) {
+            const int s = threadIdx.x;
+            float h = 0.f, l = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                const float2 v = red[w * kNumStats + s];
+                if (s < 5) {
+                    ff_add(h, l, v.x);
+                    l += v.y;
+                } else {
+                    h = fmaxf(h, v.x);
+                }
+            }
+            p.partials[(size_t)s * gridDim.x + blockIdx.x] = make_float2(h, l);
+        }
+    }
+
+    // ---- (5) forward x-transform of the next stage input ----
+    if (p.x_out) {
+        // zero the padded half x in [nx, px) of every packed line
+        float *pk = reinterpret_cast<float *>(pack);
+        const int padw = 2 * half - nx;
+        for (int idx = threadIdx.x; idx < rows * 3 * padw; idx += blockDim.x) {
+            const int line = g.fd_padw.div(idx);
+            const int x = nx + (idx - line * padw);
+            pk[2 * (line * lsx + sk(x >> 1)) + (x & 1)] = 0.f;
+        }
+        __syncthreads();
+        float2 *other = (pack == fa) ? fb : fa;
+        float2 *Z = fft_lines(pack, other, rows * 3, lsx, p.xplan, false);
+        for (int idx = threadIdx.x; idx < rows * 3 * nkx; idx += blockDim.x) {
+            const int line = g.fd_nkx.div(idx);
+            const int k = idx - line * nkx;
+            const int rr = line / 3;
+            const int c = line - rr * 3;
+            const float2 *zl = Z + line * lsx;
+            const float2 a = zl[sk(k == half ? 0 : k)];
+            const float2 b = cconj(zl[sk(k == 0 ? 0 : half - k)]);
+            const float2 E = cscale(cadd(a, b), 0.5f);
+            const float2 O = div2i(csub(a, b));
+            p.x_out[((size_t)c * nrows + row0 + rr) * nkx + k] = cadd(E, cmul(__ldg(p.xpost + k), O));
+        }
+    }
+}
+
+}  // namespace
+
+// ---- host launchers ----
+
+size_t row_pass_smem(const RowPass &p) {
+    const bool use_fft = (p.x_in != nullptr) || (p.x_out != nullptr);
+    size_t b = 0;
+    if (use_fft) b += 2 * sizeof(float2) * (size_t)p.rows * 3 * skewed_len(p.g.half);
+    b += sizeof(double) * kWarps * kNumStats;
+    return b;
+}
+
+int row_pass_blocks(const RowPass &p) {
+    const int nrows = p.g.ny * p.g.nz;
+    return (nrows + p.rows - 1) / p.rows;
+}
+
+static cudaError_t ensure_smem(const void *fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t launch_row_pass(const RowPass &p, cudaStream_t s) {
+    const size_t sm = row_pass_smem(p);
+    cudaError_t e = ensure_smem((const void *)row_pass_kernel, sm);
+    if (e != cudaSuccess) return e;
+    row_pass_kernel<<<row_pass_blocks(p), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace fm
