@@ -283,8 +283,10 @@ def main():
 
     # ---- e2e through the C ABI with host buffers ----
     if args.profile:
+        tun = be.tuning()
         be.close()
-        print(json.dumps({"profile_ms_per_step": ms_per_step, "gpu_launches": launches}), flush=True)
+        print(json.dumps({"workload": args.workload, "profile_ms_per_step": ms_per_step, "gpu_launches": launches,
+                          "tuning": tun}), flush=True)
         return
     m_host = np.ascontiguousarray(kw["m0"], dtype=np.float64)
     if dist:
@@ -312,7 +314,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "grid": [w["nx"], w["ny"], w["nz"]], "integrator": w["integrator"],
-                   "dt": dt, "padded": list(be.fft_shape()), "parallelism": "replicas" if world > 1 else "single",
+                   "dt": dt, "padded": list(be.fft_shape()), "tuning": be.tuning(), "parallelism": "replicas" if world > 1 else "single",
                    "l2_flush": "none needed: working set > 129 MB L2"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": None,

@@ -224,6 +224,7 @@ SIGNATURES = [
     ("fullmag_fdm_backend_step_many", _i, [_vp, _d, _u64, _pss]),
     ("fullmag_fdm_backend_device_magnetization", _i, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     ("fullmag_fdm_backend_stream", _i, [_vp, C.POINTER(_vp)]),
+    ("fullmag_fdm_backend_tuning", _i, [_vp, C.POINTER(_u32)]),
     ("fullmag_fdm_backend_launch_count", _i, [_vp, C.POINTER(_u64)]),
     ("fullmag_fdm_backend_fft_shape", _i, [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
 ]

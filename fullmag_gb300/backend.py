@@ -242,6 +242,11 @@ class FdmBackend:
                     "fft_shape")
         return a.value, b.value, c.value
 
+    def tuning(self) -> dict:
+        a = (C.c_uint32 * 5)()
+        self._check(self.lib.fullmag_fdm_backend_tuning(self.handle, a), "tuning")
+        return {"rows_per_cta": a[0], "tx_y_forward": a[1], "tx_z": a[2], "tx_y_inverse": a[3], "tx_thin": a[4]}
+
     def launch_count(self) -> int:
         c = C.c_uint64()
         self._check(self.lib.fullmag_fdm_backend_launch_count(self.handle, C.byref(c)), "launch_count")

@@ -37,10 +37,18 @@ __global__ void __launch_bounds__(kThreads) y_forward_kernel(const ColPass p) {
     float2 *a = reinterpret_cast<float2 *>(smem);
     float2 *b = a + tx * ls;
     const float2 *src = p.in + ((size_t)c * g.nz + z) * g.ny * g.nkx;
-    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
-        const int y = p.fd_tx.div(idx), col = idx - y * tx;
-        a[col * ls + sk(y)] = (y < g.ny && col < ncol) ? src[(size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
-    }
+    batched_copy<8>(
+        g.ny * tx,
+        [&](int idx) {
+            const int y = p.fd_tx.div(idx), col = idx - y * tx;
+            return col < ncol ? src[(size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+        },
+        [&](int idx, float2 v) {
+            const int y = p.fd_tx.div(idx), col = idx - y * tx;
+            a[col * ls + sk(y)] = v;
+        });
+    for (int line = threadIdx.x >> 5; line < tx; line += blockDim.x >> 5)  // zero padding rows
+        for (int y = g.ny + (threadIdx.x & 31); y < g.py; y += 32) a[line * ls + sk(y)] = make_float2(0.f, 0.f);
     __syncthreads();
     float2 *r = fft_lines(a, b, tx, ls, p.plan, false);
     float2 *dst = p.out + ((size_t)c * g.nz + z) * g.py * g.nkx;
@@ -60,10 +68,16 @@ __global__ void __launch_bounds__(kThreads) y_inverse_kernel(const ColPass p) {
     float2 *a = reinterpret_cast<float2 *>(smem);
     float2 *b = a + tx * ls;
     const float2 *src = p.in + ((size_t)c * g.nz + z) * g.py * g.nkx;
-    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
-        const int y = p.fd_tx.div(idx), col = idx - y * tx;
-        a[col * ls + sk(y)] = col < ncol ? src[(size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
-    }
+    batched_copy<8>(
+        g.py * tx,
+        [&](int idx) {
+            const int y = p.fd_tx.div(idx), col = idx - y * tx;
+            return col < ncol ? src[(size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+        },
+        [&](int idx, float2 v) {
+            const int y = p.fd_tx.div(idx), col = idx - y * tx;
+            a[col * ls + sk(y)] = v;
+        });
     __syncthreads();
     float2 *r = fft_lines(a, b, tx, ls, p.plan, true);
     float2 *dst = p.out + ((size_t)c * g.nz + z) * g.ny * g.nkx;
@@ -94,15 +108,23 @@ __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
     float2 *b = a + (size_t)2 * 3 * tx * ls;
     const size_t cstride = (size_t)g.nz * g.py * g.nkx;  // component stride of Y
     const size_t zstride = (size_t)g.py * g.nkx;
-    for (int idx = threadIdx.x; idx < np * 3 * g.pz * tx; idx += blockDim.x) {
-        const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
-        const int r2 = g.fd_pz.div(r1), z = r1 - r2 * g.pz;
-        const int q = r2 / 3, c = r2 - 3 * q;
-        const int ky = q ? kyb : kya;
-        a[((q * 3 + c) * tx + col) * ls + sk(z)] =
-            (z < g.nz && col < ncol) ? p.in[c * cstride + z * zstride + (size_t)ky * g.nkx + kx0 + col]
-                                     : make_float2(0.f, 0.f);
-    }
+    batched_copy<8>(
+        np * 3 * g.nz * tx,
+        [&](int idx) {
+            const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+            const int r2 = g.fd_nz.div(r1), z = r1 - r2 * g.nz;
+            const int q = r2 / 3, c = r2 - 3 * q;
+            const int ky = q ? kyb : kya;
+            return col < ncol ? p.in[c * cstride + z * zstride + (size_t)ky * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+        },
+        [&](int idx, float2 v) {
+            const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+            const int r2 = g.fd_nz.div(r1), z = r1 - r2 * g.nz;
+            a[(r2 * tx + col) * ls + sk(z)] = v;
+        });
+    // zero the padded planes z in [nz, pz): one warp per line
+    for (int line = threadIdx.x >> 5; line < nl; line += blockDim.x >> 5)
+        for (int z = g.nz + (threadIdx.x & 31); z < g.pz; z += 32) a[line * ls + sk(z)] = make_float2(0.f, 0.f);
     __syncthreads();
     float2 *r = fft_lines(a, b, nl, ls, p.plan, false);
     float2 *o = (r == a) ? b : a;
@@ -152,12 +174,20 @@ __global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p
     float2 *a = reinterpret_cast<float2 *>(smem);
     float2 *b = a + nl * ls;
     const size_t cstride = (size_t)g.ny * g.nkx;
-    for (int idx = threadIdx.x; idx < 3 * g.py * tx; idx += blockDim.x) {
-        const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
-        const int c = g.fd_py.div(r1), y = r1 - c * g.py;
-        a[(c * tx + col) * ls + sk(y)] =
-            (y < g.ny && col < ncol) ? p.in[c * cstride + (size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
-    }
+    batched_copy<8>(
+        3 * g.ny * tx,
+        [&](int idx) {
+            const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+            const int c = g.fd_ny.div(r1), y = r1 - c * g.ny;
+            return col < ncol ? p.in[c * cstride + (size_t)y * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+        },
+        [&](int idx, float2 v) {
+            const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+            const int c = g.fd_ny.div(r1), y = r1 - c * g.ny;
+            a[(c * tx + col) * ls + sk(y)] = v;
+        });
+    for (int line = threadIdx.x >> 5; line < nl; line += blockDim.x >> 5)  // zero padding rows
+        for (int y = g.ny + (threadIdx.x & 31); y < g.py; y += 32) a[line * ls + sk(y)] = make_float2(0.f, 0.f);
     __syncthreads();
     float2 *r = fft_lines(a, b, nl, ls, p.plan, false);
     float2 *o = (r == a) ? b : a;

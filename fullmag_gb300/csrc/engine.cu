@@ -16,8 +16,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/fullmag_fdm.h"
@@ -212,40 +216,58 @@ struct Engine {
         return !cuda_fail("row pass", launch_row_pass(p, stream));
     }
 
-    bool run_columns() {
-        if (!demag) return true;
+    // kx tile widths of the column passes (autotuned at create, see autotune())
+    int tx_yf = 1, tx_z = 1, tx_yi = 1, tx_2d = 1;
+    int row_blocks = 1;  // CTAs of the row pass at the current rows-per-CTA
+
+    ColPass col_pass(const FftPlan &plan, int tx, const float2 *in, float2 *out) const {
         ColPass c{};
         c.g = g;
         c.kern = kern;
-        if (g.thin) {
-            c.plan = plan_y;
-            c.tx = col_tile(g, 3, g.py);
-            c.fd_tx = FastDiv((uint32_t)c.tx);
-            c.in = X;
-            c.out = X;
-            launches += 1;
-            return !cuda_fail("y convolve", launch_y_convolve_2d(c, stream));
-        }
-        c.plan = plan_y;
-        c.tx = col_tile(g, 1, g.py);
-        c.fd_tx = FastDiv((uint32_t)c.tx);
-        c.in = X;
-        c.out = Y;
-        if (cuda_fail("y forward", launch_y_forward(c, stream))) return false;
-        c.plan = plan_z;
-        c.tx = col_tile(g, 6, g.pz);
-        c.fd_tx = FastDiv((uint32_t)c.tx);
-        c.in = Y;
-        c.out = Y;
-        if (cuda_fail("z convolve", launch_z_convolve(c, stream))) return false;
-        c.plan = plan_y;
-        c.tx = col_tile(g, 1, g.py);
-        c.fd_tx = FastDiv((uint32_t)c.tx);
-        c.in = Y;
-        c.out = X;
-        launches += 3;
-        return !cuda_fail("y inverse", launch_y_inverse(c, stream));
+        c.plan = plan;
+        c.tx = tx;
+        c.fd_tx = FastDiv((uint32_t)tx);
+        c.in = in;
+        c.out = out;
+        return c;
     }
+
+    bool run_columns() {
+        if (!demag) return true;
+        if (g.thin) {
+            launches += 1;
+            return !cuda_fail("y convolve", launch_y_convolve_2d(col_pass(plan_y, tx_2d, X, X), stream));
+        }
+        if (cuda_fail("y forward", launch_y_forward(col_pass(plan_y, tx_yf, X, Y), stream))) return false;
+        if (cuda_fail("z convolve", launch_z_convolve(col_pass(plan_z, tx_z, Y, Y), stream))) return false;
+        launches += 3;
+        return !cuda_fail("y inverse", launch_y_inverse(col_pass(plan_y, tx_yi, Y, X), stream));
+    }
+
+    // ---- autotuner: tile widths of the column passes and rows per CTA of the row
+    // pass, timed on the live buffers at create time and cached per grid shape ----
+    float time_ms(const std::function<bool()> &fn) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        bool ok = fn();  // warm-up (also sets shared-memory attributes)
+        cudaEventRecord(e0, stream);
+        for (int r = 0; r < 3 && ok; ++r) ok = fn();
+        cudaEventRecord(e1, stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (!ok) {
+            cudaGetLastError();
+            last_error.clear();
+            return 1e30f;
+        }
+        return ms;
+    }
+
+    bool autotune();
 
     // forward x-transform of a state (no combination)
     bool pass_forward(const float *m) {
@@ -258,7 +280,7 @@ struct Engine {
 
     bool enqueue_stats() {
         launches += 1;
-        if (cuda_fail("finalize", launch_finalize_stats(partials, max_row_blocks, dstats, stream))) return false;
+        if (cuda_fail("finalize", launch_finalize_stats(partials, row_blocks, dstats, stream))) return false;
         return !cuda_fail("stats copy",
                           cudaMemcpyAsync(hstats, dstats, sizeof(double) * kNumStats, cudaMemcpyDeviceToHost, stream));
     }
@@ -815,7 +837,11 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     nk = integrator == FULLMAG_FDM_INTEGRATOR_DP45 ? 7 : (integrator == FULLMAG_FDM_INTEGRATOR_RK4 ? 3 : 1);
     const char *rr_env = std::getenv("FULLMAG_FDM_ROWS_PER_CTA");
     row_rows = rr_env ? std::max(1, std::atoi(rr_env)) : std::max(1, std::min(16, 512 / std::max(1, g.nx)));
-    max_row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
+    max_row_blocks = g.ny * g.nz;  // statistics partials sized for one row per CTA
+    row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
+    tx_yf = tx_yi = col_tile(g, 1, g.py);
+    tx_z = col_tile(g, 6, g.pz);
+    tx_2d = col_tile(g, 3, g.py);
     const size_t vec = sizeof(float) * 3 * (size_t)g.n;
     const size_t xlen = demag ? sizeof(float2) * 3 * (size_t)g.nz * g.ny * g.nkx : 0;
     const size_t ylen = (demag && !thin) ? sizeof(float2) * 3 * (size_t)g.nz * g.py * g.nkx : 0;
@@ -882,6 +908,107 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         }
     }
     if (cuda_fail("setup sync", cudaStreamSynchronize(stream))) return false;
+    const char *no_tune = std::getenv("FULLMAG_FDM_NO_TUNE");
+    if (!(no_tune && *no_tune && *no_tune != '0') && !autotune()) return false;
+    return true;
+}
+
+namespace {
+struct TuneKey {
+    int nx, ny, nz, px, py, pz, thin, masked;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(nx, ny, nz, px, py, pz, thin, masked) < std::tie(o.nx, o.ny, o.nz, o.px, o.py, o.pz, o.thin, o.masked);
+    }
+};
+struct TuneChoice {
+    int tx_yf, tx_z, tx_yi, tx_2d, rows;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneChoice> g_tune_cache;
+}  // namespace
+
+// Picks the kx tile width of each column pass and the rows per CTA of the row pass
+// by timing the candidates (3 launches each, CUDA events on the engine stream) on
+// the live, still-unused buffers.  Results are cached per grid shape in the process,
+// so batched problems of the same shape pay for the search once.
+bool Engine::autotune() {
+    const TuneKey key{g.nx, g.ny, g.nz, g.px, g.py, g.pz, g.thin, has_mask ? 1 : 0};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            tx_yf = it->second.tx_yf;
+            tx_z = it->second.tx_z;
+            tx_yi = it->second.tx_yi;
+            tx_2d = it->second.tx_2d;
+            if (!std::getenv("FULLMAG_FDM_ROWS_PER_CTA")) row_rows = it->second.rows;
+            row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
+            return true;
+        }
+    }
+    auto fits = [&](int lines_per_col, int len, int tx) {
+        return tx <= std::max(1, g.nkx) && (size_t)2 * lines_per_col * tx * skewed_len(len) * sizeof(float2) <= 200u * 1024u;
+    };
+    auto best_tx = [&](int lines_per_col, int len, const std::function<bool(int)> &run, int fallback) {
+        int best = fallback;
+        float bt = 1e30f;
+        for (int tx : {1, 2, 4, 8, 16}) {
+            if (!fits(lines_per_col, len, tx)) continue;
+            const float t = time_ms([&] { return run(tx); });
+            if (t < bt) {
+                bt = t;
+                best = tx;
+            }
+        }
+        return best;
+    };
+    if (demag) {
+        if (g.thin) {
+            tx_2d = best_tx(3, g.py, [&](int tx) { return launch_y_convolve_2d(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; },
+                            tx_2d);
+        } else {
+            tx_yf = best_tx(1, g.py, [&](int tx) { return launch_y_forward(col_pass(plan_y, tx, X, Y), stream) == cudaSuccess; },
+                            tx_yf);
+            tx_z = best_tx(6, g.pz, [&](int tx) { return launch_z_convolve(col_pass(plan_z, tx, Y, Y), stream) == cudaSuccess; },
+                           tx_z);
+            tx_yi = best_tx(1, g.py, [&](int tx) { return launch_y_inverse(col_pass(plan_y, tx, Y, X), stream) == cudaSuccess; },
+                            tx_yi);
+        }
+    }
+    if (!std::getenv("FULLMAG_FDM_ROWS_PER_CTA")) {
+        // a full stage pass: inverse x, fields, statistics, combination, forward x
+        int best = row_rows;
+        float bt = 1e30f;
+        const int nrows = g.ny * g.nz;
+        for (int rows : {1, 2, 4, 8, 16}) {
+            if (rows > nrows || rows * g.nx > 8192) continue;
+            RowPass p = row_base();
+            p.rows = rows;
+            p.x_in = demag ? X : nullptr;
+            p.m_in = S[0];
+            p.k_out = K[0];
+            p.partials = partials;
+            p.m0 = S[1];
+            p.m_next = A[0];
+            p.n_comb = 1;
+            p.comb_k[0] = nullptr;
+            p.comb_c[0] = 0.f;
+            p.x_out = demag ? X : nullptr;
+            if (row_pass_smem(p) > 200u * 1024u) continue;
+            const float t = time_ms([&] { return launch_row_pass(p, stream) == cudaSuccess; });
+            if (t < bt) {
+                bt = t;
+                best = rows;
+            }
+        }
+        row_rows = best;
+    }
+    row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
+    // the timed launches only wrote scratch (X, Y, A[0], K[0], partials); every one of
+    // those is rewritten before it is read again
+    if (cuda_fail("autotune sync", cudaStreamSynchronize(stream))) return false;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = TuneChoice{tx_yf, tx_z, tx_yi, tx_2d, row_rows};
     return true;
 }
 
@@ -1231,6 +1358,17 @@ int fullmag_fdm_backend_stream(fullmag_fdm_backend *handle, void **out_stream) {
     Engine *e = eng(handle);
     if (!e || !out_stream) return FULLMAG_FDM_ERR_INVALID;
     *out_stream = (void *)e->stream;
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out5) {
+    Engine *e = eng(handle);
+    if (!e || !out5) return FULLMAG_FDM_ERR_INVALID;
+    out5[0] = (uint32_t)e->row_rows;
+    out5[1] = (uint32_t)e->tx_yf;
+    out5[2] = (uint32_t)e->tx_z;
+    out5[3] = (uint32_t)e->tx_yi;
+    out5[4] = (uint32_t)e->tx_2d;
     return FULLMAG_FDM_OK;
 }
 

@@ -49,6 +49,26 @@ struct FastDiv {
 
 __host__ __device__ __forceinline__ int sk(int e) { return e + (e >> 4); }
 
+// Gather `total` elements: B independent loads per thread are issued before any of
+// them is consumed, so each thread keeps B requests in flight (the passes are
+// latency-bound otherwise: one outstanding load per thread at 2-4 CTAs per SM).
+template <int B, typename Load, typename Store>
+__device__ __forceinline__ void batched_copy(int total, Load ld, Store st) {
+    for (int base = threadIdx.x; base < total; base += B * blockDim.x) {
+        float2 v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int idx = base + u * (int)blockDim.x;
+            if (idx < total) v[u] = ld(idx);
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int idx = base + u * (int)blockDim.x;
+            if (idx < total) st(idx, v[u]);
+        }
+    }
+}
+
 // Compensated float-float accumulation (Knuth TwoSum): hi + lo carries the sum of
 // every added value with error ~ n * eps^2 instead of n * eps, using FP32 pipes only.
 __device__ __forceinline__ void ff_add(float &hi, float &lo, float v) {

@@ -74,15 +74,26 @@ __global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
     // ---- (1) inverse x-transform of the demag spectrum ----
     float2 *hd = nullptr;
     if (p.x_in) {
+        // stage the spectrum rows in smem (batched loads), then form the half-length input
+        batched_copy<8>(
+            rows * 3 * nkx,
+            [&](int idx) {
+                const int line = g.fd_nkx.div(idx), k = idx - line * nkx;
+                const int rr = line / 3, c = line - 3 * rr;
+                return p.x_in[((size_t)c * nrows + row0 + rr) * nkx + k];
+            },
+            [&](int idx, float2 v) {
+                const int line = g.fd_nkx.div(idx), k = idx - line * nkx;
+                fb[line * lsx + sk(k)] = v;  // lsx >= nkx + 1 holds the nkx values
+            });
+        __syncthreads();
         for (int idx = threadIdx.x; idx < rows * 3 * half; idx += blockDim.x) {
-            const int r1 = g.fd_half.div(idx), k = idx - r1 * half;
-            const int rr = r1 / 3, c = r1 - 3 * rr;
-            const float2 *X = p.x_in + ((size_t)c * nrows + row0 + rr) * nkx;
-            const float2 a = X[k];
-            const float2 b = cconj(X[half - k]);
+            const int line = g.fd_half.div(idx), k = idx - line * half;
+            const float2 a = fb[line * lsx + sk(k)];
+            const float2 b = cconj(fb[line * lsx + sk(half - k)]);
             const float2 E = cadd(a, b);
             const float2 O = cmul(csub(a, b), cconj(__ldg(p.xpost + k)));
-            fa[(rr * 3 + c) * lsx + sk(k)] = cadd(E, mul_i(O));
+            fa[line * lsx + sk(k)] = cadd(E, mul_i(O));
         }
         __syncthreads();
         hd = fft_lines(fa, fb, rows * 3, lsx, p.xplan, true);
