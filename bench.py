@@ -65,6 +65,74 @@ WORKLOADS = {
                               b_mt=(5.0, 0.0, 0.0), dt=5e-14, integrator="rk4", seed=2),
 }
 DEFAULT_WORKLOAD = "volume_256x256x64_rk4"
+SWEEP_WORKLOAD = "sweep_384_films_dp45"
+
+
+def sweep_plans(count=384, seed=1):
+    """Batched-sweep workload: independent films, grid and material drawn from `seed`:
+    nx in {16..256}, ny in {16..128}, nz in {1,2,4}, 4 nm cells, Ms ~ U[4e5,1.2e6] A/m,
+    A ~ U[5e-12,2e-11] J/m, alpha ~ U[0.005,0.1], |B| ~ U[0,100] mT at a uniform in-plane
+    angle, random unit m0; Dormand-Prince with max error 1e-5."""
+    from fullmag_gb300 import _abi
+    rng = np.random.default_rng(seed)
+    plans = []
+    for _ in range(count):
+        nx = int(rng.integers(16, 257))
+        ny = int(rng.integers(16, 129))
+        nz = int(rng.choice([1, 2, 4]))
+        ms = float(rng.uniform(4e5, 1.2e6))
+        a_ex = float(rng.uniform(5e-12, 2e-11))
+        alpha = float(rng.uniform(0.005, 0.1))
+        bmag = float(rng.uniform(0.0, 100.0)) * 1e-3
+        ang = float(rng.uniform(0.0, 2 * np.pi))
+        m0 = rng.standard_normal((nx * ny * nz, 3))
+        m0 /= np.linalg.norm(m0, axis=1, keepdims=True)
+        plans.append(dict(nx=nx, ny=ny, nz=nz, dx=4e-9, dy=4e-9, dz=4e-9, ms=ms, a_ex=a_ex, alpha=alpha,
+                          gamma=2.211e5, m0=m0, h_ext=(bmag * np.cos(ang) / MU0, bmag * np.sin(ang) / MU0, 0.0),
+                          integrator=_abi.INTEGRATOR_DP45, adaptive_max_error=1e-5))
+    return plans
+
+
+def run_sweep(args):
+    """problems/s of the batched sweep vs one problem at a time (a subsample solved
+    sequentially through fullmag_fdm_backend_step), with p50/p99 time-to-solution."""
+    from fullmag_gb300 import FdmBackend, FdmBatch
+    from fullmag_gb300.build import build
+    build()
+    count = args.sweep_count
+    t_end, dt0 = args.sweep_t_end, 1e-13
+    plans = sweep_plans(count)
+    t0 = time.perf_counter()
+    batch = FdmBatch(plans)
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    steps, wall = batch.step_until(t_end, dt0)
+    t_batch = time.perf_counter() - t0
+    batch.close()
+    seq_n = min(args.sweep_sequential, count)
+    seq_times = []
+    for kw in plans[:seq_n]:
+        be = FdmBackend(**kw)
+        ts = time.perf_counter()
+        t, dt = 0.0, dt0
+        while t < t_end * (1 - 1e-12):
+            st = be.step(min(dt, t_end - t))
+            t, dt = st["time_seconds"], st["suggested_next_dt"]
+        seq_times.append(time.perf_counter() - ts)
+        be.close()
+    seq_rate = seq_n / sum(seq_times)
+    out = {"metric": "problems/s (batched sweep, DP45 to %.2g s)" % t_end, "value": count / t_batch,
+           "unit": "problems/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": SWEEP_WORKLOAD, "problems": count, "t_end": t_end, "dt0": dt0,
+                      "cells_total": int(sum(p["nx"] * p["ny"] * p["nz"] for p in plans)),
+                      "accepted_steps_total": int(steps.sum())},
+           "batch_wall_s": t_batch, "setup_s": t_setup,
+           "time_to_solution_s": {"p50": float(np.percentile(wall, 50)), "p99": float(np.percentile(wall, 99))},
+           "sequential": {"problems": seq_n, "problems_per_s": seq_rate,
+                          "time_to_solution_s": {"p50": float(np.percentile(seq_times, 50)),
+                                                 "p99": float(np.percentile(seq_times, 99))}},
+           "speedup_vs_sequential": (count / t_batch) / seq_rate}
+    print(json.dumps(out), flush=True)
 
 
 def smoothed_random_unit(nx, ny, nz, seed, passes=3):
@@ -222,7 +290,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD])
+    ap.add_argument("--sweep-count", type=int, default=384)
+    ap.add_argument("--sweep-t-end", type=float, default=0.5e-9)
+    ap.add_argument("--sweep-sequential", type=int, default=8, help="problems solved one at a time for the baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="timed steps only: no e2e leg, no CPU baseline")
     args = ap.parse_args()
@@ -231,6 +302,10 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == SWEEP_WORKLOAD:
+        if rank == 0:
+            run_sweep(args)
+        return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w, args.workload, rank, world)

@@ -5,6 +5,6 @@ the FDM backend interface of mzrptu/fullmag).  This package builds it in-tree an
 offers a Python mirror of the reference's safe wrapper
 (crates/fullmag-runner/src/native_fdm.rs) for Python callers and tests.
 """
-from .backend import FdmBackend, FdmError, FdmInterrupted, library, load_library  # noqa: F401
+from .backend import FdmBackend, FdmBatch, FdmError, FdmInterrupted, library, load_library, make_plan  # noqa: F401
 
-__all__ = ["FdmBackend", "FdmError", "FdmInterrupted", "library", "load_library"]
+__all__ = ["FdmBackend", "FdmBatch", "FdmError", "FdmInterrupted", "library", "load_library", "make_plan"]

@@ -226,6 +226,13 @@ SIGNATURES = [
     ("fullmag_fdm_backend_stream", _i, [_vp, C.POINTER(_vp)]),
     ("fullmag_fdm_backend_tuning", _i, [_vp, C.POINTER(_u32)]),
     ("fullmag_fdm_backend_launch_count", _i, [_vp, C.POINTER(_u64)]),
+    ("fullmag_fdm_batch_create", _vp, [C.POINTER(PlanDesc), _u32]),
+    ("fullmag_fdm_batch_last_error", C.c_char_p, [_vp]),
+    ("fullmag_fdm_batch_size", _u32, [_vp]),
+    ("fullmag_fdm_batch_step_until", _i, [_vp, _d, _d, C.POINTER(_u64), C.POINTER(_u64)]),
+    ("fullmag_fdm_batch_get_stats", _i, [_vp, _u32, _pss]),
+    ("fullmag_fdm_batch_copy_field_f64", _i, [_vp, _u32, _i, _pd, _u64]),
+    ("fullmag_fdm_batch_destroy", None, [_vp]),
     ("fullmag_fdm_backend_fft_shape", _i, [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
 ]
 

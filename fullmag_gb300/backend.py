@@ -5,7 +5,8 @@ Mirrors ``NativeFdmBackend`` (crates/fullmag-runner/src/native_fdm.rs:50-970): b
 ``last_error`` on a non-NULL handle (native_fdm.rs:477-492), step with interrupt
 support (native_fdm.rs:516-569), copy fields as AoS (n, 3) arrays, upload and
 refresh (native_fdm.rs:829-857) and destroy.  Everything runs through the C ABI of
-``libfullmag_fdm.so``; there is no CPU path.
+``libfullmag_fdm.so``; there is no CPU path.  ``FdmBatch`` wraps the additive batched
+sweep entry points.
 """
 from __future__ import annotations
 
@@ -62,80 +63,85 @@ def _dptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
+              ms: float, a_ex: float, alpha: float, gamma: float = DEFAULT_GAMMA,
+              m0: np.ndarray, integrator: int = _abi.INTEGRATOR_HEUN,
+              enable_exchange: bool = True, enable_demag: bool = True,
+              h_ext: Optional[Sequence[float]] = None, disable_precession: bool = False,
+              ku1: Optional[float] = None, ku2: float = 0.0, u_axis=(0.0, 0.0, 1.0),
+              kc1: Optional[float] = None, kc2: float = 0.0, kc3: float = 0.0,
+              c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0),
+              active_mask: Optional[np.ndarray] = None,
+              spectra: Optional[np.ndarray] = None,
+              adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
+              adaptive_dt_max: float = 0.0, adaptive_headroom: float = 0.0,
+              precision: int = _abi.PRECISION_SINGLE):
+    """Fill a fullmag_fdm_plan_desc the way native_fdm.rs:132-499 does.
+
+    ``spectra`` is an optional (6, 2P) array of interleaved FP64 Newell spectra
+    (xx yy zz xy xz yz) as the reference computes them on the host; when omitted the
+    engine builds the tensor on the GPU.  Returns (plan, keepalive): the arrays in
+    keepalive back the plan's pointers and must outlive the create call."""
+    p = PlanDesc()
+    keep = []
+    p.grid.nx, p.grid.ny, p.grid.nz = nx, ny, nz
+    p.grid.dx, p.grid.dy, p.grid.dz = dx, dy, dz
+    p.material.saturation_magnetisation = ms
+    p.material.exchange_stiffness = a_ex
+    p.material.damping = alpha
+    p.material.gyromagnetic_ratio = gamma
+    p.precision = precision
+    p.integrator = integrator
+    p.disable_precession = int(disable_precession)
+    p.enable_exchange = int(enable_exchange)
+    p.enable_demag = int(enable_demag)
+    p.has_external_field = int(h_ext is not None)
+    p.external_field_am[:] = list(h_ext) if h_ext is not None else [0.0, 0.0, 0.0]
+    p.has_uniaxial_anisotropy = int(ku1 is not None)
+    p.uniaxial_anisotropy_constant = ku1 or 0.0
+    p.uniaxial_anisotropy_k2 = ku2
+    p.anisotropy_axis[:] = list(u_axis)
+    p.has_cubic_anisotropy = int(kc1 is not None)
+    p.cubic_Kc1, p.cubic_Kc2, p.cubic_Kc3 = (kc1 or 0.0), kc2, kc3
+    p.cubic_axis1[:] = list(c1)
+    p.cubic_axis2[:] = list(c2)
+    p.sot_sigma[:] = [0.0, 0.0, 1.0]
+    p.sot_thickness = 1e-9
+    p.oersted_axis[:] = [0.0, 0.0, 1.0]
+    if spectra is not None and enable_demag:
+        sp = np.ascontiguousarray(spectra, dtype=np.float64)
+        keep.append(sp)
+        (p.demag_kernel_xx_spectrum, p.demag_kernel_yy_spectrum, p.demag_kernel_zz_spectrum,
+         p.demag_kernel_xy_spectrum, p.demag_kernel_xz_spectrum,
+         p.demag_kernel_yz_spectrum) = [_dptr(sp[i]) for i in range(6)]
+        p.demag_kernel_spectrum_len = sp.shape[1]
+    if active_mask is not None:
+        mk = np.ascontiguousarray(active_mask, dtype=np.uint8).reshape(-1)
+        keep.append(mk)
+        p.active_mask = mk.ctypes.data_as(C.POINTER(C.c_uint8))
+        p.active_mask_len = mk.size
+    m = np.ascontiguousarray(m0, dtype=np.float64).reshape(-1)
+    keep.append(m)
+    p.initial_magnetization_xyz = _dptr(m)
+    p.initial_magnetization_len = m.size
+    p.adaptive_max_error = adaptive_max_error
+    p.adaptive_dt_min = adaptive_dt_min
+    p.adaptive_dt_max = adaptive_dt_max
+    p.adaptive_headroom = adaptive_headroom
+    return p, keep
+
+
 class FdmBackend:
-    """One FDM problem on the GPU behind the C ABI.
+    """One FDM problem on the GPU behind the C ABI (keyword arguments: ``make_plan``)."""
 
-    Parameters mirror ``FdmPlanIR`` fields the reference wrapper reads.  ``spectra`` is
-    an optional (6, 2P) array of interleaved FP64 Newell spectra (xx yy zz xy xz yz)
-    exactly as the reference computes them on the host; when omitted the engine
-    builds the tensor on the GPU.
-    """
-
-    def __init__(self, *, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
-                 ms: float, a_ex: float, alpha: float, gamma: float = DEFAULT_GAMMA,
-                 m0: np.ndarray, integrator: int = _abi.INTEGRATOR_HEUN,
-                 enable_exchange: bool = True, enable_demag: bool = True,
-                 h_ext: Optional[Sequence[float]] = None, disable_precession: bool = False,
-                 ku1: Optional[float] = None, ku2: float = 0.0, u_axis=(0.0, 0.0, 1.0),
-                 kc1: Optional[float] = None, kc2: float = 0.0, kc3: float = 0.0,
-                 c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0),
-                 active_mask: Optional[np.ndarray] = None,
-                 spectra: Optional[np.ndarray] = None,
-                 adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
-                 adaptive_dt_max: float = 0.0, adaptive_headroom: float = 0.0,
-                 precision: int = _abi.PRECISION_SINGLE):
+    def __init__(self, **plan_kwargs):
         self.lib = load_library()
-        self.n = nx * ny * nz
-        self.shape = (nz, ny, nx)
-        p = PlanDesc()
-        p.grid.nx, p.grid.ny, p.grid.nz = nx, ny, nz
-        p.grid.dx, p.grid.dy, p.grid.dz = dx, dy, dz
-        p.material.saturation_magnetisation = ms
-        p.material.exchange_stiffness = a_ex
-        p.material.damping = alpha
-        p.material.gyromagnetic_ratio = gamma
-        p.precision = precision
-        p.integrator = integrator
-        p.disable_precession = int(disable_precession)
-        p.enable_exchange = int(enable_exchange)
-        p.enable_demag = int(enable_demag)
-        p.has_external_field = int(h_ext is not None)
-        p.external_field_am[:] = list(h_ext) if h_ext is not None else [0.0, 0.0, 0.0]
-        p.has_uniaxial_anisotropy = int(ku1 is not None)
-        p.uniaxial_anisotropy_constant = ku1 or 0.0
-        p.uniaxial_anisotropy_k2 = ku2
-        p.anisotropy_axis[:] = list(u_axis)
-        p.has_cubic_anisotropy = int(kc1 is not None)
-        p.cubic_Kc1, p.cubic_Kc2, p.cubic_Kc3 = (kc1 or 0.0), kc2, kc3
-        p.cubic_axis1[:] = list(c1)
-        p.cubic_axis2[:] = list(c2)
-        p.sot_sigma[:] = [0.0, 0.0, 1.0]
-        p.sot_thickness = 1e-9
-        p.oersted_axis[:] = [0.0, 0.0, 1.0]
-        keep = []
-        if spectra is not None and enable_demag:
-            sp = np.ascontiguousarray(spectra, dtype=np.float64)
-            keep.append(sp)
-            rows = [sp[i] for i in range(6)]
-            (p.demag_kernel_xx_spectrum, p.demag_kernel_yy_spectrum, p.demag_kernel_zz_spectrum,
-             p.demag_kernel_xy_spectrum, p.demag_kernel_xz_spectrum,
-             p.demag_kernel_yz_spectrum) = [_dptr(r) for r in rows]
-            p.demag_kernel_spectrum_len = sp.shape[1]
-        if active_mask is not None:
-            mk = np.ascontiguousarray(active_mask, dtype=np.uint8).reshape(-1)
-            keep.append(mk)
-            p.active_mask = mk.ctypes.data_as(C.POINTER(C.c_uint8))
-            p.active_mask_len = mk.size
-        m = np.ascontiguousarray(m0, dtype=np.float64).reshape(-1)
-        keep.append(m)
-        p.initial_magnetization_xyz = _dptr(m)
-        p.initial_magnetization_len = m.size
-        p.adaptive_max_error = adaptive_max_error
-        p.adaptive_dt_min = adaptive_dt_min
-        p.adaptive_dt_max = adaptive_dt_max
-        p.adaptive_headroom = adaptive_headroom
+        p, keep = make_plan(**plan_kwargs)
+        self.n = p.grid.nx * p.grid.ny * p.grid.nz
+        self.shape = (p.grid.nz, p.grid.ny, p.grid.nx)
         self._poll = None
         self.handle = self.lib.fullmag_fdm_backend_create(C.byref(p))
+        del keep
         if not self.handle:
             raise FdmError(_abi.ERR_INTERNAL, "fullmag_fdm_backend_create returned NULL")
         err = self.lib.fullmag_fdm_backend_last_error(self.handle)
@@ -256,3 +262,59 @@ class FdmBackend:
         s = C.c_void_p()
         self._check(self.lib.fullmag_fdm_backend_stream(self.handle, C.byref(s)), "stream")
         return s.value or 0
+
+
+class FdmBatch:
+    """Many independent problems advanced together (fullmag_fdm_batch_*)."""
+
+    def __init__(self, plans: Sequence[dict]):
+        self.lib = load_library()
+        built = [make_plan(**kw) for kw in plans]
+        arr = (PlanDesc * len(built))(*[b[0] for b in built])
+        self.ns = [b[0].grid.nx * b[0].grid.ny * b[0].grid.nz for b in built]
+        self.handle = self.lib.fullmag_fdm_batch_create(arr, len(built))
+        del built
+        if not self.handle:
+            raise FdmError(_abi.ERR_INTERNAL, "fullmag_fdm_batch_create returned NULL")
+        err = self.lib.fullmag_fdm_batch_last_error(self.handle)
+        if err:
+            self.close()
+            raise FdmError(_abi.ERR_INVALID, err.decode())
+
+    def __len__(self):
+        return len(self.ns)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fullmag_fdm_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step_until(self, t_end: float, dt0: float):
+        n = len(self.ns)
+        steps = (C.c_uint64 * n)()
+        wall = (C.c_uint64 * n)()
+        rc = self.lib.fullmag_fdm_batch_step_until(self.handle, t_end, dt0, steps, wall)
+        if rc != _abi.OK:
+            err = self.lib.fullmag_fdm_batch_last_error(self.handle)
+            raise FdmError(rc, f"batch step_until: {err.decode() if err else 'no detail'}")
+        return np.array(steps[:], dtype=np.int64), np.array(wall[:], dtype=np.float64) * 1e-9
+
+    def stats(self, i: int) -> dict:
+        st = StepStats()
+        rc = self.lib.fullmag_fdm_batch_get_stats(self.handle, i, C.byref(st))
+        if rc != _abi.OK:
+            raise FdmError(rc, "batch get_stats")
+        return st.as_dict()
+
+    def copy_field(self, i: int, observable: int = _abi.OBSERVABLE_M) -> np.ndarray:
+        out = np.empty(3 * self.ns[i], dtype=np.float64)
+        rc = self.lib.fullmag_fdm_batch_copy_field_f64(self.handle, i, observable, _dptr(out), out.size)
+        if rc != _abi.OK:
+            raise FdmError(rc, "batch copy_field")
+        return out.reshape(-1, 3)

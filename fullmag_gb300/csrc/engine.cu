@@ -119,6 +119,8 @@ struct Engine {
         staging = nullptr;
         if (hstats) cudaFreeHost(hstats);
         hstats = nullptr;
+        if (dt_host) cudaFreeHost(dt_host);
+        dt_host = nullptr;
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -341,6 +343,7 @@ struct Engine {
             p.comb_c[t] = (float)coef[t];
         }
         p.dt = (float)dt;
+        p.dt_dev = pass_dt_dev;
         p.x_out = X;
         return run_row(p) && run_columns();
     }
@@ -359,6 +362,7 @@ struct Engine {
             p.err_c[t] = coef[t];
         }
         p.err_dt = dt;
+        p.dt_dev = pass_dt_dev;
         return run_row(p) && (sync ? read_stats() : enqueue_stats());
     }
 
@@ -375,6 +379,8 @@ struct Engine {
         for (int c = 0; c < 2; ++c) {
             if (gexec[c]) cudaGraphExecDestroy(gexec[c]);
             gexec[c] = nullptr;
+            if (dexec[c]) cudaGraphExecDestroy(dexec[c]);
+            dexec[c] = nullptr;
         }
     }
 
@@ -476,9 +482,22 @@ struct Engine {
         cur_stats.suggested_next_dt = 0.0;
     }
 
-    // ---- integrators: return 0 ok, 1 interrupted, -1 error ----
-    int step_dp45(double dt) {
-        static const double a21 = 1.0 / 5.0;
+    // ---- Dormand-Prince 5(4) with first-same-as-last ----
+    // An attempt is seven passes from S[cur] into S[1-cur] ending with the error norm
+    // and statistics at the proposed state.  With no interrupt poll it runs as one
+    // CUDA graph per state parity: dt comes from a device scalar (an H2D node copies
+    // the host value each replay) and the FSAL hand-over is a device copy K6 -> K0,
+    // so the captured pointers never change.
+    cudaGraphExec_t dexec[2] = {nullptr, nullptr};
+    uint64_t dkernels[2] = {0, 0};
+    double *dt_dev = nullptr;   // device scalar (arena)
+    double *dt_host = nullptr;  // pinned
+    const double *pass_dt_dev = nullptr;  // set while capturing: passes read dt from dt_dev
+    bool dp45_pending = false;
+    double dp45_dt = 0.0;
+
+    int enqueue_dp45(double dt, bool poll_between) {
+        static const double a21[1] = {1.0 / 5.0};
         static const double a3[2] = {3.0 / 40.0, 9.0 / 40.0};
         static const double a4[3] = {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0};
         static const double a5[4] = {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0};
@@ -486,55 +505,142 @@ struct Engine {
         static const double b[5] = {35.0 / 384.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0};
         static const double e[6] = {71.0 / 57600.0, -71.0 / 16695.0, 71.0 / 1920.0, -17253.0 / 339200.0, 22.0 / 525.0,
                                     -1.0 / 40.0};
-        if (!ensure_k1()) return -1;
         const int nxt = 1 - cur;
-        for (;;) {
-            if (poll_hit()) return 1;
-            {
-                const int k[1] = {0};
-                const double c[1] = {a21};
-                if (!stage(nullptr, nullptr, 1, k, c, dt, A[0])) return -1;
+        const int k1[1] = {0}, k2[2] = {0, -1}, k3[3] = {0, 1, -1}, k4[4] = {0, 1, 2, -1}, k5[5] = {0, 1, 2, 3, -1};
+        const int kb[5] = {0, 2, 3, 4, -1}, ke[6] = {0, 2, 3, 4, 5, -1};
+        if (!stage(nullptr, nullptr, 1, k1, a21, dt, A[0])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[0], K[1], 2, k2, a3, dt, A[1])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[1], K[2], 3, k3, a4, dt, A[0])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[0], K[3], 4, k4, a5, dt, A[1])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[1], K[4], 5, k5, a6, dt, A[0])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[0], K[5], 5, kb, b, dt, S[nxt])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        return final_eval(S[nxt], K[6], 6, ke, e, dt, false) ? 0 : -1;
+    }
+
+    bool capture_dp45() {
+        if (dexec[cur]) {
+            cudaGraphExecDestroy(dexec[cur]);
+            dexec[cur] = nullptr;
+        }
+        const uint64_t l0 = launches;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+        bool ok = cudaMemcpyAsync(dt_dev, dt_host, sizeof(double), cudaMemcpyHostToDevice, stream) == cudaSuccess;
+        pass_dt_dev = dt_dev;
+        if (ok) ok = enqueue_dp45(0.0, false) == 0;
+        pass_dt_dev = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        launches = l0;
+        if (!ok || e != cudaSuccess || graph == nullptr) {
+            if (graph) cudaGraphDestroy(graph);
+            return false;
+        }
+        size_t nnodes = 0;
+        cudaGraphGetNodes(graph, nullptr, &nnodes);
+        const cudaError_t ie = cudaGraphInstantiate(&dexec[cur], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            dexec[cur] = nullptr;
+            return false;
+        }
+        dkernels[cur] = nnodes > 2 ? nnodes - 2 : 0;  // all but the dt and stats copies
+        return true;
+    }
+
+    // Starts one attempt of size dt without waiting for it (graph path) or runs it
+    // pass by pass with interrupt polls.  Returns 0 queued, 1 interrupted, -1 error.
+    int begin_dp45_attempt(double dt) {
+        if (!ensure_k1()) return -1;
+        if (poll_hit()) return 1;
+        dp45_dt = dt;
+        if (poll == nullptr && use_graphs) {
+            if (!dexec[cur] && !capture_dp45()) {
+                cudaGetLastError();
+                use_graphs = false;
+                last_error.clear();
             }
-            if (poll_hit()) return 1;
-            {
-                const int k[2] = {0, -1};
-                if (!stage(A[0], K[1], 2, k, a3, dt, A[1])) return -1;
-            }
-            if (poll_hit()) return 1;
-            {
-                const int k[3] = {0, 1, -1};
-                if (!stage(A[1], K[2], 3, k, a4, dt, A[0])) return -1;
-            }
-            if (poll_hit()) return 1;
-            {
-                const int k[4] = {0, 1, 2, -1};
-                if (!stage(A[0], K[3], 4, k, a5, dt, A[1])) return -1;
-            }
-            if (poll_hit()) return 1;
-            {
-                const int k[5] = {0, 1, 2, 3, -1};
-                if (!stage(A[1], K[4], 5, k, a6, dt, A[0])) return -1;
-            }
-            if (poll_hit()) return 1;
-            {
-                const int k[5] = {0, 2, 3, 4, -1};
-                if (!stage(A[0], K[5], 5, k, b, dt, S[nxt])) return -1;
-            }
-            if (poll_hit()) return 1;
-            {
-                const int k[6] = {0, 2, 3, 4, 5, -1};
-                if (!final_eval(S[nxt], K[6], 6, k, e, dt)) return -1;
-            }
-            const double err = sqrt(hstats[8]);
-            if (err <= max_error || dt <= dt_min) {
-                double dt_next = dt_max;
-                if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
-                std::swap(K[0], K[6]);  // first-same-as-last
-                commit(dt, hstats);
-                cur_stats.suggested_next_dt = dt_next;
+            if (use_graphs) {
+                *dt_host = dt;
+                if (cuda_fail("graph launch", cudaGraphLaunch(dexec[cur], stream))) return -1;
+                launches += dkernels[cur];
+                dp45_pending = true;
                 return 0;
             }
-            dt = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+        }
+        const int rc = enqueue_dp45(dt, true);
+        if (rc != 0) return rc;
+        dp45_pending = true;
+        return 0;
+    }
+
+    // Waits for the pending attempt and applies the accept/reject rule of the C ABI
+    // (native/backends/fdm/src/llg_dp45_fp32.cu:286-341).  Returns 1 accepted,
+    // 0 rejected (next_dt holds the retry size), -1 error.
+    int finish_dp45_attempt(double &next_dt) {
+        if (!dp45_pending) return -1;
+        dp45_pending = false;
+        if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
+        const double dt = dp45_dt;
+        const double err = sqrt(hstats[8]);
+        if (err <= max_error || dt <= dt_min) {
+            double dt_next = dt_max;
+            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+            // first-same-as-last: k7 at the accepted state is the next step's k1
+            if (cuda_fail("fsal copy", cudaMemcpyAsync(K[0], K[6], sizeof(float) * 3 * (size_t)g.n,
+                                                       cudaMemcpyDeviceToDevice, stream)))
+                return -1;
+            commit(dt, hstats);
+            cur_stats.suggested_next_dt = dt_next;
+            next_dt = dt_next;
+            return 1;
+        }
+        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+        return 0;
+    }
+
+    // Asynchronous fixed-step step for the batch driver (no interrupt polling).
+    bool fixed_pending = false;
+    double fixed_dt = 0.0;
+    int begin_fixed_step(double dt) {
+        if (!ensure_k1()) return -1;
+        if (use_graphs && (!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
+            cudaGetLastError();
+            use_graphs = false;
+            last_error.clear();
+        }
+        if (use_graphs) {
+            if (cuda_fail("graph launch", cudaGraphLaunch(gexec[cur], stream))) return -1;
+            launches += gkernels[cur];
+        } else if (enqueue_fixed_step(dt, false) != 0) {
+            return -1;
+        }
+        fixed_pending = true;
+        fixed_dt = dt;
+        return 0;
+    }
+    int finish_fixed_step() {
+        if (!fixed_pending) return -1;
+        fixed_pending = false;
+        if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
+        commit(fixed_dt, hstats);
+        return 1;
+    }
+
+    int step_dp45(double dt) {
+        for (;;) {
+            const int rc = begin_dp45_attempt(dt);
+            if (rc != 0) return rc;
+            double next = dt;
+            const int ok = finish_dp45_attempt(next);
+            if (ok < 0) return -1;
+            if (ok == 1) return cuda_fail("stream sync", cudaStreamSynchronize(stream)) ? -1 : 0;
+            dt = next;
         }
     }
 
@@ -859,7 +965,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     take(xlen); take(ylen); take(klen);                     // spectra + kernel
     take(has_mask ? (size_t)g.n : 0);                       // mask
     take(sizeof(float2) * kNumStats * (size_t)max_row_blocks);
-    take(sizeof(double) * kNumStats);
+    take(sizeof(double) * (kNumStats + 1));
     take(sizeof(float2) * tw.size());
     arena_bytes = off;
     if (cuda_fail("cudaMalloc(arena)", cudaMalloc((void **)&arena, arena_bytes))) return false;
@@ -885,6 +991,8 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     dstats = (double *)(arena + o[q++]);
     twid = (float2 *)(arena + o[q++]);
     if (cuda_fail("cudaMallocHost(stats)", cudaMallocHost((void **)&hstats, sizeof(double) * kNumStats))) return false;
+    if (cuda_fail("cudaMallocHost(dt)", cudaMallocHost((void **)&dt_host, sizeof(double)))) return false;
+    dt_dev = dstats + kNumStats;  // the stats slot reserves one extra double for dt
 
     if (cuda_fail("cudaMemcpy(twiddles)", cudaMemcpyAsync(twid, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, stream)))
         return false;
@@ -1387,5 +1495,134 @@ int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
     *out_pz = e->g.pz;
     return FULLMAG_FDM_OK;
 }
+
+}  // extern "C"
+
+// =====================================================================
+// Batched sweeps: many independent problems of uneven size
+// =====================================================================
+
+struct FdmBatch {
+    std::vector<Engine *> items;
+    std::vector<double> next_dt;  // per problem: suggested step (DP45) or 0 before the first step
+    std::string last_error;
+    ~FdmBatch() {
+        for (Engine *e : items) delete e;
+    }
+};
+
+extern "C" {
+
+fullmag_fdm_batch *fullmag_fdm_batch_create(const fullmag_fdm_plan_desc *plans, uint32_t count) {
+    if (!plans || count == 0) return nullptr;
+    auto *b = new (std::nothrow) FdmBatch();
+    if (!b) return nullptr;
+    b->items.reserve(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        Engine *e = new (std::nothrow) Engine();
+        if (!e) {
+            b->last_error = "out of host memory";
+            break;
+        }
+        b->items.push_back(e);
+        if (!e->setup(&plans[i]) || !e->upload<double>(plans[i].initial_magnetization_xyz) || !e->eval_state(false)) {
+            b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
+            break;
+        }
+    }
+    b->next_dt.assign(b->items.size(), 0.0);
+    return reinterpret_cast<fullmag_fdm_batch *>(b);
+}
+
+const char *fullmag_fdm_batch_last_error(fullmag_fdm_batch *batch) {
+    if (!batch) return "null batch";
+    auto *b = reinterpret_cast<FdmBatch *>(batch);
+    return b->last_error.empty() ? nullptr : b->last_error.c_str();
+}
+
+uint32_t fullmag_fdm_batch_size(fullmag_fdm_batch *batch) {
+    return batch ? (uint32_t)reinterpret_cast<FdmBatch *>(batch)->items.size() : 0u;
+}
+
+int fullmag_fdm_batch_step_until(fullmag_fdm_batch *batch, double t_end, double dt0, uint64_t *out_steps,
+                                 uint64_t *out_wall_ns) {
+    auto *b = reinterpret_cast<FdmBatch *>(batch);
+    if (!b || !b->last_error.empty()) return FULLMAG_FDM_ERR_INVALID;
+    if (!(dt0 > 0.0) || !std::isfinite(t_end)) {
+        b->last_error = "dt0 must be positive and t_end finite";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    const size_t n = b->items.size();
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<uint64_t> steps0(n);
+    std::vector<size_t> active;
+    for (size_t i = 0; i < n; ++i) {
+        steps0[i] = b->items[i]->step_count;
+        if (b->items[i]->time < t_end * (1.0 - 1e-12)) active.push_back(i);
+        else if (out_wall_ns) out_wall_ns[i] = 0;
+        if (b->next_dt[i] <= 0.0) b->next_dt[i] = dt0;
+    }
+    std::vector<size_t> still;
+    while (!active.empty()) {
+        // issue one attempt for every unfinished problem, then collect
+        for (size_t i : active) {
+            Engine *e = b->items[i];
+            const bool adaptive = e->integrator == FULLMAG_FDM_INTEGRATOR_DP45;
+            const double want = adaptive ? b->next_dt[i] : dt0;
+            const double d = std::min(want, t_end - e->time);
+            const int rc = adaptive ? e->begin_dp45_attempt(d) : e->begin_fixed_step(d);
+            if (rc != 0) {
+                b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
+                return FULLMAG_FDM_ERR_CUDA;
+            }
+        }
+        still.clear();
+        for (size_t i : active) {
+            Engine *e = b->items[i];
+            const bool adaptive = e->integrator == FULLMAG_FDM_INTEGRATOR_DP45;
+            double nd = b->next_dt[i];
+            const int rc = adaptive ? e->finish_dp45_attempt(nd) : e->finish_fixed_step();
+            if (rc < 0) {
+                b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
+                return FULLMAG_FDM_ERR_CUDA;
+            }
+            if (adaptive) b->next_dt[i] = nd;
+            if (e->time >= t_end * (1.0 - 1e-12)) {
+                if (out_wall_ns)
+                    out_wall_ns[i] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                         std::chrono::steady_clock::now() - t0)
+                                         .count();
+            } else {
+                still.push_back(i);
+            }
+        }
+        active.swap(still);
+    }
+    for (size_t i = 0; i < n; ++i) {
+        Engine *e = b->items[i];
+        if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
+            b->last_error = "problem " + std::to_string(i) + ": stream sync failed";
+            return FULLMAG_FDM_ERR_CUDA;
+        }
+        if (out_steps) out_steps[i] = e->step_count - steps0[i];
+    }
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_batch_get_stats(fullmag_fdm_batch *batch, uint32_t index, fullmag_fdm_step_stats *out_stats) {
+    auto *b = reinterpret_cast<FdmBatch *>(batch);
+    if (!b || !out_stats || index >= b->items.size()) return FULLMAG_FDM_ERR_INVALID;
+    return fullmag_fdm_backend_snapshot_stats(reinterpret_cast<fullmag_fdm_backend *>(b->items[index]), out_stats);
+}
+
+int fullmag_fdm_batch_copy_field_f64(fullmag_fdm_batch *batch, uint32_t index, fullmag_fdm_observable observable,
+                                     double *out_xyz, uint64_t out_len) {
+    auto *b = reinterpret_cast<FdmBatch *>(batch);
+    if (!b || index >= b->items.size()) return FULLMAG_FDM_ERR_INVALID;
+    return fullmag_fdm_backend_copy_field_f64(reinterpret_cast<fullmag_fdm_backend *>(b->items[index]), observable,
+                                              out_xyz, out_len);
+}
+
+void fullmag_fdm_batch_destroy(fullmag_fdm_batch *batch) { delete reinterpret_cast<FdmBatch *>(batch); }
 
 }  // extern "C"

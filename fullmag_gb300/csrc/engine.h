@@ -90,6 +90,7 @@ struct RowPass {
     const float *comb_k[kMaxTerms];  // NULL entry = current k
     float comb_c[kMaxTerms];
     float dt;
+    const double *dt_dev;    // non-NULL: dt (and err_dt) read from device memory (graph replays)
     // (5)
     float2 *x_out;           // NULL: no forward transform
     const float *m_fwd;      // forward-transform source when m0 == NULL

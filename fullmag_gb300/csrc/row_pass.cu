@@ -106,6 +106,9 @@ __global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
     float sum_hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sum_lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     float mx2[4] = {0.f, 0.f, 0.f, 0.f};
     const Material &M = p.mat;
+    const double dt_d = p.dt_dev ? *p.dt_dev : (double)p.dt;  // step size of this pass
+    const float dt_f = (float)dt_d;
+    const double err_dt = p.dt_dev ? dt_d : p.err_dt;
     for (int idx = threadIdx.x; idx < rows * nx; idx += blockDim.x) {
         const int rr = g.fd_nx.div(idx);
         const int x = idx - rr * nx;
@@ -243,9 +246,9 @@ __global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
                         e2 += w * (double)kz_;
                     }
                 }
-                e0 *= p.err_dt;
-                e1 *= p.err_dt;
-                e2 *= p.err_dt;
+                e0 *= err_dt;
+                e1 *= err_dt;
+                e2 *= err_dt;
                 mx2[3] = fmaxf(mx2[3], (float)(e0 * e0 + e1 * e1 + e2 * e2));
             }
             if (p.k_out) {
@@ -286,9 +289,9 @@ __global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
                     sz += w * kz_;
                 }
             }
-            const float vx = p.m0[i] + p.dt * sx;
-            const float vy = p.m0[n + i] + p.dt * sy;
-            const float vz = p.m0[2 * n + i] + p.dt * sz;
+            const float vx = p.m0[i] + dt_f * sx;
+            const float vy = p.m0[n + i] + dt_f * sy;
+            const float vz = p.m0[2 * n + i] + dt_f * sz;
             const float nn = sqrtf(vx * vx + vy * vy + vz * vz);
             const float inv = nn > 0.f ? 1.0f / nn : 0.f;
             nxv = vx * inv;

@@ -376,6 +376,30 @@ int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_
 int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
                                   uint32_t *out_py, uint32_t *out_pz);
 
+/* ---- Batched sweeps (additive; no counterpart in the reference interface) ----
+ * Many independent problems of uneven grid size advanced together: every problem
+ * owns its device state and CUDA stream, each step is a replayed CUDA graph, and one
+ * attempt is issued for every unfinished problem before any of them is waited on,
+ * so small problems fill the GPU concurrently instead of one after another. */
+typedef struct fullmag_fdm_batch fullmag_fdm_batch;
+
+/* One problem per plan; plans follow fullmag_fdm_backend_create.  Check
+ * fullmag_fdm_batch_last_error on a non-NULL result. */
+fullmag_fdm_batch *fullmag_fdm_batch_create(const fullmag_fdm_plan_desc *plans, uint32_t count);
+const char *fullmag_fdm_batch_last_error(fullmag_fdm_batch *batch);
+uint32_t fullmag_fdm_batch_size(fullmag_fdm_batch *batch);
+
+/* Advances every problem to simulated time t_end.  DP45 problems start from dt0 and
+ * carry their suggested step; fixed-step problems use dt0.  out_steps (optional,
+ * size entries) receives the accepted steps per problem, out_wall_ns (optional) the
+ * wall time from the call's start at which each problem reached t_end. */
+int fullmag_fdm_batch_step_until(fullmag_fdm_batch *batch, double t_end, double dt0, uint64_t *out_steps,
+                                 uint64_t *out_wall_ns);
+int fullmag_fdm_batch_get_stats(fullmag_fdm_batch *batch, uint32_t index, fullmag_fdm_step_stats *out_stats);
+int fullmag_fdm_batch_copy_field_f64(fullmag_fdm_batch *batch, uint32_t index, fullmag_fdm_observable observable,
+                                     double *out_xyz, uint64_t out_len);
+void fullmag_fdm_batch_destroy(fullmag_fdm_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif
