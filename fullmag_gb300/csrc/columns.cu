@@ -163,12 +163,95 @@ __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
     }
 }
 
-// Thin film: forward y-transform of ny physical rows (zero-padded to py), multiply by
-// the 2-D kernel, inverse, keep ny rows.  X -> X in place.
-__global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p) {
+// 3-D grids whose (y, z) plane fits in shared memory: forward y-transform of the nz
+// physical planes, in-smem transpose, forward z, multiply, inverse z, transpose back,
+// inverse y -- X -> X in place, one pass instead of three and no Y round trip.
+// Lines: y-lines (c, col, z) at ((c*tx + col)*nz + z), z-lines (c, col, ky) at
+// ((c*tx + col)*py + ky); both layouts share two ping-pong buffers of `half_buf`.
+__device__ __forceinline__ void yz_convolve_body(const ColPass &p, const int tile) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
-    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const FftPlan &plan_z = p.plan2;
+    const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
+    const int lsy = skewed_len(g.py), lsz = skewed_len(g.pz);
+    const int nly = 3 * tx * g.nz, nlz = 3 * tx * g.py;
+    const int half_buf = max(nly * lsy, nlz * lsz);
+    float2 *P = reinterpret_cast<float2 *>(smem);
+    float2 *Q = P + half_buf;
+    const size_t cstride = (size_t)g.nz * g.ny * g.nkx;
+    batched_copy<8>(
+        3 * g.nz * g.ny * tx,
+        [&](int idx) {
+            const int r = p.fd_tx.div(idx), col = idx - r * tx;
+            const int r2 = g.fd_ny.div(r), y = r - r2 * g.ny;
+            const int c = g.fd_nz.div(r2), z = r2 - c * g.nz;
+            return col < ncol ? p.in[c * cstride + ((size_t)z * g.ny + y) * g.nkx + kx0 + col] : make_float2(0.f, 0.f);
+        },
+        [&](int idx, float2 v) {
+            const int r = p.fd_tx.div(idx), col = idx - r * tx;
+            const int r2 = g.fd_ny.div(r), y = r - r2 * g.ny;
+            const int c = g.fd_nz.div(r2), z = r2 - c * g.nz;
+            P[((c * tx + col) * g.nz + z) * lsy + sk(y)] = v;
+        });
+    for (int line = threadIdx.x >> 5; line < nly; line += blockDim.x >> 5)
+        for (int y = g.ny + (threadIdx.x & 31); y < g.py; y += 32) P[line * lsy + sk(y)] = make_float2(0.f, 0.f);
+    __syncthreads();
+    float2 *R = fft_lines(P, Q, nly, lsy, p.plan, false);
+    float2 *O = (R == P) ? Q : P;
+    // transpose to z-lines, zero planes z >= nz
+    for (int idx = threadIdx.x; idx < nlz * g.pz; idx += blockDim.x) {
+        const int lz = g.fd_pz.div(idx), z = idx - lz * g.pz;
+        const int cc = g.fd_py.div(lz), ky = lz - cc * g.py;
+        O[lz * lsz + sk(z)] = z < g.nz ? R[(cc * g.nz + z) * lsy + sk(ky)] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *R2 = fft_lines(O, R, nlz, lsz, plan_z, false);
+    const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
+    for (int idx = threadIdx.x; idx < tx * g.py * g.pz; idx += blockDim.x) {
+        const int r = g.fd_pz.div(idx), kz = idx - r * g.pz;
+        const int col = g.fd_py.div(r), ky = r - col * g.py;
+        const int kx = min(kx0 + col, g.nkx - 1);
+        int kym, kzm;
+        float sy, sz;
+        kernel_mirror(ky, g.py, kym, sy);
+        kernel_mirror(kz, g.pz, kzm, sz);
+        const float *K = p.kern + ((size_t)kzm * g.nky + kym) * g.nkx + kx;
+        const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
+        const float kxy = sy * __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz = sy * sz * __ldg(K + 5 * kc);
+        float2 *lx = R2 + ((0 * tx + col) * g.py + ky) * lsz + sk(kz);
+        float2 *ly = R2 + ((1 * tx + col) * g.py + ky) * lsz + sk(kz);
+        float2 *lz = R2 + ((2 * tx + col) * g.py + ky) * lsz + sk(kz);
+        const float2 mx = *lx, my = *ly, mz = *lz;
+        *lx = make_float2(-(kxx * mx.x + kxy * my.x + kxz * mz.x), -(kxx * mx.y + kxy * my.y + kxz * mz.y));
+        *ly = make_float2(-(kxy * mx.x + kyy * my.x + kyz * mz.x), -(kxy * mx.y + kyy * my.y + kyz * mz.y));
+        *lz = make_float2(-(kxz * mx.x + kyz * my.x + kzz * mz.x), -(kxz * mx.y + kyz * my.y + kzz * mz.y));
+    }
+    __syncthreads();
+    float2 *R3 = fft_lines(R2, (R2 == P) ? Q : P, nlz, lsz, plan_z, true);
+    float2 *O3 = (R3 == P) ? Q : P;
+    // transpose back to y-lines, keeping the physical planes z < nz
+    for (int idx = threadIdx.x; idx < nly * g.py; idx += blockDim.x) {
+        const int ly = g.fd_py.div(idx), ky = idx - ly * g.py;
+        const int cc = g.fd_nz.div(ly), z = ly - cc * g.nz;
+        O3[ly * lsy + sk(ky)] = R3[(cc * g.py + ky) * lsz + sk(z)];
+    }
+    __syncthreads();
+    float2 *R4 = fft_lines(O3, R3, nly, lsy, p.plan, true);
+    for (int idx = threadIdx.x; idx < 3 * g.nz * g.ny * tx; idx += blockDim.x) {
+        const int r = p.fd_tx.div(idx), col = idx - r * tx;
+        const int r2 = g.fd_ny.div(r), y = r - r2 * g.ny;
+        const int c = g.fd_nz.div(r2), z = r2 - c * g.nz;
+        if (col < ncol)
+            p.out[c * cstride + ((size_t)z * g.ny + y) * g.nkx + kx0 + col] = R4[((c * tx + col) * g.nz + z) * lsy + sk(y)];
+    }
+}
+
+// Thin film: forward y-transform of ny physical rows (zero-padded to py), multiply by
+// the 2-D kernel, inverse, keep ny rows.  X -> X in place.
+__device__ __forceinline__ void y_convolve_2d_body(const ColPass &p, const int tile) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
     const int ls = skewed_len(g.py);
     const int nl = 3 * tx;
     float2 *a = reinterpret_cast<float2 *>(smem);
@@ -217,6 +300,24 @@ __global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p
     }
 }
 
+__global__ void __launch_bounds__(kThreads) yz_convolve_kernel(const ColPass p) { yz_convolve_body(p, blockIdx.x); }
+__global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p) { y_convolve_2d_body(p, blockIdx.x); }
+
+// One launch for many problems: work[blockIdx.x] = (problem, kx tile); kind 0 thin
+// film, 1 fused y+z.
+__global__ void __launch_bounds__(kThreads) col_batched_kernel(const ColPass *__restrict__ ps,
+                                                               const int2 *__restrict__ work, int kind) {
+    __shared__ __align__(16) unsigned char desc[sizeof(ColPass)];  // descriptor staged once per CTA
+    const int2 w = work[blockIdx.x];
+    const int *src = reinterpret_cast<const int *>(ps + w.x);
+    for (int i = threadIdx.x; i < (int)(sizeof(ColPass) / sizeof(int)); i += blockDim.x)
+        reinterpret_cast<int *>(desc)[i] = src[i];
+    __syncthreads();
+    const ColPass &p = *reinterpret_cast<const ColPass *>(desc);
+    if (kind == 0) y_convolve_2d_body(p, w.y);
+    else yz_convolve_body(p, w.y);
+}
+
 // Deterministic final reduction of the per-block partials (layout [stat][block] of
 // float-float pairs): 1024 threads stride over the blocks with compensated TwoSum
 // accumulation for the energies and max for the norms, then a fixed-order tree
@@ -224,8 +325,7 @@ __global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p
 // the compensation runs on FP32 pipes; only the final hi + lo is formed in FP64.
 constexpr int kFinThreads = 1024;
 
-__global__ void __launch_bounds__(kFinThreads) finalize_stats_kernel(const float2 *__restrict__ partials, int nblocks,
-                                                                     double *__restrict__ out) {
+__device__ __forceinline__ void finalize_body(const float2 *__restrict__ partials, int nblocks, double *__restrict__ out) {
     __shared__ float2 sh[kFinThreads];
     for (int s = 0; s < kNumStats; ++s) {
         const bool is_sum = s < 5;
@@ -259,6 +359,17 @@ __global__ void __launch_bounds__(kFinThreads) finalize_stats_kernel(const float
         if (threadIdx.x == 0) out[s] = (double)sh[0].x + (double)sh[0].y;
         __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(kFinThreads) finalize_stats_kernel(const float2 *__restrict__ partials, int nblocks,
+                                                                     double *__restrict__ out) {
+    finalize_body(partials, nblocks, out);
+}
+
+// One block per problem; statistics land in out[problem * kNumStats + s].
+__global__ void __launch_bounds__(kFinThreads) finalize_batched_kernel(const FinDesc *__restrict__ fd, double *__restrict__ out) {
+    const FinDesc d = fd[blockIdx.x];
+    finalize_body(d.partials, d.nblocks, out + (size_t)blockIdx.x * kNumStats);
 }
 
 cudaError_t ensure_smem(const void *fn, size_t bytes) {
@@ -299,6 +410,34 @@ cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
     cudaError_t e = ensure_smem((const void *)z_convolve_kernel, sm);
     if (e != cudaSuccess) return e;
     z_convolve_kernel<<<dim3(tiles(p), p.g.nky), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+size_t yz_convolve_smem(const Grid &g, int tx) {
+    const size_t a = (size_t)3 * tx * g.nz * skewed_len(g.py);
+    const size_t b = (size_t)3 * tx * g.py * skewed_len(g.pz);
+    return 2 * sizeof(float2) * (a > b ? a : b);
+}
+
+cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s) {
+    const size_t sm = yz_convolve_smem(p.g, p.tx);
+    cudaError_t e = ensure_smem((const void *)yz_convolve_kernel, sm);
+    if (e != cudaSuccess) return e;
+    yz_convolve_kernel<<<tiles(p), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+size_t y_convolve_2d_smem(const Grid &g, int tx) { return 2 * sizeof(float2) * (size_t)3 * tx * skewed_len(g.py); }
+
+cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, int kind, size_t smem, cudaStream_t s) {
+    cudaError_t e = ensure_smem((const void *)col_batched_kernel, smem);
+    if (e != cudaSuccess) return e;
+    col_batched_kernel<<<nwork, kThreads, smem, s>>>(ps, work, kind);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_batched(const FinDesc *fd, int nproblems, double *out, cudaStream_t s) {
+    finalize_batched_kernel<<<nproblems, kFinThreads, 0, s>>>(fd, out);
     return cudaGetLastError();
 }
 

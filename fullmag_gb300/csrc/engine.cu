@@ -45,6 +45,43 @@ __global__ void aos_to_soa_kernel(const double *__restrict__ in_d, const float *
         }
     }
 }
+// Control block of a batched DP45 attempt (host-pinned, copied to the device by the
+// first node of the attempt graph).
+struct BatchCtl {
+    double dt;        // step size of this attempt
+    int accept_prev;  // 1: the previous attempt was accepted and still has to be committed
+    int pad;
+};
+
+// Commit of an accepted batched attempt, run at the start of the next one:
+// S0 <- S1 (proposal becomes the state) and K0 <- K6 (first-same-as-last).
+__global__ void batch_commit_kernel(const BatchCtl *__restrict__ ctl, float *__restrict__ s0, const float *__restrict__ s1,
+                                    float *__restrict__ k0, const float *__restrict__ k6, long long n3) {
+    if (ctl->accept_prev == 0) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x) {
+        s0[i] = s1[i];
+        k0[i] = k6[i];
+    }
+}
+
+struct CommitDesc {
+    float *s0;
+    const float *s1;
+    float *k0;
+    const float *k6;
+    long long n3;
+};
+
+// Batched commit: blockIdx.y selects the problem.
+__global__ void batch_commit_all_kernel(const CommitDesc *__restrict__ cd, const BatchCtl *__restrict__ ctl) {
+    if (ctl[blockIdx.y].accept_prev == 0) return;
+    const CommitDesc d = cd[blockIdx.y];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.n3; i += (long long)gridDim.x * blockDim.x) {
+        d.s0[i] = d.s1[i];
+        d.k0[i] = d.k6[i];
+    }
+}
+
 __global__ void soa_to_aos_kernel(const float *__restrict__ in, double *__restrict__ out_d, float *__restrict__ out_f,
                                   long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -193,6 +230,14 @@ struct Engine {
             if (smooth_enough(m)) return m;
         }
     }
+    // Padded extent >= n when the engine builds the tensor: the next power of two.
+    // It is at most 2x the 2,3,5,7-smooth extent, and the compile-time radix-16/8/4
+    // path it selects runs several times faster per point than the generic radices.
+    static int pad_extent(int n, bool even) {
+        int p2 = 1;
+        while (p2 < std::max(n, even ? 2 : 1)) p2 <<= 1;
+        return p2;
+    }
 
     bool setup(const fullmag_fdm_plan_desc *plan);
     bool upload_spectra(const fullmag_fdm_plan_desc *plan, bool thin_from_len);
@@ -209,17 +254,29 @@ struct Engine {
         return p;
     }
 
+    // Recording mode (batched execution): passes are appended as descriptors instead
+    // of being launched; column passes record their kind (0 thin film, 1 fused y+z).
+    std::vector<RowPass> *rec_rows = nullptr;
+    std::vector<int> *rec_cols = nullptr;
+
     bool run_row(RowPass &p) {
         if (!demag) {
             p.x_in = nullptr;
             p.x_out = nullptr;
         }
+        if (rec_rows) {
+            rec_rows->push_back(p);
+            return true;
+        }
         launches += 1;
         return !cuda_fail("row pass", launch_row_pass(p, stream));
     }
 
-    // kx tile widths of the column passes (autotuned at create, see autotune())
+    // kx tile widths of the column passes (autotuned at create, see autotune());
+    // tx_z doubles as the tile of the fused y+z pass when the (y, z) plane of a kx
+    // column fits in shared memory (use_yz)
     int tx_yf = 1, tx_z = 1, tx_yi = 1, tx_2d = 1;
+    bool use_yz = false;
     int row_blocks = 1;  // CTAs of the row pass at the current rows-per-CTA
 
     ColPass col_pass(const FftPlan &plan, int tx, const float2 *in, float2 *out) const {
@@ -231,14 +288,27 @@ struct Engine {
         c.fd_tx = FastDiv((uint32_t)tx);
         c.in = in;
         c.out = out;
+        c.plan2 = plan_z;
         return c;
     }
 
     bool run_columns() {
         if (!demag) return true;
+        if (rec_cols) {
+            if (!g.thin && !use_yz) {
+                last_error = "grid too large for the batched passes";
+                return false;
+            }
+            rec_cols->push_back(g.thin ? 0 : 1);
+            return true;
+        }
         if (g.thin) {
             launches += 1;
             return !cuda_fail("y convolve", launch_y_convolve_2d(col_pass(plan_y, tx_2d, X, X), stream));
+        }
+        if (use_yz) {
+            launches += 1;
+            return !cuda_fail("yz convolve", launch_yz_convolve(col_pass(plan_y, tx_z, X, X), stream));
         }
         if (cuda_fail("y forward", launch_y_forward(col_pass(plan_y, tx_yf, X, Y), stream))) return false;
         if (cuda_fail("z convolve", launch_z_convolve(col_pass(plan_z, tx_z, Y, Y), stream))) return false;
@@ -281,6 +351,7 @@ struct Engine {
     }
 
     bool enqueue_stats() {
+        if (rec_rows) return true;  // the batched round finalizes all problems at once
         launches += 1;
         if (cuda_fail("finalize", launch_finalize_stats(partials, row_blocks, dstats, stream))) return false;
         return !cuda_fail("stats copy",
@@ -632,6 +703,74 @@ struct Engine {
         return 1;
     }
 
+    // ---- batched DP45 (fullmag_fdm_batch_*) ----
+    // A batched attempt always reads the committed state S[0] and writes its proposal
+    // to S[1]; an accepted proposal is committed on the device at the start of the
+    // next round (S0 <- S1, K0 <- K6), so the recorded pass descriptors never change
+    // and every round of the batch replays one CUDA graph.
+    bool batch_prepare() {
+        if (cur != 0) {  // bring the committed state to S[0]
+            if (cuda_fail("state copy", cudaMemcpyAsync(S[0], S[1], sizeof(float) * 3 * (size_t)g.n,
+                                                        cudaMemcpyDeviceToDevice, stream)))
+                return false;
+            cur = 0;
+            k1_valid = false;
+        }
+        if (!ensure_k1()) return false;
+        return !cuda_fail("stream sync", cudaStreamSynchronize(stream));
+    }
+
+    // Records the seven row passes and six column passes of one attempt, with dt read
+    // from dt_ptr.  False when a pass cannot run batched (large 3-D grids).
+    bool record_attempt(const double *dt_ptr, std::vector<RowPass> &rows, std::vector<int> &cols) {
+        rows.clear();
+        cols.clear();
+        rec_rows = &rows;
+        rec_cols = &cols;
+        pass_dt_dev = dt_ptr;
+        const int rc = enqueue_dp45(0.0, false);
+        rec_rows = nullptr;
+        rec_cols = nullptr;
+        pass_dt_dev = nullptr;
+        return rc == 0 && rows.size() == 7 && (cols.size() == 6 || (!demag && cols.empty()));
+    }
+
+    // Host side of a finished batched attempt (statistics st, control block ctl);
+    // returns 1 accepted, 0 rejected.
+    int batch_decide(const double *st, BatchCtl *ctl, double &next_dt) {
+        const double dt = ctl->dt;
+        const double err = sqrt(st[8]);
+        if (err <= max_error || dt <= dt_min) {
+            double dt_next = dt_max;
+            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+            memcpy(stat_raw, st, sizeof(stat_raw));
+            step_count += 1;
+            time += dt;
+            stats_valid = true;
+            fields_valid = false;
+            fill_stats(stat_raw, cur_stats);
+            cur_stats.step = step_count;
+            cur_stats.time_seconds = time;
+            cur_stats.dt_seconds = dt;
+            cur_stats.suggested_next_dt = dt_next;
+            ctl->accept_prev = 1;
+            next_dt = dt_next;
+            return 1;
+        }
+        ctl->accept_prev = 0;
+        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+        return 0;
+    }
+
+    // Applies a pending commit outside the round graph.
+    bool batch_flush(BatchCtl *ctl, cudaStream_t s) {
+        if (!ctl->accept_prev) return true;
+        ctl->accept_prev = 0;
+        const size_t b = sizeof(float) * 3 * (size_t)g.n;
+        return !cuda_fail("commit copy", cudaMemcpyAsync(S[0], S[1], b, cudaMemcpyDeviceToDevice, s)) &&
+               !cuda_fail("commit copy", cudaMemcpyAsync(K[0], K[6], b, cudaMemcpyDeviceToDevice, s));
+    }
+
     int step_dp45(double dt) {
         for (;;) {
             const int rc = begin_dp45_attempt(dt);
@@ -864,12 +1003,12 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                 use_gpu_newell = true;
         }
         if (use_gpu_newell) {
-            g.px = next_smooth(2 * g.nx - 1, true);
-            g.py = next_smooth(2 * g.ny - 1, false);
+            g.px = pad_extent(2 * g.nx - 1, true);
+            g.py = pad_extent(2 * g.ny - 1, false);
         }
     }
     g.thin = thin ? 1 : 0;
-    g.pz = thin ? 1 : (use_gpu_newell ? next_smooth(2 * g.nz - 1, false) : 2 * g.nz);
+    g.pz = thin ? 1 : (use_gpu_newell ? pad_extent(2 * g.nz - 1, false) : 2 * g.nz);
     if (g.px < 2) g.px = 2;
     g.half = g.px / 2;
     g.nkx = g.half + 1;
@@ -948,9 +1087,17 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     tx_yf = tx_yi = col_tile(g, 1, g.py);
     tx_z = col_tile(g, 6, g.pz);
     tx_2d = col_tile(g, 3, g.py);
+    {
+        const char *no_yz = std::getenv("FULLMAG_FDM_NO_FUSED_YZ");
+        use_yz = demag && !thin && !(no_yz && *no_yz && *no_yz != '0') && yz_convolve_smem(g, 1) <= 200u * 1024u;
+        if (use_yz) {
+            tx_z = 1;
+            while (tx_z < 8 && yz_convolve_smem(g, 2 * tx_z) <= 200u * 1024u) tx_z *= 2;
+        }
+    }
     const size_t vec = sizeof(float) * 3 * (size_t)g.n;
     const size_t xlen = demag ? sizeof(float2) * 3 * (size_t)g.nz * g.ny * g.nkx : 0;
-    const size_t ylen = (demag && !thin) ? sizeof(float2) * 3 * (size_t)g.nz * g.py * g.nkx : 0;
+    const size_t ylen = (demag && !thin && !use_yz) ? sizeof(float2) * 3 * (size_t)g.nz * g.py * g.nkx : 0;
     const size_t klen = demag ? sizeof(float) * (thin ? 4 : 6) * (size_t)g.nkz * g.nky * g.nkx : 0;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     size_t off = 0;
@@ -1074,6 +1221,18 @@ bool Engine::autotune() {
         if (g.thin) {
             tx_2d = best_tx(3, g.py, [&](int tx) { return launch_y_convolve_2d(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; },
                             tx_2d);
+        } else if (use_yz) {
+            int best = tx_z;
+            float bt = 1e30f;
+            for (int tx : {1, 2, 4, 8}) {
+                if (tx > std::max(1, g.nkx) || yz_convolve_smem(g, tx) > 200u * 1024u) continue;
+                const float t = time_ms([&] { return launch_yz_convolve(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; });
+                if (t < bt) {
+                    bt = t;
+                    best = tx;
+                }
+            }
+            tx_z = best;
         } else {
             tx_yf = best_tx(1, g.py, [&](int tx) { return launch_y_forward(col_pass(plan_y, tx, X, Y), stream) == cudaSuccess; },
                             tx_yf);
@@ -1148,7 +1307,7 @@ bool Engine::upload_spectra(const fullmag_fdm_plan_desc *plan, bool thin) {
 // C ABI
 // =====================================================================
 
-using fm::Engine;
+using namespace fm;
 
 static Engine *eng(fullmag_fdm_backend *h) { return reinterpret_cast<Engine *>(h); }
 
@@ -1502,12 +1661,188 @@ int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
 // Batched sweeps: many independent problems of uneven size
 // =====================================================================
 
+// One round of a batched sweep: the attempt of every member problem, executed as
+// 7 batched row passes + 6 batched column passes (one launch per pass and column
+// kind for all problems, through (problem, block) work tables) + one batched
+// finalize, captured once as a CUDA graph and replayed every round.
+struct BatchRound {
+    std::vector<size_t> members;
+    BatchCtl *h_ctl = nullptr;  // pinned [n]
+    BatchCtl *d_ctl = nullptr;
+    double *h_stats = nullptr;  // pinned [n * kNumStats]
+    double *d_stats = nullptr;
+    void *d_blob = nullptr;     // descriptors and work tables
+    cudaGraphExec_t exec = nullptr;
+
+    void release() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        if (h_ctl) cudaFreeHost(h_ctl);
+        h_ctl = nullptr;
+        if (h_stats) cudaFreeHost(h_stats);
+        h_stats = nullptr;
+        if (d_ctl) cudaFree(d_ctl);
+        d_ctl = nullptr;
+        if (d_stats) cudaFree(d_stats);
+        d_stats = nullptr;
+        if (d_blob) cudaFree(d_blob);
+        d_blob = nullptr;
+    }
+};
+
 struct FdmBatch {
     std::vector<Engine *> items;
     std::vector<double> next_dt;  // per problem: suggested step (DP45) or 0 before the first step
     std::string last_error;
+    cudaStream_t bstream = nullptr;
+    BatchRound round;
     ~FdmBatch() {
+        if (bstream) cudaStreamSynchronize(bstream);
+        round.release();
+        if (bstream) cudaStreamDestroy(bstream);
         for (Engine *e : items) delete e;
+    }
+
+    // Builds (and captures) the round for `act`; false when a member cannot run batched.
+    bool build_round(const std::vector<size_t> &act, std::string &err) {
+        // commits still pending in the old round's control blocks run before it goes away
+        for (size_t k = 0; k < round.members.size(); ++k)
+            if (round.h_ctl && !items[round.members[k]]->batch_flush(&round.h_ctl[k], bstream)) {
+                err = "commit failed";
+                return false;
+            }
+        if (bstream) cudaStreamSynchronize(bstream);
+        round.release();
+        const int n = (int)act.size();
+        round.members = act;
+        if (cudaMallocHost((void **)&round.h_ctl, sizeof(BatchCtl) * n) != cudaSuccess ||
+            cudaMallocHost((void **)&round.h_stats, sizeof(double) * kNumStats * n) != cudaSuccess ||
+            cudaMalloc((void **)&round.d_ctl, sizeof(BatchCtl) * n) != cudaSuccess ||
+            cudaMalloc((void **)&round.d_stats, sizeof(double) * kNumStats * n) != cudaSuccess) {
+            err = "batch round allocation failed";
+            return false;
+        }
+        // Work is bucketed by shared-memory class so one large member does not set the
+        // occupancy of every CTA: row buckets rb, column groups (kind, class).
+        constexpr int NC = 5;
+        auto smem_class = [](size_t b) {
+            return b <= 24u * 1024u ? 0 : b <= 48u * 1024u ? 1 : b <= 96u * 1024u ? 2 : b <= 150u * 1024u ? 3 : 4;
+        };
+        std::vector<RowPass> rows[7];
+        std::vector<ColPass> cols[2 * NC];
+        std::vector<int2> row_work[NC], col_work[2 * NC];
+        std::vector<FinDesc> fin(n);
+        std::vector<CommitDesc> com(n);
+        size_t row_smem[NC] = {0, 0, 0, 0, 0}, col_smem[2 * NC] = {};
+        std::vector<RowPass> rec;
+        std::vector<int> kinds;
+        for (int k = 0; k < n; ++k) {
+            Engine *e = items[act[k]];
+            round.h_ctl[k] = BatchCtl{0.0, 0, 0};
+            if (!e->record_attempt(&round.d_ctl[k].dt, rec, kinds)) {
+                err = "problem " + std::to_string(act[k]) + ": " + (e->last_error.empty() ? "not batchable" : e->last_error);
+                return false;
+            }
+            size_t rs = 0;
+            for (int s = 0; s < 7; ++s) {
+                rows[s].push_back(rec[s]);
+                rs = std::max(rs, row_pass_smem(rec[s]));
+            }
+            const int rb = smem_class(rs);
+            row_smem[rb] = std::max(row_smem[rb], rs);
+            const int nb = row_pass_blocks(rec[0]);
+            for (int b = 0; b < nb; ++b) row_work[rb].push_back(make_int2(k, b));
+            if (e->demag) {
+                const int kind = kinds[0];
+                const int tx = kind == 0 ? e->tx_2d : e->tx_z;
+                const size_t cs = kind == 0 ? y_convolve_2d_smem(e->g, tx) : yz_convolve_smem(e->g, tx);
+                const int cg = kind * NC + smem_class(cs);
+                ColPass c = e->col_pass(e->plan_y, tx, e->X, e->X);
+                const int idx = (int)cols[cg].size();
+                cols[cg].push_back(c);
+                const int ntiles = (e->g.nkx + tx - 1) / tx;
+                for (int t = 0; t < ntiles; ++t) col_work[cg].push_back(make_int2(idx, t));
+                col_smem[cg] = std::max(col_smem[cg], cs);
+            }
+            fin[k] = FinDesc{e->partials, nb, 0};
+            com[k] = CommitDesc{e->S[0], e->S[1], e->K[0], e->K[6], 3 * e->g.n};
+        }
+        // one device blob for every descriptor array
+        size_t off = 0;
+        auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+        size_t o_rows[7], o_cols[2 * NC], o_rw[NC], o_cw[2 * NC], o_fin, o_com;
+        for (int s = 0; s < 7; ++s) { o_rows[s] = off; off += al(sizeof(RowPass) * rows[s].size()); }
+        for (int k = 0; k < 2 * NC; ++k) { o_cols[k] = off; off += al(sizeof(ColPass) * cols[k].size()); }
+        for (int k = 0; k < NC; ++k) { o_rw[k] = off; off += al(sizeof(int2) * row_work[k].size()); }
+        for (int k = 0; k < 2 * NC; ++k) { o_cw[k] = off; off += al(sizeof(int2) * col_work[k].size()); }
+        o_fin = off; off += al(sizeof(FinDesc) * n);
+        o_com = off; off += al(sizeof(CommitDesc) * n);
+        if (cudaMalloc(&round.d_blob, off) != cudaSuccess) {
+            err = "batch descriptor allocation failed";
+            return false;
+        }
+        char *blob = (char *)round.d_blob;
+        std::vector<char> hb(off);
+        for (int s = 0; s < 7; ++s) memcpy(hb.data() + o_rows[s], rows[s].data(), sizeof(RowPass) * rows[s].size());
+        for (int k = 0; k < 2 * NC; ++k) memcpy(hb.data() + o_cols[k], cols[k].data(), sizeof(ColPass) * cols[k].size());
+        for (int k = 0; k < NC; ++k) memcpy(hb.data() + o_rw[k], row_work[k].data(), sizeof(int2) * row_work[k].size());
+        for (int k = 0; k < 2 * NC; ++k) memcpy(hb.data() + o_cw[k], col_work[k].data(), sizeof(int2) * col_work[k].size());
+        memcpy(hb.data() + o_fin, fin.data(), sizeof(FinDesc) * n);
+        memcpy(hb.data() + o_com, com.data(), sizeof(CommitDesc) * n);
+        if (cudaMemcpy(blob, hb.data(), off, cudaMemcpyHostToDevice) != cudaSuccess) {
+            err = "batch descriptor upload failed";
+            return false;
+        }
+        // capture the round
+        long long max_n3 = 0;
+        for (auto &c : com) max_n3 = std::max(max_n3, c.n3);
+        // set the shared-memory limits outside the capture
+        size_t max_row = 0, max_col = 0;
+        for (int k = 0; k < NC; ++k) max_row = std::max(max_row, row_smem[k]);
+        for (int k = 0; k < 2 * NC; ++k) max_col = std::max(max_col, col_smem[k]);
+        launch_row_pass_batched((const RowPass *)(blob + o_rows[0]), (const int2 *)(blob + o_rw[0]), 0, max_row, bstream);
+        launch_col_batched((const ColPass *)(blob + o_cols[0]), (const int2 *)(blob + o_cw[0]), 0, 0, max_col, bstream);
+        cudaGetLastError();
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(bstream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            err = "batch capture failed";
+            return false;
+        }
+        bool ok = cudaMemcpyAsync(round.d_ctl, round.h_ctl, sizeof(BatchCtl) * n, cudaMemcpyHostToDevice, bstream) == cudaSuccess;
+        if (ok) {
+            const unsigned gx = (unsigned)std::min<long long>((max_n3 + 255) / 256, 64);
+            batch_commit_all_kernel<<<dim3(gx, n), 256, 0, bstream>>>((const CommitDesc *)(blob + o_com), round.d_ctl);
+            ok = cudaGetLastError() == cudaSuccess;
+        }
+        for (int s = 0; s < 7 && ok; ++s) {
+            for (int rb = 0; rb < NC && ok; ++rb)
+                if (!row_work[rb].empty())
+                    ok = launch_row_pass_batched((const RowPass *)(blob + o_rows[s]), (const int2 *)(blob + o_rw[rb]),
+                                                 (int)row_work[rb].size(), row_smem[rb], bstream) == cudaSuccess;
+            if (s < 6)
+                for (int cg = 0; cg < 2 * NC && ok; ++cg)
+                    if (!col_work[cg].empty())
+                        ok = launch_col_batched((const ColPass *)(blob + o_cols[cg]), (const int2 *)(blob + o_cw[cg]),
+                                                (int)col_work[cg].size(), cg / NC, col_smem[cg], bstream) == cudaSuccess;
+        }
+        if (ok) ok = launch_finalize_batched((const FinDesc *)(blob + o_fin), n, round.d_stats, bstream) == cudaSuccess;
+        if (ok)
+            ok = cudaMemcpyAsync(round.h_stats, round.d_stats, sizeof(double) * kNumStats * n, cudaMemcpyDeviceToHost,
+                                 bstream) == cudaSuccess;
+        const cudaError_t ce = cudaStreamEndCapture(bstream, &graph);
+        if (!ok || ce != cudaSuccess || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            err = "batch round capture failed";
+            return false;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&round.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            round.exec = nullptr;
+            err = "batch round instantiation failed";
+            return false;
+        }
+        return true;
     }
 };
 
@@ -1544,6 +1879,100 @@ uint32_t fullmag_fdm_batch_size(fullmag_fdm_batch *batch) {
     return batch ? (uint32_t)reinterpret_cast<FdmBatch *>(batch)->items.size() : 0u;
 }
 
+// Batched-kernel path (all problems DP45 and small enough for the fused column
+// passes).  Each round replays one graph for all unfinished problems, waits once,
+// then applies the accept/reject rule per problem on the host.  Problems that reached
+// t_end keep computing discarded proposals until the round is rebuilt without them
+// (when a quarter of its members have finished).  Returns 1 when not batchable.
+static int batch_step_until_batched(FdmBatch *b, double t_end, double dt0, uint64_t *out_steps, uint64_t *out_wall_ns) {
+    const size_t n = b->items.size();
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<uint64_t> steps0(n);
+    std::vector<char> done(n, 0);
+    std::vector<size_t> active;
+    if (!b->bstream && cudaStreamCreateWithFlags(&b->bstream, cudaStreamNonBlocking) != cudaSuccess) {
+        b->last_error = "cudaStreamCreate failed";
+        return FULLMAG_FDM_ERR_CUDA;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        Engine *e = b->items[i];
+        steps0[i] = e->step_count;
+        if (!e->batch_prepare()) {
+            b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
+            return FULLMAG_FDM_ERR_CUDA;
+        }
+        if (b->next_dt[i] <= 0.0) b->next_dt[i] = dt0;
+        if (e->time < t_end * (1.0 - 1e-12)) active.push_back(i);
+        else {
+            done[i] = 1;
+            if (out_wall_ns) out_wall_ns[i] = 0;
+        }
+    }
+    bool built = false;
+    while (!active.empty()) {
+        if (!built || active.size() * 10 < b->round.members.size() * 9) {
+            std::string err;
+            if (!b->build_round(active, err)) {
+                if (!built) return 1;  // not batchable: caller falls back
+                b->last_error = err;
+                return FULLMAG_FDM_ERR_CUDA;
+            }
+            built = true;
+        }
+        const std::vector<size_t> &mem = b->round.members;
+        for (size_t k = 0; k < mem.size(); ++k) {
+            Engine *e = b->items[mem[k]];
+            b->round.h_ctl[k].dt = done[mem[k]] ? e->dt_min : std::min(b->next_dt[mem[k]], t_end - e->time);
+        }
+        if (cudaGraphLaunch(b->round.exec, b->bstream) != cudaSuccess || cudaStreamSynchronize(b->bstream) != cudaSuccess) {
+            b->last_error = "batch round launch failed";
+            return FULLMAG_FDM_ERR_CUDA;
+        }
+        std::vector<size_t> still;
+        for (size_t k = 0; k < mem.size(); ++k) {
+            const size_t i = mem[k];
+            Engine *e = b->items[i];
+            BatchCtl *ctl = &b->round.h_ctl[k];
+            if (done[i]) {  // proposal discarded; any pending commit ran at this round's start
+                ctl->accept_prev = 0;
+                continue;
+            }
+            e->launches += 7 + (e->demag ? 6 : 0) + 1;
+            double nd = b->next_dt[i];
+            e->batch_decide(b->round.h_stats + k * kNumStats, ctl, nd);
+            b->next_dt[i] = nd;
+            if (e->time >= t_end * (1.0 - 1e-12)) {
+                done[i] = 1;
+                if (out_wall_ns)
+                    out_wall_ns[i] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                         std::chrono::steady_clock::now() - t0)
+                                         .count();
+                if (!e->batch_flush(ctl, b->bstream)) {  // commit the final step now
+                    b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
+                    return FULLMAG_FDM_ERR_CUDA;
+                }
+            } else {
+                still.push_back(i);
+            }
+        }
+        active.swap(still);
+    }
+    for (size_t k = 0; k < b->round.members.size(); ++k)
+        if (!b->items[b->round.members[k]]->batch_flush(&b->round.h_ctl[k], b->bstream)) {
+            b->last_error = "commit failed";
+            return FULLMAG_FDM_ERR_CUDA;
+        }
+    if (cudaStreamSynchronize(b->bstream) != cudaSuccess) {
+        b->last_error = "batch stream sync failed";
+        return FULLMAG_FDM_ERR_CUDA;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        b->items[i]->k1_valid = true;
+        if (out_steps) out_steps[i] = b->items[i]->step_count - steps0[i];
+    }
+    return FULLMAG_FDM_OK;
+}
+
 int fullmag_fdm_batch_step_until(fullmag_fdm_batch *batch, double t_end, double dt0, uint64_t *out_steps,
                                  uint64_t *out_wall_ns) {
     auto *b = reinterpret_cast<FdmBatch *>(batch);
@@ -1551,6 +1980,13 @@ int fullmag_fdm_batch_step_until(fullmag_fdm_batch *batch, double t_end, double 
     if (!(dt0 > 0.0) || !std::isfinite(t_end)) {
         b->last_error = "dt0 must be positive and t_end finite";
         return FULLMAG_FDM_ERR_INVALID;
+    }
+    bool all_dp45 = true;
+    for (Engine *e : b->items) all_dp45 = all_dp45 && e->integrator == FULLMAG_FDM_INTEGRATOR_DP45 && e->use_graphs;
+    const char *nog = std::getenv("FULLMAG_FDM_BATCH_NO_GRAPH");
+    if (all_dp45 && !(nog && *nog && *nog != '0')) {
+        const int rc = batch_step_until_batched(b, t_end, dt0, out_steps, out_wall_ns);
+        if (rc != 1) return rc;
     }
     const size_t n = b->items.size();
     const auto t0 = std::chrono::steady_clock::now();

@@ -102,6 +102,7 @@ struct RowPass {
 struct ColPass {
     Grid g;
     FftPlan plan;
+    FftPlan plan2;           // z plan of the fused y+z pass
     int tx;                  // kx columns per CTA
     FastDiv fd_tx;
     const float2 *in;
@@ -117,6 +118,19 @@ cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s);     // X -> Y  (
 cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s);    // Y -> Y  (3-D, z FFT, multiply, inverse)
 cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (3-D)
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
+cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s);  // X -> X (small 3-D, uses plan2 for z)
+size_t yz_convolve_smem(const Grid &g, int tx);
+size_t y_convolve_2d_smem(const Grid &g, int tx);
+
+// Batched launches: one grid covering many problems through a (problem, block) table.
+struct FinDesc {
+    const float2 *partials;
+    int nblocks;
+    int pad;
+};
+cudaError_t launch_row_pass_batched(const RowPass *ps, const int2 *work, int nwork, size_t smem, cudaStream_t s);
+cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, int kind, size_t smem, cudaStream_t s);
+cudaError_t launch_finalize_batched(const FinDesc *fd, int nproblems, double *out, cudaStream_t s);
 cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s);
 int row_pass_blocks(const RowPass &p);
 int col_tile(const Grid &g, int lines_per_col, int len);

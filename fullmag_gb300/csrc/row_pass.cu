@@ -56,13 +56,15 @@ __device__ __forceinline__ float warp_maxf(float v) {
     return v;
 }
 
-__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
+// Body of the row pass for CTA `bid` of `nblk`; shared by the single-problem kernel
+// and the batched kernel that walks a (problem, block) work table.
+__device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, const int nblk) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const int nx = g.nx, half = g.half, nkx = g.nkx;
     const long long n = g.n;
     const int nrows = g.ny * g.nz;
-    const int row0 = blockIdx.x * p.rows;
+    const int row0 = bid * p.rows;
     const int rows = min(p.rows, nrows - row0);
     const bool use_fft = (p.x_in != nullptr) || (p.x_out != nullptr);
     const int lsx = skewed_len(half);  // line stride of the x-transform buffers
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
                     h = fmaxf(h, v.x);
                 }
             }
-            p.partials[(size_t)s * gridDim.x + blockIdx.x] = make_float2(h, l);
+            p.partials[(size_t)s * nblk + bid] = make_float2(h, l);
         }
     }
 
@@ -374,7 +376,33 @@ __global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) {
     }
 }
 
+__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) { row_pass_body(p, blockIdx.x, gridDim.x); }
+
+// One launch for many problems: work[blockIdx.x] = (problem, block within problem).
+__global__ void __launch_bounds__(kThreads) row_pass_batched_kernel(const RowPass *__restrict__ ps,
+                                                                    const int2 *__restrict__ work) {
+    // stage the problem's descriptor in shared memory once per CTA: the body reads its
+    // fields in every loop, and global reads could not be hoisted past the stores
+    __shared__ __align__(16) unsigned char desc[sizeof(RowPass)];
+    const int2 w = work[blockIdx.x];
+    const int *src = reinterpret_cast<const int *>(ps + w.x);
+    for (int i = threadIdx.x; i < (int)(sizeof(RowPass) / sizeof(int)); i += blockDim.x)
+        reinterpret_cast<int *>(desc)[i] = src[i];
+    __syncthreads();
+    const RowPass &p = *reinterpret_cast<const RowPass *>(desc);
+    row_pass_body(p, w.y, (p.g.ny * p.g.nz + p.rows - 1) / p.rows);
+}
+
 }  // namespace
+
+cudaError_t launch_row_pass_batched(const RowPass *ps, const int2 *work, int nwork, size_t smem, cudaStream_t s) {
+    cudaError_t e = smem > 48 * 1024 ? cudaFuncSetAttribute((const void *)row_pass_batched_kernel,
+                                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                     : cudaSuccess;
+    if (e != cudaSuccess) return e;
+    row_pass_batched_kernel<<<nwork, kThreads, smem, s>>>(ps, work);
+    return cudaGetLastError();
+}
 
 // ---- host launchers ----
 
