@@ -226,6 +226,9 @@ SIGNATURES = [
     ("fullmag_fdm_backend_stream", _i, [_vp, C.POINTER(_vp)]),
     ("fullmag_fdm_backend_tuning", _i, [_vp, C.POINTER(_u32)]),
     ("fullmag_fdm_backend_launch_count", _i, [_vp, C.POINTER(_u64)]),
+    ("fullmag_fdm_backend_set_field_map", _i, [_vp, _pd, _u64]),
+    ("fullmag_fdm_adjoint_forward", _i, [_vp, _d, _u64, _u32]),
+    ("fullmag_fdm_adjoint_backward", _i, [_vp, _pd, _u64, _pd, _pd]),
     ("fullmag_fdm_batch_create", _vp, [C.POINTER(PlanDesc), _u32]),
     ("fullmag_fdm_batch_last_error", C.c_char_p, [_vp]),
     ("fullmag_fdm_batch_size", _u32, [_vp]),

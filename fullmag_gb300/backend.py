@@ -236,6 +236,33 @@ class FdmBackend:
     def refresh(self):
         self._check(self.lib.fullmag_fdm_backend_refresh_observables(self.handle), "refresh_observables")
 
+    # -- adjoint (additive entry points) --
+    def set_field_map(self, h: Optional[np.ndarray]):
+        """Per-cell applied field (n, 3) in A/m added to H_eff; None removes it."""
+        if h is None:
+            rc = self.lib.fullmag_fdm_backend_set_field_map(self.handle, None, 0)
+        else:
+            a = np.ascontiguousarray(h, dtype=np.float64).reshape(-1)
+            rc = self.lib.fullmag_fdm_backend_set_field_map(self.handle, _dptr(a), a.size)
+        self._check(rc, "set_field_map")
+
+    def adjoint_forward(self, dt: float, n_steps: int, checkpoint_every: int = 0):
+        """n_steps fixed RK4 steps from the current state, keeping checkpoints for
+        adjoint_backward (checkpoint_every 0: ceil(sqrt(n_steps)))."""
+        self._check(self.lib.fullmag_fdm_adjoint_forward(self.handle, dt, n_steps, checkpoint_every),
+                    "adjoint_forward")
+
+    def adjoint_backward(self, lam: np.ndarray, want_lambda0: bool = True):
+        """Given d loss / d m_final (n, 3), returns (d loss / d field map in per A/m,
+        d loss / d m_initial or None), both (n, 3) float64."""
+        a = np.ascontiguousarray(lam, dtype=np.float64).reshape(-1)
+        grad = np.empty(3 * self.n)
+        lam0 = np.empty(3 * self.n) if want_lambda0 else None
+        rc = self.lib.fullmag_fdm_adjoint_backward(self.handle, _dptr(a), a.size, _dptr(grad),
+                                                   _dptr(lam0) if lam0 is not None else None)
+        self._check(rc, "adjoint_backward")
+        return grad.reshape(self.n, 3), (lam0.reshape(self.n, 3) if lam0 is not None else None)
+
     def device_info(self) -> dict:
         info = _abi.DeviceInfo()
         self._check(self.lib.fullmag_fdm_backend_get_device_info(self.handle, C.byref(info)), "get_device_info")

@@ -116,6 +116,7 @@ struct Engine {
     float *K[7] = {};
     int nk = 0;
     float *h_ex = nullptr, *h_d = nullptr, *h_eff = nullptr;
+    float *hmap = nullptr;  // per-cell applied field map (SoA, A/m), allocated on first use
     float2 *X = nullptr, *Y = nullptr;
     float *kern = nullptr;
     uint8_t *mask = nullptr;
@@ -150,6 +151,9 @@ struct Engine {
     void release() {
         if (stream) cudaStreamSynchronize(stream);
         drop_graphs();
+        adj_free();
+        if (hmap) cudaFree(hmap);
+        hmap = nullptr;
         if (arena) cudaFree(arena);
         arena = nullptr;
         if (staging) cudaFree(staging);
@@ -251,6 +255,7 @@ struct Engine {
         p.xplan = plan_x;
         p.xpost = xpost;
         p.rows = row_rows;
+        p.hmap = hmap;
         return p;
     }
 
@@ -364,7 +369,7 @@ struct Engine {
         const double V = dx * dy * dz;
         st.exchange_energy_joules = exchange ? a_ex * V * d[0] : 0.0;
         st.demag_energy_joules = demag ? -0.5 * kMu0 * ms * V * d[1] : 0.0;
-        st.external_energy_joules = has_ext ? -kMu0 * ms * V * d[2] : 0.0;
+        st.external_energy_joules = (has_ext || hmap) ? -kMu0 * ms * V * d[2] : 0.0;
         st.anisotropy_energy_joules = has_uni ? -V * d[3] : 0.0;
         st.cubic_energy_joules = has_cub ? V * d[4] : 0.0;
         st.dmi_energy_joules = 0.0;
@@ -701,6 +706,228 @@ struct Engine {
         if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
         commit(fixed_dt, hstats);
         return 1;
+    }
+
+    // ---- adjoint: reverse-mode RK4 with checkpointing ----
+    // adjoint_forward integrates n steps from the current state, keeping the state
+    // every C steps (C ~ sqrt(n)).  adjoint_backward walks the segments backwards:
+    // it recomputes a segment from its checkpoint while storing every stage input
+    // y0..y3, effective field H0..H3 and k1..k4, then applies the transposed step
+    // (adjoint.cu) in reverse, accumulating d loss / d field map in float-float.
+    float *adj_ckpt = nullptr;  // [n_ckpt][3n]
+    float *adj_seg = nullptr;   // [C][12][3n]: y0 y1 y2 y3 H0 H1 H2 H3 k1 k2 k3 k4
+    float *adj_work = nullptr;  // [12][3n]: lam_next lam_y0 lk1 lk2 lk3 lk4 lam_h lam_m lin g_hi g_lo spare
+    uint64_t adj_nsteps = 0;
+    uint32_t adj_C = 0;
+    size_t adj_nck = 0;
+    double adj_h = 0.0;
+
+    void adj_free() {
+        if (adj_ckpt) cudaFree(adj_ckpt);
+        if (adj_seg) cudaFree(adj_seg);
+        if (adj_work) cudaFree(adj_work);
+        adj_ckpt = adj_seg = adj_work = nullptr;
+    }
+
+    size_t vec3() const { return 3 * (size_t)g.n; }
+
+    // One RK4 step from y0 into y_next.  out[1..3] receive y1..y3, out[4..7] H0..H3
+    // (NULL: not stored), out[8..11] k1..k4 (k1..k3 required).  X must hold the
+    // convolved transform of y0 on entry; on return it holds that of y_next.
+    bool adj_step(const float *y0, float *const *out, float *y_next, double h) {
+        const double cs[3] = {0.5, 0.5, 1.0};
+        const float *ys[4] = {y0, out[1], out[2], out[3]};
+        for (int s = 0; s < 4; ++s) {
+            RowPass p = row_base();
+            p.x_in = X;
+            p.m_in = ys[s];
+            p.k_out = out[8 + s];
+            p.h_eff_out = out[4 + s];
+            p.m0 = y0;
+            p.dt = (float)h;
+            p.x_out = X;
+            if (s < 3) {
+                p.m_next = out[1 + s];
+                p.n_comb = 1;
+                p.comb_k[0] = nullptr;
+                p.comb_c[0] = (float)cs[s];
+            } else {
+                p.m_next = y_next;
+                p.n_comb = 4;
+                p.comb_k[0] = out[8];
+                p.comb_k[1] = out[9];
+                p.comb_k[2] = out[10];
+                p.comb_k[3] = nullptr;
+                p.comb_c[0] = (float)(1.0 / 6.0);
+                p.comb_c[1] = (float)(1.0 / 3.0);
+                p.comb_c[2] = (float)(1.0 / 3.0);
+                p.comb_c[3] = (float)(1.0 / 6.0);
+            }
+            if (!run_row(p) || !run_columns()) return false;
+        }
+        return true;
+    }
+
+    int adjoint_forward(double h, uint64_t nsteps, uint32_t C) {
+        if (integrator != FULLMAG_FDM_INTEGRATOR_RK4) {
+            last_error = "the adjoint requires the RK4 integrator";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
+        if (nsteps == 0 || !(h > 0.0)) {
+            last_error = "adjoint_forward needs n_steps > 0 and dt > 0";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
+        if (C == 0) C = (uint32_t)std::max<uint64_t>(1, (uint64_t)std::ceil(std::sqrt((double)nsteps)));
+        adj_free();
+        adj_nsteps = nsteps;
+        adj_C = C;
+        adj_h = h;
+        adj_nck = (size_t)((nsteps + C - 1) / C);
+        const size_t v3 = vec3();
+        if (cuda_fail("cudaMalloc(adjoint checkpoints)", cudaMalloc((void **)&adj_ckpt, sizeof(float) * v3 * adj_nck)))
+            return FULLMAG_FDM_ERR_CUDA;
+        // scratch stage buffers: y1 y2 y3 k1 k2 k3 (k4 stays in registers)
+        float *scr = nullptr;
+        if (cuda_fail("cudaMalloc(adjoint scratch)", cudaMalloc((void **)&scr, sizeof(float) * v3 * 6))) return FULLMAG_FDM_ERR_CUDA;
+        float *out[12] = {nullptr, scr, scr + v3, scr + 2 * v3, nullptr, nullptr, nullptr, nullptr,
+                          scr + 3 * v3, scr + 4 * v3, scr + 5 * v3, nullptr};
+        bool ok = pass_forward(S[cur]);
+        for (uint64_t st = 0; st < nsteps && ok; ++st) {
+            if (st % C == 0)
+                ok = !cuda_fail("checkpoint copy", cudaMemcpyAsync(adj_ckpt + (st / C) * v3, S[cur], sizeof(float) * v3,
+                                                                   cudaMemcpyDeviceToDevice, stream));
+            if (ok) ok = adj_step(S[cur], out, S[1 - cur], h);
+            cur = 1 - cur;
+        }
+        if (ok) ok = !cuda_fail("adjoint sync", cudaStreamSynchronize(stream));
+        cudaFree(scr);
+        if (!ok) return FULLMAG_FDM_ERR_CUDA;
+        step_count += nsteps;
+        time += h * (double)nsteps;
+        k1_valid = fields_valid = stats_valid = false;
+        return eval_state(false) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+    }
+
+    // lin <- H_lin(v): exchange stencil + Newell convolution applied to an arbitrary field.
+    bool apply_linear(const float *v, float *lin) {
+        if (!pass_forward(v)) return false;
+        RowPass p = row_base();
+        p.mat.has_ext = 0;
+        p.mat.has_uni = 0;
+        p.mat.has_cub = 0;
+        p.hmap = nullptr;
+        p.x_in = X;
+        p.m_in = v;
+        p.h_eff_out = lin;
+        return run_row(p);
+    }
+
+    int adjoint_backward(const double *lam_T, double *grad_out, double *lam0_out) {
+        if (!adj_ckpt) {
+            last_error = "adjoint_backward needs a preceding adjoint_forward";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
+        if (has_cub) {
+            last_error = "the adjoint does not support cubic anisotropy";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
+        const size_t v3 = vec3();
+        const long long n = g.n;
+        if (!adj_seg && cuda_fail("cudaMalloc(adjoint segment)", cudaMalloc((void **)&adj_seg, sizeof(float) * v3 * 12 * adj_C)))
+            return FULLMAG_FDM_ERR_CUDA;
+        if (!adj_work && cuda_fail("cudaMalloc(adjoint work)", cudaMalloc((void **)&adj_work, sizeof(float) * v3 * 12)))
+            return FULLMAG_FDM_ERR_CUDA;
+        float *W[12];
+        for (int i = 0; i < 12; ++i) W[i] = adj_work + i * v3;
+        float *lam_next = W[0], *lam_y0 = W[1], *lk[5] = {nullptr, W[2], W[3], W[4], W[5]};
+        float *lam_h = W[6], *lam_m = W[7], *lin = W[8], *g_hi = W[9], *g_lo = W[10], *spare = W[11];
+        if (!ensure_staging()) return FULLMAG_FDM_ERR_CUDA;
+        if (cuda_fail("cudaMemcpy(lambda)", cudaMemcpyAsync(staging, lam_T, sizeof(double) * v3, cudaMemcpyHostToDevice, stream)))
+            return FULLMAG_FDM_ERR_CUDA;
+        aos_to_soa_kernel<<<std::min<long long>((n + 255) / 256, 4096), 256, 0, stream>>>((const double *)staging, nullptr,
+                                                                                          lam_next, mask, n);
+        if (cuda_fail("zero", cudaMemsetAsync(g_hi, 0, sizeof(float) * v3 * 2, stream))) return FULLMAG_FDM_ERR_CUDA;
+        const double h = adj_h;
+        const float hf = (float)h;
+        const float cs[4] = {0.f, 0.5f, 0.5f, 1.0f};
+        bool ok = true;
+        for (long long seg = (long long)adj_nck - 1; seg >= 0 && ok; --seg) {
+            const uint64_t s0 = (uint64_t)seg * adj_C;
+            const uint64_t len = std::min<uint64_t>(adj_C, adj_nsteps - s0);
+            auto slot = [&](uint64_t t, int f) { return adj_seg + (t * 12 + f) * v3; };
+            ok = !cuda_fail("segment copy", cudaMemcpyAsync(slot(0, 0), adj_ckpt + seg * v3, sizeof(float) * v3,
+                                                            cudaMemcpyDeviceToDevice, stream)) &&
+                 pass_forward(slot(0, 0));
+            for (uint64_t t = 0; t < len && ok; ++t) {
+                float *out[12];
+                for (int f = 0; f < 12; ++f) out[f] = slot(t, f);
+                ok = adj_step(slot(t, 0), out, t + 1 < len ? slot(t + 1, 0) : spare, h);
+            }
+            for (long long t = (long long)len - 1; t >= 0 && ok; --t) {
+                AdjFinal af{n, lam_next, slot(t, 0), slot(t, 8), slot(t, 9), slot(t, 10), slot(t, 11), hf,
+                            lam_y0, lk[1], lk[2], lk[3], lk[4]};
+                ok = !cuda_fail("adjoint final", launch_adj_final(af, stream));
+                for (int s = 3; s >= 0 && ok; --s) {
+                    AdjLocal al{};
+                    al.n = n;
+                    al.m = slot(t, s);
+                    al.H = slot(t, 4 + s);
+                    al.w = lk[s + 1];
+                    al.lam_h = lam_h;
+                    al.lam_m = lam_m;
+                    al.g_hi = g_hi;
+                    al.g_lo = g_lo;
+                    al.gbar = mat.gbar;
+                    al.alpha = mat.alpha;
+                    al.prec = mat.prec;
+                    al.has_uni = mat.has_uni;
+                    al.ku1c = mat.ku1c;
+                    al.ku2c = mat.ku2c;
+                    for (int c = 0; c < 3; ++c) al.u[c] = mat.u[c];
+                    ok = !cuda_fail("adjoint local", launch_adj_local(al, stream)) && apply_linear(lam_h, lin);
+                    if (!ok) break;
+                    AdjStage as{n, lam_m, lin, slot(t, 0), s >= 1 ? slot(t, 8 + s - 1) : nullptr, cs[s] * hf, lam_y0,
+                                s >= 1 ? lk[s] : nullptr};
+                    ok = !cuda_fail("adjoint stage", launch_adj_stage(as, stream));
+                }
+                std::swap(lam_next, lam_y0);
+            }
+        }
+        if (!ok) return FULLMAG_FDM_ERR_CUDA;
+        // gradient: g_hi + g_lo (per A/m of the map), lambda_0 = lam_next
+        std::vector<float> hi(v3), lo(v3), l0(v3);
+        if (cuda_fail("cudaMemcpy(grad)", cudaMemcpyAsync(hi.data(), g_hi, sizeof(float) * v3, cudaMemcpyDeviceToHost, stream)) ||
+            cuda_fail("cudaMemcpy(grad)", cudaMemcpyAsync(lo.data(), g_lo, sizeof(float) * v3, cudaMemcpyDeviceToHost, stream)) ||
+            cuda_fail("cudaMemcpy(lambda0)",
+                      cudaMemcpyAsync(l0.data(), lam_next, sizeof(float) * v3, cudaMemcpyDeviceToHost, stream)) ||
+            cuda_fail("adjoint sync", cudaStreamSynchronize(stream)))
+            return FULLMAG_FDM_ERR_CUDA;
+        for (long long i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) {
+                if (grad_out) grad_out[3 * i + c] = (double)hi[c * n + i] + (double)lo[c * n + i];
+                if (lam0_out) lam0_out[3 * i + c] = (double)l0[c * n + i];
+            }
+        return FULLMAG_FDM_OK;
+    }
+
+    bool set_field_map(const double *h_xyz) {
+        if (!h_xyz) {
+            if (hmap) cudaFree(hmap);
+            hmap = nullptr;
+            k1_valid = fields_valid = stats_valid = false;
+            return true;
+        }
+        if (!hmap && cuda_fail("cudaMalloc(field map)", cudaMalloc((void **)&hmap, sizeof(float) * vec3()))) return false;
+        if (!ensure_staging()) return false;
+        if (cuda_fail("cudaMemcpy(field map)",
+                      cudaMemcpyAsync(staging, h_xyz, sizeof(double) * vec3(), cudaMemcpyHostToDevice, stream)))
+            return false;
+        aos_to_soa_kernel<<<std::min<long long>((g.n + 255) / 256, 4096), 256, 0, stream>>>((const double *)staging, nullptr,
+                                                                                            hmap, mask, g.n);
+        if (cuda_fail("field map convert", cudaGetLastError())) return false;
+        drop_graphs();  // captured passes hold the previous map pointer
+        k1_valid = fields_valid = stats_valid = false;
+        return !cuda_fail("field map sync", cudaStreamSynchronize(stream));
     }
 
     // ---- batched DP45 (fullmag_fdm_batch_*) ----
@@ -1626,6 +1853,36 @@ int fullmag_fdm_backend_stream(fullmag_fdm_backend *handle, void **out_stream) {
     if (!e || !out_stream) return FULLMAG_FDM_ERR_INVALID;
     *out_stream = (void *)e->stream;
     return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_set_field_map(fullmag_fdm_backend *handle, const double *h_xyz, uint64_t len) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (h_xyz && len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "field map length mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->set_field_map(h_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_adjoint_forward(fullmag_fdm_backend *handle, double dt_seconds, uint64_t n_steps,
+                                uint32_t checkpoint_every) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    e->last_error.clear();
+    return e->adjoint_forward(dt_seconds, n_steps, checkpoint_every);
+}
+
+int fullmag_fdm_adjoint_backward(fullmag_fdm_backend *handle, const double *lambda_xyz, uint64_t len,
+                                 double *grad_field_map_xyz, double *lambda0_xyz) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena || !lambda_xyz) return FULLMAG_FDM_ERR_INVALID;
+    if (len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "lambda length mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    e->last_error.clear();
+    return e->adjoint_backward(lambda_xyz, grad_field_map_xyz, lambda0_xyz);
 }
 
 int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out5) {

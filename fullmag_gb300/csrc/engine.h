@@ -94,6 +94,8 @@ struct RowPass {
     // (5)
     float2 *x_out;           // NULL: no forward transform
     const float *m_fwd;      // forward-transform source when m0 == NULL
+    // per-cell applied field map (SoA, A/m), added to H_eff at active cells; NULL: none
+    const float *hmap;
     // observables
     float *h_ex_out, *h_d_out, *h_eff_out;  // NULL: not written
     int rows;                // rows per CTA
@@ -121,6 +123,33 @@ cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (
 cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s);  // X -> X (small 3-D, uses plan2 for z)
 size_t yz_convolve_smem(const Grid &g, int tx);
 size_t y_convolve_2d_smem(const Grid &g, int tx);
+
+// Adjoint (reverse-mode RK4) element-wise passes (adjoint.cu); all fields SoA.
+struct AdjLocal {
+    long long n;
+    const float *m, *H, *w;     // stage input, its effective field, cotangent of k
+    float *lam_h, *lam_m;       // outputs
+    float *g_hi, *g_lo;         // float-float accumulator of d loss / d field map (NULL: none)
+    float gbar, alpha, prec;
+    int has_uni;
+    float ku1c, ku2c, u[3];
+};
+struct AdjStage {
+    long long n;
+    const float *lam_m, *lin;   // local VJP and H_lin(lambda_H)
+    const float *y0, *k;        // k == NULL: stage 0 (no normalisation to undo)
+    float ch;                   // c * h of y_s = N(y0 + c h k_s)
+    float *lam_y0, *lam_k;      // accumulators
+};
+struct AdjFinal {
+    long long n;
+    const float *lam_next, *y0, *k1, *k2, *k3, *k4;
+    float h;
+    float *lam_y0, *lk1, *lk2, *lk3, *lk4;
+};
+cudaError_t launch_adj_local(const AdjLocal &a, cudaStream_t s);
+cudaError_t launch_adj_stage(const AdjStage &a, cudaStream_t s);
+cudaError_t launch_adj_final(const AdjFinal &a, cudaStream_t s);
 
 // Batched launches: one grid covering many problems through a (problem, block) table.
 struct FinDesc {

@@ -188,6 +188,11 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
                     hy += M.hext[1];
                     hz += M.hext[2];
                 }
+                if (p.hmap) {
+                    hx += p.hmap[i];
+                    hy += p.hmap[n + i];
+                    hz += p.hmap[2 * n + i];
+                }
                 float e_uni = 0.f, e_cub = 0.f;
                 if (M.has_uni) {
                     const float mu = m0x * M.u[0] + m0y * M.u[1] + m0z * M.u[2];
@@ -226,6 +231,7 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
                     ff_add(sum_hi[0], sum_lo[0], e_pair);
                     ff_add(sum_hi[1], sum_lo[1], m0x * dx_ + m0y * dy_ + m0z * dz_);
                     if (M.has_ext) ff_add(sum_hi[2], sum_lo[2], m0x * M.hext[0] + m0y * M.hext[1] + m0z * M.hext[2]);
+                    if (p.hmap) ff_add(sum_hi[2], sum_lo[2], m0x * p.hmap[i] + m0y * p.hmap[n + i] + m0z * p.hmap[2 * n + i]);
                     ff_add(sum_hi[3], sum_lo[3], e_uni);
                     ff_add(sum_hi[4], sum_lo[4], e_cub);
                     mx2[0] = fmaxf(mx2[0], hx * hx + hy * hy + hz * hz);

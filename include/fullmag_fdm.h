@@ -376,6 +376,21 @@ int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_
 int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
                                   uint32_t *out_py, uint32_t *out_pz);
 
+/* ---- Adjoint gradients (additive; no counterpart in the reference interface) ----
+ * A per-cell applied field map (A/m, AoS, 3*cell_count) is added to H_eff at active
+ * cells; NULL removes it.  The adjoint of a fixed-step RK4 run is split in two calls:
+ * adjoint_forward integrates n_steps from the current state keeping a checkpoint every
+ * checkpoint_every steps (0: ceil(sqrt(n_steps))); the caller then reads the final
+ * state, evaluates its loss and passes d loss / d m_final to adjoint_backward, which
+ * returns d loss / d field map (per A/m, AoS) and, optionally, d loss / d m_initial.
+ * The backward pass recomputes each segment from its checkpoint, so device memory is
+ * O(n/C + 12 C) states.  RK4 only; uniaxial anisotropy supported, cubic not. */
+int fullmag_fdm_backend_set_field_map(fullmag_fdm_backend *handle, const double *h_xyz, uint64_t len);
+int fullmag_fdm_adjoint_forward(fullmag_fdm_backend *handle, double dt_seconds, uint64_t n_steps,
+                                uint32_t checkpoint_every);
+int fullmag_fdm_adjoint_backward(fullmag_fdm_backend *handle, const double *lambda_xyz, uint64_t len,
+                                 double *grad_field_map_xyz, double *lambda0_xyz);
+
 /* ---- Batched sweeps (additive; no counterpart in the reference interface) ----
  * Many independent problems of uneven grid size advanced together: every problem
  * owns its device state and CUDA stream, each step is a replayed CUDA graph, and one

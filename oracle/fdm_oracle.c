@@ -418,6 +418,7 @@ struct fo_problem {
     /* integrator buffers (AoS) */
     double *m0, *mst, *heff, *hscr, *k[7], *fsal;
     int fsal_valid;
+    double *hmap; /* optional per-cell applied field (AoS, A/m) */
 };
 
 static inline int active(const fo_problem *pr, long i) { return pr->mask == NULL || pr->mask[i] != 0; }
@@ -438,7 +439,7 @@ void fo_destroy(fo_problem *pr) {
     free(pr->m);
     for (int c = 0; c < 6; ++c) free(pr->kern[c]);
     for (int c = 0; c < 3; ++c) { free(pr->bm[c]); free(pr->bh[c]); }
-    free(pr->m0); free(pr->mst); free(pr->heff); free(pr->hscr); free(pr->fsal);
+    free(pr->m0); free(pr->mst); free(pr->heff); free(pr->hscr); free(pr->fsal); free(pr->hmap);
     for (int s = 0; s < 7; ++s) free(pr->k[s]);
     free(pr);
 }
@@ -494,6 +495,20 @@ int fo_set_m(fo_problem *pr, const double *m_aos) {
 
 int fo_get_m(const fo_problem *pr, double *m_aos) {
     memcpy(m_aos, pr->m, sizeof(double) * 3 * pr->n);
+    return 0;
+}
+
+/* Per-cell applied field added to H_eff at active cells (the field map of the
+ * adjoint entry points of the engine); NULL removes it. */
+int fo_set_field_map(fo_problem *pr, const double *h_aos) {
+    free(pr->hmap);
+    pr->hmap = NULL;
+    if (h_aos) {
+        pr->hmap = dalloc(3 * pr->n);
+        for (long i = 0; i < pr->n; ++i)
+            for (int c = 0; c < 3; ++c) pr->hmap[3 * i + c] = active(pr, i) ? h_aos[3 * i + c] : 0.0;
+    }
+    pr->fsal_valid = 0;
     return 0;
 }
 
@@ -623,6 +638,8 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
         if (active(pr, i)) {
             if (p->has_external_field)
                 for (int c = 0; c < 3; ++c) h[c] += p->h_ext[c];
+            if (pr->hmap)
+                for (int c = 0; c < 3; ++c) h[c] += pr->hmap[3 * i + c];
             anis_field_cell(pr, m + 3 * i, h);
         }
         for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
@@ -687,6 +704,9 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
             ed += -0.5 * FO_MU0 * p->ms * V * (mi[0] * h_d[3 * i] + mi[1] * h_d[3 * i + 1] + mi[2] * h_d[3 * i + 2]);
         if (p->has_external_field)
             eext += -FO_MU0 * p->ms * V * (mi[0] * p->h_ext[0] + mi[1] * p->h_ext[1] + mi[2] * p->h_ext[2]);
+        if (pr->hmap)
+            eext += -FO_MU0 * p->ms * V *
+                    (mi[0] * pr->hmap[3 * i] + mi[1] * pr->hmap[3 * i + 1] + mi[2] * pr->hmap[3 * i + 2]);
         if (p->has_uniaxial) {
             const double mu = mi[0] * pr->u[0] + mi[1] * pr->u[1] + mi[2] * pr->u[2];
             const double s = mu * mu;
@@ -862,6 +882,119 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st) {
     st->dt_used = dt;
     st->suggested_next_dt = suggested;
     st->rejected_attempts = rejected;
+    return 0;
+}
+
+/* ---- Tangent-linear RK4 (checks the engine's reverse-mode gradients) ----
+ * Differentiates the fixed-step RK4 of fo_step (fdm_integrators.rs:155-262) with
+ * respect to the initial state and the field map, in FP64:
+ *   dk   = -gb [s (dm x H + m x dH) + alpha (dm x (m x H) + m x (dm x H + m x dH))]
+ *   dH   = H_lin(dm) + J_anis(m) dm + dh_map      (H_lin: exchange + demag, linear)
+ *   d N(v) = (dv - u (u . dv)) / |v|,  u = N(v). */
+static void tangent_rhs(fo_problem *pr, const double *m, const double *dm, const double *dh, double *k,
+                        double *dk, double *ha, double *hb, double *dha, double *dhb) {
+    const fo_params *p = &pr->p;
+    const long n3 = 3 * pr->n;
+    double *heff = pr->heff, *dheff = pr->hscr;
+    eval_fields(pr, m, ha, hb, heff, k);
+    memset(dha, 0, sizeof(double) * n3);
+    memset(dhb, 0, sizeof(double) * n3);
+    if (p->enable_exchange) exchange_add(pr, dm, dha);
+    if (p->enable_demag) demag_add(pr, dm, dhb);
+    const double gb = p->gamma / (1.0 + p->alpha * p->alpha);
+    const double s = p->disable_precession ? 0.0 : 1.0;
+    const double ms = p->ms > 1e-30 ? p->ms : 1e-30;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        const double *mi = m + 3 * i, *dmi = dm + 3 * i, *H = heff + 3 * i;
+        double dH[3] = {dha[3 * i] + dhb[3 * i], dha[3 * i + 1] + dhb[3 * i + 1], dha[3 * i + 2] + dhb[3 * i + 2]};
+        if (active(pr, i)) {
+            if (dh)
+                for (int c = 0; c < 3; ++c) dH[c] += dh[3 * i + c];
+            if (p->has_uniaxial) {
+                const double mu = mi[0] * pr->u[0] + mi[1] * pr->u[1] + mi[2] * pr->u[2];
+                const double dmu = dmi[0] * pr->u[0] + dmi[1] * pr->u[1] + dmi[2] * pr->u[2];
+                const double cf = (2.0 * p->ku1 + 12.0 * p->ku2 * mu * mu) / (FO_MU0 * ms) * dmu;
+                for (int c = 0; c < 3; ++c) dH[c] += cf * pr->u[c];
+            }
+        }
+        for (int c = 0; c < 3; ++c) dheff[3 * i + c] = dH[c];
+        const double P_[3] = {mi[1] * H[2] - mi[2] * H[1], mi[2] * H[0] - mi[0] * H[2], mi[0] * H[1] - mi[1] * H[0]};
+        const double dP[3] = {dmi[1] * H[2] - dmi[2] * H[1] + mi[1] * dH[2] - mi[2] * dH[1],
+                              dmi[2] * H[0] - dmi[0] * H[2] + mi[2] * dH[0] - mi[0] * dH[2],
+                              dmi[0] * H[1] - dmi[1] * H[0] + mi[0] * dH[1] - mi[1] * dH[0]};
+        const double dQ[3] = {dmi[1] * P_[2] - dmi[2] * P_[1] + mi[1] * dP[2] - mi[2] * dP[1],
+                              dmi[2] * P_[0] - dmi[0] * P_[2] + mi[2] * dP[0] - mi[0] * dP[2],
+                              dmi[0] * P_[1] - dmi[1] * P_[0] + mi[0] * dP[1] - mi[1] * dP[0]};
+        for (int c = 0; c < 3; ++c) dk[3 * i + c] = -gb * (s * dP[c] + p->alpha * dQ[c]);
+    }
+}
+
+/* out = N(y0 + dt sum c_j k_j), dout = dN(v)[dy0 + dt sum c_j dk_j]. */
+static void tangent_combine(const fo_problem *pr, double *out, double *dout, const double *y0, const double *dy0,
+                            int nk, double *const *ks, double *const *dks, const double *cs, double dt) {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        double v[3], dv[3];
+        for (int c = 0; c < 3; ++c) {
+            double a = 0.0, da = 0.0;
+            for (int j = 0; j < nk; ++j) {
+                a += cs[j] * ks[j][3 * i + c];
+                da += cs[j] * dks[j][3 * i + c];
+            }
+            v[c] = y0[3 * i + c] + a * dt;
+            dv[c] = dy0[3 * i + c] + da * dt;
+        }
+        const double nn = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        const double inv = nn > 0.0 ? 1.0 / nn : 0.0;
+        double u[3], ud = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            u[c] = v[c] * inv;
+            ud += u[c] * dv[c];
+        }
+        for (int c = 0; c < 3; ++c) {
+            out[3 * i + c] = u[c];
+            dout[3 * i + c] = (dv[c] - u[c] * ud) * inv;
+        }
+    }
+}
+
+int fo_tangent_rk4(fo_problem *pr, double dt, uint64_t n_steps, const double *dh_aos, const double *dm0_aos,
+                   double *dm_out) {
+    const fo_params *p = &pr->p;
+    if (p->has_cubic) return -1;
+    const long n = pr->n, n3 = 3 * n;
+    double *y0 = pr->m0, *ys = pr->mst, *ks[4], *dks[4];
+    double *dy0 = dalloc(n3), *dys = dalloc(n3), *ha = dalloc(n3), *hb = dalloc(n3), *dha = dalloc(n3),
+           *dhb = dalloc(n3), *ynext = dalloc(n3), *dynext = dalloc(n3);
+    for (int s = 0; s < 4; ++s) {
+        ks[s] = pr->k[s];
+        dks[s] = dalloc(n3);
+    }
+    if (dm0_aos)
+        for (long i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) dy0[3 * i + c] = active(pr, i) ? dm0_aos[3 * i + c] : 0.0;
+    memcpy(y0, pr->m, sizeof(double) * n3);
+    const double half[1] = {0.5}, one[1] = {1.0}, w[4] = {1.0 / 6.0, 2.0 / 6.0, 2.0 / 6.0, 1.0 / 6.0};
+    for (uint64_t st = 0; st < n_steps; ++st) {
+        tangent_rhs(pr, y0, dy0, dh_aos, ks[0], dks[0], ha, hb, dha, dhb);
+        tangent_combine(pr, ys, dys, y0, dy0, 1, &ks[0], &dks[0], half, dt);
+        tangent_rhs(pr, ys, dys, dh_aos, ks[1], dks[1], ha, hb, dha, dhb);
+        tangent_combine(pr, ys, dys, y0, dy0, 1, &ks[1], &dks[1], half, dt);
+        tangent_rhs(pr, ys, dys, dh_aos, ks[2], dks[2], ha, hb, dha, dhb);
+        tangent_combine(pr, ys, dys, y0, dy0, 1, &ks[2], &dks[2], one, dt);
+        tangent_rhs(pr, ys, dys, dh_aos, ks[3], dks[3], ha, hb, dha, dhb);
+        tangent_combine(pr, ynext, dynext, y0, dy0, 4, ks, dks, w, dt);
+        memcpy(y0, ynext, sizeof(double) * n3);
+        memcpy(dy0, dynext, sizeof(double) * n3);
+        pr->t += dt;
+        pr->step += 1.0;
+    }
+    memcpy(pr->m, y0, sizeof(double) * n3);
+    if (dm_out) memcpy(dm_out, dy0, sizeof(double) * n3);
+    pr->fsal_valid = 0;
+    free(dy0); free(dys); free(ha); free(hb); free(dha); free(dhb); free(ynext); free(dynext);
+    for (int s = 0; s < 4; ++s) free(dks[s]);
     return 0;
 }
 

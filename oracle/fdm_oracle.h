@@ -78,6 +78,8 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos);
 void fo_destroy(fo_problem *pr);
 int fo_set_m(fo_problem *pr, const double *m_aos);
 int fo_get_m(const fo_problem *pr, double *m_aos);
+/* Per-cell applied field (AoS, A/m) added to H_eff at active cells; NULL removes it. */
+int fo_set_field_map(fo_problem *pr, const double *h_aos);
 /* Fields at an arbitrary state (AoS in/out, any pointer may be NULL). */
 int fo_fields(fo_problem *pr, const double *m_aos, double *h_ex, double *h_demag,
               double *h_ext, double *h_eff, double *rhs);
@@ -85,6 +87,12 @@ int fo_fields(fo_problem *pr, const double *m_aos, double *h_ex, double *h_demag
 int fo_observe(fo_problem *pr, fo_stats *st);
 /* One accepted step with the ABI semantics of the configured integrator. */
 int fo_step(fo_problem *pr, double dt, fo_stats *st);
+/* FP64 tangent-linear model of n_steps fixed RK4 steps from the current state (which
+ * it advances): dm_out = d m_final [dm0, dh] for an initial-state perturbation dm0 and
+ * a field-map perturbation dh (A/m), either may be NULL.  Returns -1 with cubic
+ * anisotropy (not differentiated). */
+int fo_tangent_rk4(fo_problem *pr, double dt, uint64_t n_steps, const double *dh_aos, const double *dm0_aos,
+                   double *dm_out);
 /* Demag field by direct O(N^2) real-space Newell sum (FFT-independent check). */
 int fo_demag_direct(fo_problem *pr, const double *m_aos, double *h_demag);
 

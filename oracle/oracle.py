@@ -80,6 +80,8 @@ def lib():
         L.fo_destroy.argtypes = [C.c_void_p]
         L.fo_set_m.argtypes = [C.c_void_p, dp]
         L.fo_get_m.argtypes = [C.c_void_p, dp]
+        L.fo_set_field_map.argtypes = [C.c_void_p, dp]
+        L.fo_tangent_rk4.argtypes = [C.c_void_p, C.c_double, C.c_uint64, dp, dp, dp]
         L.fo_fields.argtypes = [C.c_void_p] + [dp] * 6
         L.fo_observe.argtypes = [C.c_void_p, C.POINTER(Stats)]
         L.fo_step.argtypes = [C.c_void_p, C.c_double, C.POINTER(Stats)]
@@ -195,6 +197,14 @@ class Problem:
         lib().fo_get_m(self._h, _dp(a))
         return a.reshape(self.n, 3)
 
+    def set_field_map(self, h):
+        """Per-cell applied field (n, 3) in A/m added at active cells; None removes it."""
+        if h is None:
+            lib().fo_set_field_map(self._h, None)
+            return
+        self._hmap = np.ascontiguousarray(h, dtype=np.float64).reshape(-1)
+        lib().fo_set_field_map(self._h, _dp(self._hmap))
+
     def fields(self, m=None):
         if m is None:
             m = self.get_m()
@@ -215,6 +225,15 @@ class Problem:
         if rc != 0:
             raise RuntimeError(f"oracle step failed ({rc})")
         return st.as_dict()
+
+    def tangent_rk4(self, dt, n_steps, dh=None, dm0=None):
+        """Advance n_steps RK4 steps and return d m_final along (dm0, dh) in FP64, (n, 3)."""
+        a = None if dh is None else np.ascontiguousarray(dh, dtype=np.float64).reshape(-1)
+        b = None if dm0 is None else np.ascontiguousarray(dm0, dtype=np.float64).reshape(-1)
+        out = np.zeros(3 * self.n)
+        if lib().fo_tangent_rk4(self._h, dt, n_steps, _dp(a), _dp(b), _dp(out)) != 0:
+            raise RuntimeError("oracle tangent failed (cubic anisotropy is not differentiated)")
+        return out.reshape(self.n, 3)
 
     def demag_direct(self, m=None):
         if m is None:

@@ -70,3 +70,31 @@ def test_rk45_tracks_heun(oracle):
     for _ in range(400):
         a.step(5e-15)
     assert np.abs(a.get_m() - b.get_m()).max() < 1e-3
+
+
+def test_tangent_rk4_matches_central_differences(oracle):
+    """The FP64 tangent-linear RK4 (checker of the engine's adjoint) against central
+    differences of full RK4 runs: second-order convergence to the tangent."""
+    nx, ny, n, dt, steps = 8, 4, 32, 5e-14, 40
+    rng = np.random.default_rng(0)
+    m0 = np.tile([1.0, 0.1, 0.0], (n, 1)) + 0.05 * rng.normal(size=(n, 3))
+    m0 /= np.linalg.norm(m0, axis=1, keepdims=True)
+    kw = problem(nx, ny, 1, alpha=0.05, b_mt=(5.0, 0.0, 0.0), ku1=1e4, u_axis=(1.0, 0.0, 0.0))
+    kw["m0"] = m0
+    hmap = rng.normal(0.0, 2e-3 / MU0, size=(n, 3))
+    dh, dm0 = rng.normal(size=(n, 3)), 0.1 * rng.normal(size=(n, 3))
+
+    def run(eps):
+        pr = oracle.Problem(**kw, integrator=oracle.RK4)
+        pr.set_field_map(hmap + eps * dh)
+        pr.set_m(m0 + eps * dm0)
+        for _ in range(steps):
+            pr.step(dt)
+        return pr.get_m()
+
+    pr = oracle.Problem(**kw, integrator=oracle.RK4)
+    pr.set_field_map(hmap)
+    tl = pr.tangent_rk4(dt, steps, dh=dh, dm0=dm0)
+    assert np.abs(pr.get_m() - run(0.0)).max() < 1e-14
+    errs = [np.abs((run(e) - run(-e)) / (2 * e) - tl).max() / np.abs(tl).max() for e in (1e-1, 1e-2)]
+    assert errs[1] < 1e-4 and errs[1] < errs[0] / 50
