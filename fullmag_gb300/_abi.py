@@ -237,6 +237,7 @@ SIGNATURES = [
     ("fullmag_fdm_batch_copy_field_f64", _i, [_vp, _u32, _i, _pd, _u64]),
     ("fullmag_fdm_batch_destroy", None, [_vp]),
     ("fullmag_fdm_backend_fft_shape", _i, [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    ("fullmag_fdm_backend_upload_magnetization_f64_noalloc", _i, [_vp, _pd, _u64]),
 ]
 
 REFERENCE_SYMBOLS = [s[0] for s in SIGNATURES[:22]]

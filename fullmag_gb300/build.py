@@ -16,7 +16,7 @@ PKG = Path(__file__).resolve().parent
 SRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libfullmag_fdm.so"
-SOURCES = ["row_pass.cu", "columns.cu", "engine.cu", "newell.cu", "adjoint.cu"]
+SOURCES = ["row_pass.cu", "columns.cu", "engine.cu", "newell.cu", "adjoint.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 

@@ -26,6 +26,7 @@
 
 #include "../../include/fullmag_fdm.h"
 #include "engine.h"
+#include "noalloc.h"
 
 namespace fm {
 
@@ -1041,6 +1042,16 @@ struct Engine {
         return true;
     }
 
+    // Same result as upload<double>, staged through the static scratch of noalloc.cu
+    // instead of the handle's lazily allocated staging buffer.
+    bool upload_noalloc(const double *m_xyz) {
+        if (cuda_fail("upload (no allocation)", noalloc_upload_f64(device, m_xyz, g.n, S[cur], mask, stream))) return false;
+        k1_valid = false;
+        fields_valid = false;
+        stats_valid = false;
+        return true;
+    }
+
     const float *field_ptr(int obs) {
         switch (obs) {
             case FULLMAG_FDM_OBSERVABLE_M: return S[cur];
@@ -1771,6 +1782,22 @@ int fullmag_fdm_backend_upload_magnetization_f64(fullmag_fdm_backend *handle, co
         return FULLMAG_FDM_ERR_INVALID;
     }
     return e->upload<double>(m_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
+}
+
+int fullmag_fdm_backend_upload_magnetization_f64_noalloc(fullmag_fdm_backend *handle, const double *m_xyz,
+                                                         uint64_t len) {
+    Engine *e = eng(handle);
+    if (!e || !m_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (len != 3 * (uint64_t)e->g.n) {
+        e->last_error = "magnetization length mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    if (e->g.n > kNoAllocMaxCells) {
+        e->last_error = "grid of " + std::to_string(e->g.n) + " cells exceeds the " + std::to_string(kNoAllocMaxCells) +
+                        "-cell limit of the allocation-free upload; use fullmag_fdm_backend_upload_magnetization_f64";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    return e->upload_noalloc(m_xyz) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
 }
 
 int fullmag_fdm_backend_upload_magnetization_f32(fullmag_fdm_backend *handle, const float *m_xyz, uint64_t len) {

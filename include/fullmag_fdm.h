@@ -415,6 +415,20 @@ int fullmag_fdm_batch_copy_field_f64(fullmag_fdm_batch *batch, uint32_t index, f
                                      double *out_xyz, uint64_t out_len);
 void fullmag_fdm_batch_destroy(fullmag_fdm_batch *batch);
 
+/* ---- Allocation-free upload (additive; no counterpart in the reference interface) ----
+ * Same result as fullmag_fdm_backend_upload_magnetization_f64, but it calls no
+ * allocating routine: the host doubles are staged in a fixed 6 MiB device array
+ * compiled into the library instead of a buffer the handle allocates on first use.
+ * For callers that must not allocate mid-run, e.g. a loop editing the state while
+ * other streams work (cudaMalloc/cudaFree can synchronise the whole device) or a
+ * process whose device memory is reserved up front.  Limits: grids of at most
+ * 262,144 cells (larger ones get FULLMAG_FDM_ERR_INVALID); the first call for a
+ * device resolves the array's address with cudaGetSymbolAddress, so make one call
+ * before any stream capture; all handles on a device share the array, so calls that
+ * overlap in time (several host threads) race and must be serialised by the caller. */
+int fullmag_fdm_backend_upload_magnetization_f64_noalloc(fullmag_fdm_backend *handle, const double *m_xyz,
+                                                         uint64_t len);
+
 #ifdef __cplusplus
 }
 #endif
