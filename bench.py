@@ -136,6 +136,95 @@ def run_sweep(args):
     print(json.dumps(out), flush=True)
 
 
+ADJOINT_WORKLOAD = "adjoint_256x64x1_rk4_4000"
+
+
+def adjoint_problem(nx=256, ny=64, seed=2):
+    """Inverse-design workload: a 256x64x1 film of 4 nm cells, Ms 8e5 A/m, A 1.3e-11 J/m,
+    alpha 0.05, uniform (5, 0, 0) mT plus a trainable in-plane field map B(x, y)
+    initialised N(0, 2 mT) (FP32, seeded), m0 = +x, and a smooth target: +x plus eight
+    seeded 2-D Gaussian bumps in m_y, renormalised."""
+    from fullmag_gb300 import _abi
+    rng = np.random.default_rng(seed)
+    n = nx * ny
+    bmap = rng.normal(0.0, 2e-3, size=(n, 2)).astype(np.float32)
+    yy, xx = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    bump = np.zeros((ny, nx))
+    for _ in range(8):
+        cx, cy = rng.uniform(0, nx), rng.uniform(0, ny)
+        sig = rng.uniform(4.0, 16.0)
+        amp = rng.uniform(0.5, 1.5) * rng.choice([-1.0, 1.0])
+        bump += amp * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) / (2 * sig ** 2))
+    target = np.zeros((n, 3))
+    target[:, 0] = 1.0
+    target[:, 1] = bump.reshape(-1)
+    target /= np.linalg.norm(target, axis=1, keepdims=True)
+    m0 = np.tile([1.0, 0.0, 0.0], (n, 1))
+    kw = dict(nx=nx, ny=ny, nz=1, dx=4e-9, dy=4e-9, dz=4e-9, ms=8e5, a_ex=1.3e-11, alpha=0.05, gamma=2.211e5,
+              m0=m0, h_ext=(5e-3 / MU0, 0.0, 0.0), integrator=_abi.INTEGRATOR_RK4)
+    return kw, bmap, target
+
+
+def run_adjoint(args):
+    """Gradients/s of mean |m_T - m*|^2 with respect to the field map through the
+    torch.autograd.Function (4000 RK4 steps, sqrt(N) checkpoints), wall clock with host
+    tensors in and out, plus the forward-only time of the same 4000 steps."""
+    import torch
+    from fullmag_gb300 import FdmBackend
+    from fullmag_gb300.adjoint import rk4_final_state
+    from fullmag_gb300.build import build
+    build()
+    kw, bmap, target = adjoint_problem()
+    n = kw["nx"] * kw["ny"]
+    dt, nsteps = 5e-14, args.adjoint_steps
+    be = FdmBackend(**kw)
+    m0 = torch.tensor(kw["m0"], dtype=torch.float64)
+    tgt = torch.tensor(target, dtype=torch.float64)
+    b = torch.tensor(bmap, requires_grad=True)
+    free0 = torch.cuda.mem_get_info()[0]
+
+    def gradient():
+        b.grad = None
+        m_t = rk4_final_state(m0, b, be, dt, nsteps)
+        loss = ((m_t - tgt) ** 2).mean()
+        loss.backward()
+        return float(loss.detach())
+
+    for _ in range(max(1, args.warmup)):
+        loss = gradient()
+    free1 = torch.cuda.mem_get_info()[0]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss = gradient()
+    t_grad = (time.perf_counter() - t0) / args.steps
+    g = b.grad.numpy().copy()
+    # forward-only cost of the same run (CUDA-graph fixed steps), for the cost ratio
+    be.upload(kw["m0"])
+    be.step_many(dt, nsteps)
+    t0 = time.perf_counter()
+    be.upload(kw["m0"])
+    be.step_many(dt, nsteps)
+    t_fwd = time.perf_counter() - t0
+    launches = be.launch_count()
+    be.close()
+    C = int(np.ceil(np.sqrt(nsteps)))
+    state = 12 * n  # bytes of one FP32 SoA state
+    out = {"metric": "adjoint gradients/s (d loss / d field map, %d RK4 steps)" % nsteps, "value": 1.0 / t_grad,
+           "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup),
+           "ms_per_step": 1e3 * t_grad, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": ADJOINT_WORKLOAD, "grid": [kw["nx"], kw["ny"], 1], "dt": dt, "rk4_steps": nsteps,
+                      "checkpoint_every": C},
+           "e2e": {"value": 1.0 / t_grad, "unit": "gradients/s", "h2d_bytes_per_step": 24 * n + 8 * 2 * n + 24 * n,
+                   "d2h_bytes_per_step": 24 * n + 24 * n + 24 * n},
+           "forward_only_s": t_fwd, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+           "memory": {"checkpoints_bytes": state * ((nsteps + C - 1) // C), "segment_bytes": state * 12 * C,
+                      "work_bytes": state * 12, "device_bytes_observed": int(free0 - free1),
+                      "store_everything_bytes": state * 12 * nsteps},
+           "loss": loss, "grad_abs_max": float(np.abs(g).max()), "engine_launches_total": launches}
+    print(json.dumps(out), flush=True)
+
+
 def smoothed_random_unit(nx, ny, nz, seed, passes=3):
     rng = np.random.default_rng(seed)
     m = rng.standard_normal((nz, ny, nx, 3))
@@ -291,7 +380,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD, ADJOINT_WORKLOAD])
+    ap.add_argument("--adjoint-steps", type=int, default=4000)
     ap.add_argument("--sweep-count", type=int, default=384)
     ap.add_argument("--sweep-t-end", type=float, default=0.5e-9)
     ap.add_argument("--sweep-sequential", type=int, default=8, help="problems solved one at a time for the baseline")
@@ -306,6 +397,10 @@ def main():
     if args.workload == SWEEP_WORKLOAD:
         if rank == 0:
             run_sweep(args)
+        return
+    if args.workload == ADJOINT_WORKLOAD:
+        if rank == 0:
+            run_adjoint(args)
         return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

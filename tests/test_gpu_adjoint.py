@@ -81,18 +81,18 @@ def test_gradient_vs_fp64_tangent(gpu_lib, oracle, ku1):
             assert np.abs(m_gpu - orc.get_m()).max() < 2e-5
         want = float(np.sum(w * dm))
         got = float(np.sum(grad * dh))
-        assert abs(got - want) <= 2e-3 * abs(want), (trial, got, want)
+        assert abs(got - want) <= 1e-4 * abs(want), (trial, got, want)
     dm0 = rng.normal(size=(n, 3)) * 0.1
     orc.set_m(kw["m0"])
     dm = orc.tangent_rk4(DT, steps, dm0=dm0)
     want = float(np.sum(w * dm))
     got = float(np.sum(lam0 * dm0))
-    assert abs(got - want) <= 2e-3 * abs(want), (got, want)
+    assert abs(got - want) <= 1e-4 * abs(want), (got, want)
 
 
 def test_torch_gradient_vs_central_fd(gpu_lib, oracle):
     """mean |m_T - m*|^2 through the autograd Function vs FP64 central differences
-    (step 1e-3 mT) of the oracle loss at random cells of the in-plane map."""
+    (step 1e-3 mT) of the oracle loss at 64 random cells of the in-plane map."""
     nx, ny, steps = 24, 12, 120
     kw, hmap = film(nx, ny, seed=9)
     n = nx * ny
@@ -117,16 +117,20 @@ def test_torch_gradient_vs_central_fd(gpu_lib, oracle):
 
     assert abs(oracle_loss(hmap[:, :2] * MU0) - float(loss.detach())) < 1e-6
     step = 1e-6  # 1e-3 mT in tesla
-    cells = rng.choice(n, size=12, replace=False)
-    gmax = np.abs(g).max()
+    cells = rng.choice(n, size=64, replace=False)
+    got, want = [], []
     for c in cells:
         for comp in range(2):
             bp = hmap[:, :2] * MU0
             bm = bp.copy()
             bp[c, comp] += step
             bm[c, comp] -= step
-            fd = (oracle_loss(bp) - oracle_loss(bm)) / (2 * step)
-            assert abs(g[c, comp] - fd) <= 2e-3 * gmax, (c, comp, g[c, comp], fd)
+            want.append((oracle_loss(bp) - oracle_loss(bm)) / (2 * step))
+            got.append(g[c, comp])
+    got, want = np.array(got), np.array(want)
+    # 1e-4 relative: in L2 over the 128 entries and per entry against the largest one
+    assert rel_l2(got, want) < 1e-4, rel_l2(got, want)
+    assert np.abs(got - want).max() <= 1e-4 * np.abs(want).max()
 
 
 def test_checkpoint_interval_invariance(gpu_lib, oracle):
