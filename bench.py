@@ -56,6 +56,32 @@ def model_bytes_per_cell_step(nx, ny, nz, integrator="rk4"):
     return sum(T(a) for a in (1, 2, 3, 4, 5, 5)) + 72
 
 
+def kernel_bytes_per_launch(kind, nx, ny, nz, padded):
+    """Algorithmic HBM bytes of one launch of a column pass: every spectrum element it
+    owns read and written once, every kernel value read once (FP32 complex = 8 B,
+    real kernel = 4 B).  Units: the X spectrum has 3 x nz x ny x nkx elements, the Y
+    spectrum 3 x nz x py x nkx, the octant kernel ncomp x nkz x nky x nkx values."""
+    px, py, pz = padded
+    nkx, nky, nkz = px // 2 + 1, py // 2 + 1, pz // 2 + 1
+    xs = 3 * nz * ny * nkx * 8
+    ys = 3 * nz * py * nkx * 8
+    if kind == "z_convolve":
+        return 2 * ys + 6 * nkz * nky * nkx * 4
+    if kind in ("y_forward", "y_inverse"):
+        return xs + ys
+    if kind == "yz_convolve":
+        return 2 * xs + 6 * nkz * nky * nkx * 4
+    if kind == "y_convolve_2d":
+        return 2 * xs + 4 * nky * nkx * 4
+    return None
+
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
+# the timed steps (profiles/launches_volume_256x256x64_rk4.md)
+NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 453.2e6, ("volume_256x256x64_rk4", "y_inverse"): 272.8e6,
+               ("volume_256x256x64_rk4", "y_forward"): 244.0e6, ("volume_256x256x64_rk4", "row_pass"): 308.7e6}
+
+
 WORKLOADS = {
     "volume_256x256x64_rk4": dict(nx=256, ny=256, nz=64, d=2e-9, ms=1.4e6, a_ex=2.1e-11, alpha=0.01,
                                   kc1=-4.8e4, dt=2e-14, integrator="rk4", seed=3),
@@ -377,7 +403,7 @@ def run_reference(args, w, name, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 300; 5 gradients for the adjoint)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
@@ -387,8 +413,11 @@ def main():
     ap.add_argument("--sweep-t-end", type=float, default=0.5e-9)
     ap.add_argument("--sweep-sequential", type=int, default=8, help="problems solved one at a time for the baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the cuFFT + unfused baseline leg")
     ap.add_argument("--profile", action="store_true", help="timed steps only: no e2e leg, no CPU baseline")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.workload == ADJOINT_WORKLOAD else 300
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
     rank = int(os.environ.get("RANK", "0"))
@@ -425,13 +454,16 @@ def main():
 
     be = FdmBackend(**kw, integrator=integ)
     stream = torch.cuda.ExternalStream(be.stream())
+    # the sampler starts before the warm-up so that nvidia-smi's own start-up does not
+    # overlap the timed steps; its samples cover the warm-up and the timed region
+    clocks = ClockSampler(int(os.environ["FULLMAG_FDM_GPU_INDEX"]))
+    clocks.start()
+    time.sleep(0.5)
     for _ in range(args.warmup):
         be.step(dt)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clocks = ClockSampler(int(os.environ["FULLMAG_FDM_GPU_INDEX"]))
-    clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = be.launch_count()
     torch.cuda.synchronize()
@@ -477,9 +509,25 @@ def main():
     h2d = 24.0 * n / args.steps
     d2h = 24.0 * n / args.steps + 120.0
 
+    # ---- per-kernel CUDA-event timing of the same step (launch by launch, no graph) ----
+    kt_steps = min(args.steps, 50)
+    be.set_kernel_timing(True)
+    for _ in range(kt_steps):
+        be.step(dt)
+    ktimes = be.kernel_times()
+    be.set_kernel_timing(False)
+    kt_total = sum(v[0] for v in ktimes.values())
+    dominant = max(ktimes, key=lambda k: ktimes[k][0])
+    dom_ms, dom_n = ktimes[dominant]
+    dom_avg_s = dom_ms / max(dom_n, 1) * 1e-3
+    padded = be.fft_shape()
+    dom_bytes = kernel_bytes_per_launch(dominant, w["nx"], w["ny"], w["nz"], padded)
+    traffic = NCU_TRAFFIC.get((args.workload, dominant))
+
     peak, peak_kind = load_peaks()
     bpc = model_bytes_per_cell_step(w["nx"], w["ny"], w["nz"], w["integrator"])
     achieved = bpc * n / (ms_per_step * 1e-3) / 1e9
+    dom_achieved = dom_bytes / dom_avg_s / 1e9 if dom_bytes else None
     out = {
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -487,9 +535,16 @@ def main():
         "config": {"workload": args.workload, "grid": [w["nx"], w["ny"], w["nz"]], "integrator": w["integrator"],
                    "dt": dt, "padded": list(be.fft_shape()), "tuning": be.tuning(), "parallelism": "replicas" if world > 1 else "single",
                    "l2_flush": "none needed: working set > 129 MB L2"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
-                     "note": f"whole step; model v1 {bpc:.1f} B/cell-step; peak {peak_kind}"},
+        "roofline": {"bound": "hbm", "achieved": dom_achieved, "peak": peak, "unit": "GB/s",
+                     "frac": dom_achieved / peak if (peak and dom_achieved) else None, "traffic": traffic,
+                     "kernel": dominant, "bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg_s * 1e3,
+                     "launches_timed": dom_n, "share_of_step": dom_ms / kt_total if kt_total else None,
+                     "note": f"dominant kernel, CUDA events per launch over {kt_steps} eager steps; "
+                             f"peak {peak_kind} (copy bandwidth)"},
+        "roofline_step": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak if peak else None,
+                          "note": f"whole step, compulsory-traffic model v1 {bpc:.1f} B/cell-step"},
+        "kernel_times_ms_per_launch": {k: (v[0] / v[1] if v[1] else None) for k, v in ktimes.items()},
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
@@ -497,6 +552,25 @@ def main():
         "m_norm_max_dev": float(np.abs(np.linalg.norm(m_out, axis=1) - 1).max()),
     }
     be.close()
+    if not args.no_plain:
+        # the cuFFT + unfused path (reference per-step kernel structure), same workload;
+        # each of its steps ends in blocking copies, so wall clock is its device time
+        from fullmag_gb300.plain import PlainBaseline
+        pb = PlainBaseline(**kw, integrator=integ)
+        for _ in range(2):
+            pb.step(dt)
+        kp = min(args.steps, 30)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(kp):
+            pb.step(dt)
+        tp = time.perf_counter() - t0
+        m_plain = pb.magnetization()
+        pb.close()
+        out["plain"] = {"value": n * kp / tp, "unit": "cell-steps/s", "ms_per_step": 1e3 * tp / kp, "steps": kp,
+                        "kind": "repo-written cuFFT C2C + one kernel per operation (reference kernel sequence)"}
+        out["fused_over_plain"] = value / out["plain"]["value"]
+        del m_plain
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
     if rank == 0:

@@ -226,6 +226,8 @@ SIGNATURES = [
     ("fullmag_fdm_backend_stream", _i, [_vp, C.POINTER(_vp)]),
     ("fullmag_fdm_backend_tuning", _i, [_vp, C.POINTER(_u32)]),
     ("fullmag_fdm_backend_launch_count", _i, [_vp, C.POINTER(_u64)]),
+    ("fullmag_fdm_backend_set_kernel_timing", _i, [_vp, _i]),
+    ("fullmag_fdm_backend_kernel_times", _i, [_vp, _pd, C.POINTER(_u64), _u32]),
     ("fullmag_fdm_backend_set_field_map", _i, [_vp, _pd, _u64]),
     ("fullmag_fdm_adjoint_forward", _i, [_vp, _d, _u64, _u32]),
     ("fullmag_fdm_adjoint_backward", _i, [_vp, _pd, _u64, _pd, _pd]),

@@ -285,6 +285,22 @@ class FdmBackend:
         self._check(self.lib.fullmag_fdm_backend_launch_count(self.handle, C.byref(c)), "launch_count")
         return c.value
 
+    KERNEL_KINDS = ("row_pass", "y_forward", "z_convolve", "y_inverse", "yz_convolve", "y_convolve_2d",
+                    "finalize_stats")
+
+    def set_kernel_timing(self, enable: bool):
+        """Per-launch CUDA-event timing of every kernel (fixed steps then run without graphs)."""
+        self._check(self.lib.fullmag_fdm_backend_set_kernel_timing(self.handle, int(bool(enable))),
+                    "set_kernel_timing")
+
+    def kernel_times(self) -> dict:
+        """{kind: (total_ms, launches)} since timing was enabled."""
+        k = len(self.KERNEL_KINDS)
+        ms = (C.c_double * k)()
+        cnt = (C.c_uint64 * k)()
+        self._check(self.lib.fullmag_fdm_backend_kernel_times(self.handle, ms, cnt, k), "kernel_times")
+        return {name: (ms[i], cnt[i]) for i, name in enumerate(self.KERNEL_KINDS)}
+
     def stream(self) -> int:
         s = C.c_void_p()
         self._check(self.lib.fullmag_fdm_backend_stream(self.handle, C.byref(s)), "stream")

@@ -17,6 +17,9 @@ SRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libfullmag_fdm.so"
 SOURCES = ["row_pass.cu", "columns.cu", "engine.cu", "newell.cu", "adjoint.cu", "noalloc.cu"]
+# the cuFFT + unfused measurement baseline: a separate library, never linked into the product
+PLAIN_SOURCES = ["plain_baseline.cu"]
+PLAIN_LIB = OUT / "libfullmag_fdm_plain.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
@@ -29,10 +32,10 @@ def nvcc() -> str:
 
 
 def _stale() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not PLAIN_LIB.exists():
         return True
-    t = LIB.stat().st_mtime
-    deps = [SRC / s for s in SOURCES if (SRC / s).exists()]
+    t = min(LIB.stat().st_mtime, PLAIN_LIB.stat().st_mtime)
+    deps = [SRC / s for s in SOURCES + PLAIN_SOURCES if (SRC / s).exists()]
     deps += list(SRC.glob("*.cuh")) + list(SRC.glob("*.h")) + [PKG.parent / "include" / "fullmag_fdm.h"]
     return any(d.stat().st_mtime > t for d in deps)
 
@@ -42,7 +45,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return LIB
     OUT.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
-    srcs = [s for s in SOURCES if (SRC / s).exists()]
+    srcs = [s for s in SOURCES + PLAIN_SOURCES if (SRC / s).exists()]
 
     def compile_one(s: str) -> Path:
         obj = OUT / (Path(s).stem + ".o")
@@ -55,13 +58,18 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return obj
 
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        objs = list(ex.map(compile_one, srcs))
-    tmp = OUT / "libfullmag_fdm.so.tmp"
-    cmd = [cc, "-shared", *ARCH, *map(str, objs), "-o", str(tmp), "-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
+        objs = dict(zip(srcs, ex.map(compile_one, srcs)))
+
+    def link(out: Path, parts, libs):
+        tmp = out.with_name(out.name + ".tmp")
+        cmd = [cc, "-shared", *ARCH, *map(str, parts), "-o", str(tmp), *libs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link of {out.name} failed:\n{r.stderr}")
+        os.replace(tmp, out)
+
+    link(LIB, [objs[s] for s in SOURCES if s in objs], ["-lcudart"])
+    link(PLAIN_LIB, [objs[s] for s in PLAIN_SOURCES if s in objs] + [objs["newell.cu"]], ["-lcufft", "-lcudart"])
     return LIB
 
 

@@ -152,6 +152,7 @@ struct Engine {
     void release() {
         if (stream) cudaStreamSynchronize(stream);
         drop_graphs();
+        kt_free();
         adj_free();
         if (hmap) cudaFree(hmap);
         hmap = nullptr;
@@ -265,6 +266,64 @@ struct Engine {
     std::vector<RowPass> *rec_rows = nullptr;
     std::vector<int> *rec_cols = nullptr;
 
+    // ---- per-kernel timing (off by default) ----
+    // With timing on, fixed steps run eagerly (no graph) and every launch is bracketed
+    // by a pair of events on the engine's stream; the elapsed times are summed per
+    // kernel kind whenever the stream has been synchronised.
+    enum { KT_ROW, KT_YF, KT_Z, KT_YI, KT_YZ, KT_Y2D, KT_FIN, KT_N };
+    bool ktime = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_ev;
+    std::vector<int> kt_kind;
+    size_t kt_used = 0;
+    double kt_ms[KT_N] = {};
+    uint64_t kt_cnt[KT_N] = {};
+
+    bool kt_armed = false;
+    void kt_begin(int kind) {
+        kt_armed = false;
+        if (!ktime || rec_rows) return;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+        if (kt_used == kt_ev.size()) {
+            cudaEvent_t a = nullptr, b = nullptr;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            kt_ev.push_back({a, b});
+            kt_kind.push_back(0);
+        }
+        kt_kind[kt_used] = kind;
+        kt_armed = cudaEventRecord(kt_ev[kt_used].first, stream) == cudaSuccess;
+    }
+    void kt_end() {
+        if (!kt_armed) return;
+        kt_armed = false;
+        if (cudaEventRecord(kt_ev[kt_used].second, stream) == cudaSuccess) ++kt_used;
+    }
+    // call only after the stream has been synchronised
+    void kt_collect() {
+        bool failed = false;
+        for (size_t i = 0; i < kt_used; ++i) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, kt_ev[i].first, kt_ev[i].second) == cudaSuccess) {
+                kt_ms[kt_kind[i]] += ms;
+                kt_cnt[kt_kind[i]] += 1;
+            } else {
+                failed = true;
+            }
+        }
+        if (failed) cudaGetLastError();  // a pair that did not complete: skipped, not an engine error
+        kt_used = 0;
+    }
+    void kt_free() {
+        for (auto &e : kt_ev) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+        kt_ev.clear();
+        kt_kind.clear();
+        kt_used = 0;
+    }
+
     bool run_row(RowPass &p) {
         if (!demag) {
             p.x_in = nullptr;
@@ -275,7 +334,10 @@ struct Engine {
             return true;
         }
         launches += 1;
-        return !cuda_fail("row pass", launch_row_pass(p, stream));
+        kt_begin(KT_ROW);
+        const cudaError_t rc = launch_row_pass(p, stream);
+        kt_end();
+        return !cuda_fail("row pass", rc);
     }
 
     // kx tile widths of the column passes (autotuned at create, see autotune());
@@ -308,18 +370,34 @@ struct Engine {
             rec_cols->push_back(g.thin ? 0 : 1);
             return true;
         }
+        cudaError_t rc;
         if (g.thin) {
             launches += 1;
-            return !cuda_fail("y convolve", launch_y_convolve_2d(col_pass(plan_y, tx_2d, X, X), stream));
+            kt_begin(KT_Y2D);
+            rc = launch_y_convolve_2d(col_pass(plan_y, tx_2d, X, X), stream);
+            kt_end();
+            return !cuda_fail("y convolve", rc);
         }
         if (use_yz) {
             launches += 1;
-            return !cuda_fail("yz convolve", launch_yz_convolve(col_pass(plan_y, tx_z, X, X), stream));
+            kt_begin(KT_YZ);
+            rc = launch_yz_convolve(col_pass(plan_y, tx_z, X, X), stream);
+            kt_end();
+            return !cuda_fail("yz convolve", rc);
         }
-        if (cuda_fail("y forward", launch_y_forward(col_pass(plan_y, tx_yf, X, Y), stream))) return false;
-        if (cuda_fail("z convolve", launch_z_convolve(col_pass(plan_z, tx_z, Y, Y), stream))) return false;
+        kt_begin(KT_YF);
+        rc = launch_y_forward(col_pass(plan_y, tx_yf, X, Y), stream);
+        kt_end();
+        if (cuda_fail("y forward", rc)) return false;
+        kt_begin(KT_Z);
+        rc = launch_z_convolve(col_pass(plan_z, tx_z, Y, Y), stream);
+        kt_end();
+        if (cuda_fail("z convolve", rc)) return false;
         launches += 3;
-        return !cuda_fail("y inverse", launch_y_inverse(col_pass(plan_y, tx_yi, Y, X), stream));
+        kt_begin(KT_YI);
+        rc = launch_y_inverse(col_pass(plan_y, tx_yi, Y, X), stream);
+        kt_end();
+        return !cuda_fail("y inverse", rc);
     }
 
     // ---- autotuner: tile widths of the column passes and rows per CTA of the row
@@ -359,12 +437,19 @@ struct Engine {
     bool enqueue_stats() {
         if (rec_rows) return true;  // the batched round finalizes all problems at once
         launches += 1;
-        if (cuda_fail("finalize", launch_finalize_stats(partials, row_blocks, dstats, stream))) return false;
+        kt_begin(KT_FIN);
+        const cudaError_t rc = launch_finalize_stats(partials, row_blocks, dstats, stream);
+        kt_end();
+        if (cuda_fail("finalize", rc)) return false;
         return !cuda_fail("stats copy",
                           cudaMemcpyAsync(hstats, dstats, sizeof(double) * kNumStats, cudaMemcpyDeviceToHost, stream));
     }
 
-    bool read_stats() { return enqueue_stats() && !cuda_fail("stream sync", cudaStreamSynchronize(stream)); }
+    bool read_stats() {
+        if (!enqueue_stats() || cuda_fail("stream sync", cudaStreamSynchronize(stream))) return false;
+        kt_collect();
+        return true;
+    }
 
     void fill_stats(const double *d, fullmag_fdm_step_stats &st) const {
         const double V = dx * dy * dz;
@@ -521,7 +606,7 @@ struct Engine {
     int step_fixed(double dt) {
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
-        if (poll == nullptr && use_graphs) {
+        if (poll == nullptr && use_graphs && !ktime) {
             if ((!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
                 // capture unavailable: clear the sticky state and fall back to eager launches
                 cudaGetLastError();
@@ -545,6 +630,7 @@ struct Engine {
     bool ensure_k1() { return k1_valid || eval_state(false); }
 
     void commit(double dt, const double *raw) {
+        kt_collect();
         cur = 1 - cur;
         memcpy(stat_raw, raw, sizeof(stat_raw));
         step_count += 1;
@@ -1910,6 +1996,31 @@ int fullmag_fdm_adjoint_backward(fullmag_fdm_backend *handle, const double *lamb
     }
     e->last_error.clear();
     return e->adjoint_backward(lambda_xyz, grad_field_map_xyz, lambda0_xyz);
+}
+
+int fullmag_fdm_backend_set_kernel_timing(fullmag_fdm_backend *handle, int enable) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess) return FULLMAG_FDM_ERR_CUDA;
+    e->kt_collect();
+    e->ktime = enable != 0;
+    for (int k = 0; k < Engine::KT_N; ++k) {
+        e->kt_ms[k] = 0.0;
+        e->kt_cnt[k] = 0;
+    }
+    return FULLMAG_FDM_OK;
+}
+
+int fullmag_fdm_backend_kernel_times(fullmag_fdm_backend *handle, double *total_ms, uint64_t *counts, uint32_t n_kinds) {
+    Engine *e = eng(handle);
+    if (!e || !e->arena || !total_ms || !counts) return FULLMAG_FDM_ERR_INVALID;
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess) return FULLMAG_FDM_ERR_CUDA;
+    e->kt_collect();
+    for (uint32_t k = 0; k < n_kinds; ++k) {
+        total_ms[k] = k < (uint32_t)Engine::KT_N ? e->kt_ms[k] : 0.0;
+        counts[k] = k < (uint32_t)Engine::KT_N ? e->kt_cnt[k] : 0;
+    }
+    return FULLMAG_FDM_OK;
 }
 
 int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out5) {

@@ -8,10 +8,10 @@
 // per line; the Stockham index map keeps the result in natural order.
 //
 // Power-of-two lengths (every padded extent of the reference's 2n grids when n
-// is a power of two) take a compile-time path: radix-8 stages then one radix-4
-// or radix-2 stage, all index arithmetic folded to shifts and masks.  Other
-// lengths use the runtime path with radices 8, 4, 2 and an O(R^2) loop for any
-// other prime factor.  Twiddles are FP64-computed host-side and stored as
+// is a power of two) take a compile-time path: radix-16 stages where possible,
+// then radix 8 or 4 (pow2_radix: never a lone radix-2 stage), all index
+// arithmetic folded to shifts and masks.  Other lengths use the runtime path
+// with radices 8, 4, 2 and an O(R^2) loop for any other prime factor.  Twiddles are FP64-computed host-side and stored as
 // float2 e^{-2 pi i e / n}; the inverse conjugates them.
 #pragma once
 #include <cuda_runtime.h>

@@ -376,6 +376,15 @@ int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_
 int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
                                   uint32_t *out_py, uint32_t *out_pz);
 
+/* ---- Per-kernel timing (additive; no counterpart in the reference interface) ----
+ * With timing enabled, fixed steps run launch by launch (no CUDA graph) and every
+ * kernel launch is bracketed by CUDA events on the handle's stream.  Enabling or
+ * disabling resets the totals.  kernel_times fills n_kinds entries in the order
+ * row pass, y forward, z convolve, y inverse, fused y+z, thin-film y, statistics
+ * finalize: total milliseconds and launch counts since timing was enabled. */
+int fullmag_fdm_backend_set_kernel_timing(fullmag_fdm_backend *handle, int enable);
+int fullmag_fdm_backend_kernel_times(fullmag_fdm_backend *handle, double *total_ms, uint64_t *counts, uint32_t n_kinds);
+
 /* ---- Adjoint gradients (additive; no counterpart in the reference interface) ----
  * A per-cell applied field map (A/m, AoS, 3*cell_count) is added to H_eff at active
  * cells; NULL removes it.  The adjoint of a fixed-step RK4 run is split in two calls:
