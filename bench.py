@@ -76,6 +76,22 @@ def kernel_bytes_per_launch(kind, nx, ny, nz, padded):
     return None
 
 
+def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
+    """Average algorithmic bytes of one row-pass launch over a fixed step.  Per cell:
+    state / stage vectors 12 B each, the X half spectrum S = 24 (nx + 1) / nx B (read
+    before and written after each evaluation).  RK4 passes: (1) m0 + k1 -> y1, forward x:
+    36 + S; (2), (3) inverse x, y_s, m0 -> k_s, y_{s+1}, forward x: 48 + 2S; (4) inverse x,
+    y3, m0, k1..k3 -> m', forward x: 72 + 2S; (5) inverse x, m' -> k1 (+ statistics):
+    24 + S.  Heun: 36 + S, 60 + 2S, 24 + S."""
+    n = nx * ny * nz
+    S = 24.0 * (nx + 1) / nx if demag else 0.0
+    if integrator == "rk4":
+        per_cell = [36 + S, 48 + 2 * S, 48 + 2 * S, 72 + 2 * S, 24 + S]
+    else:
+        per_cell = [36 + S, 60 + 2 * S, 24 + S]
+    return sum(per_cell) / len(per_cell) * n
+
+
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
 # the timed steps (profiles/launches_volume_256x256x64_rk4.md)
 NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 453.2e6, ("volume_256x256x64_rk4", "y_inverse"): 272.8e6,
@@ -521,7 +537,10 @@ def main():
     dom_ms, dom_n = ktimes[dominant]
     dom_avg_s = dom_ms / max(dom_n, 1) * 1e-3
     padded = be.fft_shape()
-    dom_bytes = kernel_bytes_per_launch(dominant, w["nx"], w["ny"], w["nz"], padded)
+    if dominant == "row_pass":
+        dom_bytes = row_pass_bytes_per_launch(w["integrator"], w["nx"], w["ny"], w["nz"])
+    else:
+        dom_bytes = kernel_bytes_per_launch(dominant, w["nx"], w["ny"], w["nz"], padded)
     traffic = NCU_TRAFFIC.get((args.workload, dominant))
 
     peak, peak_kind = load_peaks()

@@ -163,6 +163,237 @@ __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
     }
 }
 
+// ---- pruned two-level transforms (power-of-two lengths N = N1 * N2) ----
+// With n = N2 n1 + n2 and k = k1 + N1 k2:
+//   X[k1 + N1 k2] = sum_n2 W_N2^{n2 k2} W_N^{n2 k1} sum_n1 x[N2 n1 + n2] W_N1^{n1 k1}.
+// Inputs vanish for n >= N/2 (n1 >= N1/2) on the forward side and only n < N/2 is kept
+// on the inverse side, so the outer N1-point passes run on half lines.
+
+// Half-input N1-point DFT of e[0..N1/2) (two N1/2-point DFTs: even and odd outputs),
+// times W_N^{n2 k1}, stored at line[sk(k1 * N2 + n2)].
+template <int N1, int N2>
+__device__ __forceinline__ void half_dft_store(float2 (&e)[N1 / 2], int n2, float2 *line, const float2 *__restrict__ tw) {
+    constexpr int H1 = N1 / 2;
+    float2 o[H1];
+    o[0] = e[0];
+#pragma unroll
+    for (int n1 = 1; n1 < H1; ++n1) o[n1] = cmul(e[n1], __ldg(tw + n1 * N2));
+    dft_small<H1>(e, false);
+    dft_small<H1>(o, false);
+#pragma unroll
+    for (int u = 0; u < H1; ++u) {
+        const int ka = 2 * u, kb = 2 * u + 1;
+        line[sk(ka * N2 + n2)] = (n2 && ka) ? cmul(e[u], __ldg(tw + n2 * ka)) : e[u];
+        line[sk(kb * N2 + n2)] = n2 ? cmul(o[u], __ldg(tw + n2 * kb)) : o[u];
+    }
+}
+
+// Half-output inverse N1-point DFT over line[sk(k1 * N2 + n2)], k1 in [0, N1): returns
+// y[n1] for n1 < N1/2 in e (two N1/2-point inverses combined with W_N1^{-n1}).
+template <int N1, int N2>
+__device__ __forceinline__ void half_idft_load(float2 (&e)[N1 / 2], int n2, const float2 *line,
+                                               const float2 *__restrict__ tw) {
+    constexpr int H1 = N1 / 2;
+    float2 o[H1];
+#pragma unroll
+    for (int u = 0; u < H1; ++u) {
+        e[u] = line[sk(2 * u * N2 + n2)];
+        o[u] = line[sk((2 * u + 1) * N2 + n2)];
+    }
+    dft_small<H1>(e, true);
+    dft_small<H1>(o, true);
+    e[0] = cadd(e[0], o[0]);
+#pragma unroll
+    for (int n1 = 1; n1 < H1; ++n1) e[n1] = cadd(e[n1], cmul(o[n1], cconj(__ldg(tw + n1 * N2))));
+}
+
+// X[c][z][y<ny][kx] -> Y[c][z][ky<py][kx], py = N1 * N2: half-input outer pass from
+// global memory, inner N2-point pass straight to global memory, one barrier.
+template <int N1, int N2>
+__global__ void __launch_bounds__(kThreads, 2) y_forward_fused_kernel(const ColPass p) {
+    constexpr int N = N1 * N2, H1 = N1 / 2;
+    constexpr int ls = skewed_len(N);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *buf = reinterpret_cast<float2 *>(smem);
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int z = blockIdx.y, c = blockIdx.z;
+    const float2 *__restrict__ tw = p.plan.tw;
+    const float2 *src = p.in + ((size_t)c * g.nz + z) * g.ny * g.nkx + kx0;
+    for (int it = threadIdx.x; it < N2 * tx; it += blockDim.x) {
+        const int n2 = p.fd_tx.div(it), col = it - n2 * tx;
+        const bool okc = col < ncol;
+        float2 e[H1];
+#pragma unroll
+        for (int n1 = 0; n1 < H1; ++n1) {
+            const int y = N2 * n1 + n2;
+            e[n1] = (okc && y < g.ny) ? src[(size_t)y * g.nkx + col] : make_float2(0.f, 0.f);
+        }
+        half_dft_store<N1, N2>(e, n2, buf + col * ls, tw);
+    }
+    __syncthreads();
+    float2 *dst = p.out + ((size_t)c * g.nz + z) * g.py * g.nkx + kx0;
+    for (int it = threadIdx.x; it < N1 * tx; it += blockDim.x) {
+        const int k1 = p.fd_tx.div(it), col = it - k1 * tx;
+        const float2 *line = buf + col * ls;
+        float2 v[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) v[n2] = line[sk(k1 * N2 + n2)];
+        dft_small<N2>(v, false);
+        if (col < ncol) {
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) dst[(size_t)(k1 + N1 * k2) * g.nkx + col] = v[k2];
+        }
+    }
+}
+
+// Y[c][z][ky][kx] -> X[c][z][y<ny][kx]: inner inverse N2-point pass from global memory,
+// half-output outer pass straight to global memory, one barrier.
+template <int N1, int N2>
+__global__ void __launch_bounds__(kThreads, 2) y_inverse_fused_kernel(const ColPass p) {
+    constexpr int N = N1 * N2, H1 = N1 / 2;
+    constexpr int ls = skewed_len(N);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *buf = reinterpret_cast<float2 *>(smem);
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int z = blockIdx.y, c = blockIdx.z;
+    const float2 *__restrict__ tw = p.plan.tw;
+    const float2 *src = p.in + ((size_t)c * g.nz + z) * g.py * g.nkx + kx0;
+    for (int it = threadIdx.x; it < N1 * tx; it += blockDim.x) {
+        const int k1 = p.fd_tx.div(it), col = it - k1 * tx;
+        const bool okc = col < ncol;
+        float2 v[N2];
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) v[k2] = okc ? src[(size_t)(k1 + N1 * k2) * g.nkx + col] : make_float2(0.f, 0.f);
+        dft_small<N2>(v, true);
+        float2 *line = buf + col * ls;
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2)
+            line[sk(k1 * N2 + n2)] = (n2 && k1) ? cmul(v[n2], cconj(__ldg(tw + n2 * k1))) : v[n2];
+    }
+    __syncthreads();
+    float2 *dst = p.out + ((size_t)c * g.nz + z) * g.ny * g.nkx + kx0;
+    for (int it = threadIdx.x; it < N2 * tx; it += blockDim.x) {
+        const int n2 = p.fd_tx.div(it), col = it - n2 * tx;
+        float2 e[H1];
+        half_idft_load<N1, N2>(e, n2, buf + col * ls, tw);
+        if (col < ncol) {
+#pragma unroll
+            for (int n1 = 0; n1 < H1; ++n1) {
+                const int y = N2 * n1 + n2;
+                if (y < g.ny) dst[(size_t)y * g.nkx + col] = e[n1];
+            }
+        }
+    }
+}
+
+// Pruned two-level z convolution for power-of-two pz = N1 * N2.  With z = N2 z1 + z2 and
+// k = k1 + N1 k2 the transform of one z line is
+//   X[k1 + N1 k2] = sum_z2 W_N2^{z2 k2} W_pz^{z2 k1} sum_z1 x[N2 z1 + z2] W_N1^{z1 k1}
+// and its inverse runs the same factors backwards.  Inputs vanish for z >= pz/2 (z1 >=
+// N1/2) and only z < nz <= pz/2 is kept, so the outer N1-point passes work on half
+// lines: a half-input DFT is two N1/2-point DFTs (even and odd outputs), a half-output
+// inverse is two N1/2-point inverses.  Phase 1 (line, z2): global loads straight into
+// registers, half-input DFT, twiddle, one shared-memory write.  Phase 2 (ky of the pair,
+// column, k1; all three components): N2-point DFTs, the tensor multiply, inverse
+// N2-point DFTs, conjugate twiddle, in place.  Phase 3 (line, z2): half-output inverse
+// straight to global memory.  Two barriers per tile, one buffer.
+template <int N1, int N2>
+__global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve_fused_kernel(const ColPass p) {
+    constexpr int N = N1 * N2, H1 = N1 / 2;
+    constexpr int ls = skewed_len(N);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *buf = reinterpret_cast<float2 *>(smem);  // line (q, c, col) at ((q*3 + c)*tx + col)*ls
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
+    const int kya = blockIdx.y;
+    int kyb;
+    const int np = ky_pair(kya, g.py, kyb);
+    const int nz = g.nz;
+    const size_t cstride = (size_t)nz * g.py * g.nkx;  // component stride of Y
+    const size_t zstride = (size_t)g.py * g.nkx;
+    const float2 *__restrict__ tw = p.plan.tw;        // e^{-2 pi i e / N}
+
+    // phase 1: item (r2, z2, col), col fastest
+    const int n13 = np * 3 * N2 * tx;
+    for (int it = threadIdx.x; it < n13; it += blockDim.x) {
+        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        const int z2 = rz & (N2 - 1), r2 = rz / N2;
+        const int q = r2 >= 3, c = r2 - 3 * q;
+        const int ky = q ? kyb : kya;
+        const float2 *src = p.in + c * cstride + (size_t)ky * g.nkx + kx0 + col;
+        const bool okc = col < ncol;
+        float2 e[H1];
+#pragma unroll
+        for (int z1 = 0; z1 < H1; ++z1) {
+            const int z = N2 * z1 + z2;
+            e[z1] = (okc && z < nz) ? src[(size_t)z * zstride] : make_float2(0.f, 0.f);
+        }
+        half_dft_store<N1, N2>(e, z2, buf + (r2 * tx + col) * ls, tw);
+    }
+    __syncthreads();
+
+    // phase 2: item (q, k1, col), col fastest; all three components of one frequency column
+    const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
+    const int n2 = np * N1 * tx;
+    for (int it = threadIdx.x; it < n2; it += blockDim.x) {
+        const int qk = p.fd_tx.div(it), col = it - qk * tx;
+        const int k1 = qk & (N1 - 1), q = qk / N1;
+        float2 m[3][N2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 *line = buf + ((q * 3 + c) * tx + col) * ls;
+#pragma unroll
+            for (int z2 = 0; z2 < N2; ++z2) m[c][z2] = line[sk(k1 * N2 + z2)];
+            dft_small<N2>(m[c], false);
+        }
+        const int kx = min(kx0 + col, g.nkx - 1);
+        // the second frequency of the pair is the y-mirror: odd-in-y components flip sign
+        const float sy = q ? -1.f : 1.f;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+            int kzm;
+            float sz;
+            kernel_mirror(k1 + N1 * k2, N, kzm, sz);
+            const float *K = p.kern + ((size_t)kzm * g.nky + kya) * g.nkx + kx;
+            const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
+            const float kxy = sy * __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz = sy * sz * __ldg(K + 5 * kc);
+            const float2 mx = m[0][k2], my = m[1][k2], mz = m[2][k2];
+            m[0][k2] = make_float2(-(kxx * mx.x + kxy * my.x + kxz * mz.x), -(kxx * mx.y + kxy * my.y + kxz * mz.y));
+            m[1][k2] = make_float2(-(kxy * mx.x + kyy * my.x + kyz * mz.x), -(kxy * mx.y + kyy * my.y + kyz * mz.y));
+            m[2][k2] = make_float2(-(kxz * mx.x + kyz * my.x + kzz * mz.x), -(kxz * mx.y + kyz * my.y + kzz * mz.y));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            dft_small<N2>(m[c], true);
+            float2 *line = buf + ((q * 3 + c) * tx + col) * ls;
+#pragma unroll
+            for (int z2 = 0; z2 < N2; ++z2)
+                line[sk(k1 * N2 + z2)] = (z2 && k1) ? cmul(m[c][z2], cconj(__ldg(tw + z2 * k1))) : m[c][z2];
+        }
+    }
+    __syncthreads();
+
+    // phase 3: item (r2, z2, col), col fastest; outputs z1 < N1/2 with z < nz
+    for (int it = threadIdx.x; it < n13; it += blockDim.x) {
+        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        const int z2 = rz & (N2 - 1), r2 = rz / N2;
+        const int q = r2 >= 3, c = r2 - 3 * q;
+        const int ky = q ? kyb : kya;
+        float2 e[H1];
+        half_idft_load<N1, N2>(e, z2, buf + (r2 * tx + col) * ls, tw);
+        if (col < ncol) {
+            float2 *dst = p.out + c * cstride + (size_t)ky * g.nkx + kx0 + col;
+#pragma unroll
+            for (int z1 = 0; z1 < H1; ++z1) {
+                const int z = N2 * z1 + z2;
+                if (z < nz) dst[(size_t)z * zstride] = e[z1];
+            }
+        }
+    }
+}
+
 // 3-D grids whose (y, z) plane fits in shared memory: forward y-transform of the nz
 // physical planes, in-smem transpose, forward z, multiply, inverse z, transpose back,
 // inverse y -- X -> X in place, one pass instead of three and no Y round trip.
@@ -388,7 +619,42 @@ int col_tile(const Grid &g, int lines_per_col, int len) {
     return tx;
 }
 
+namespace {
+// power-of-two py with every physical row in the lower half: the pruned two-level y passes
+bool y_fused_ok(const Grid &g) {
+    const int py = g.py;
+    return (py == 16 || py == 32 || py == 64 || py == 128 || py == 256 || py == 512) && 2 * g.ny <= py;
+}
+template <int N1, int N2, bool INV>
+cudaError_t launch_y_fused(const ColPass &p, cudaStream_t s) {
+    const size_t sm = sizeof(float2) * (size_t)p.tx * skewed_len(N1 * N2);
+    const void *fn = INV ? (const void *)y_inverse_fused_kernel<N1, N2> : (const void *)y_forward_fused_kernel<N1, N2>;
+    cudaError_t e = ensure_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    if (INV) y_inverse_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
+    else y_forward_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+template <bool INV>
+cudaError_t launch_y_dispatch(const ColPass &p, cudaStream_t s) {
+    switch (p.g.py) {
+        case 16: return launch_y_fused<4, 4, INV>(p, s);
+        case 32: return launch_y_fused<8, 4, INV>(p, s);
+        case 64: return launch_y_fused<8, 8, INV>(p, s);
+        case 128: return launch_y_fused<16, 8, INV>(p, s);
+        case 256: return launch_y_fused<16, 16, INV>(p, s);
+        default: return launch_y_fused<32, 16, INV>(p, s);
+    }
+}
+}  // namespace
+
+size_t y_pass_smem(const Grid &g, int tx) {
+    const size_t one = sizeof(float2) * (size_t)tx * skewed_len(g.py);
+    return y_fused_ok(g) ? one : 2 * one;
+}
+
 cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s) {
+    if (y_fused_ok(p.g)) return launch_y_dispatch<false>(p, s);
     const size_t sm = 2 * sizeof(float2) * (size_t)p.tx * skewed_len(p.g.py);
     cudaError_t e = ensure_smem((const void *)y_forward_kernel, sm);
     if (e != cudaSuccess) return e;
@@ -397,6 +663,7 @@ cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s) {
 }
 
 cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s) {
+    if (y_fused_ok(p.g)) return launch_y_dispatch<true>(p, s);
     const size_t sm = 2 * sizeof(float2) * (size_t)p.tx * skewed_len(p.g.py);
     cudaError_t e = ensure_smem((const void *)y_inverse_kernel, sm);
     if (e != cudaSuccess) return e;
@@ -404,7 +671,38 @@ cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+namespace {
+template <int N1, int N2>
+cudaError_t launch_z_fused(const ColPass &p, cudaStream_t s) {
+    const size_t sm = sizeof(float2) * (size_t)2 * 3 * p.tx * skewed_len(N1 * N2);
+    cudaError_t e = ensure_smem((const void *)z_convolve_fused_kernel<N1, N2>, sm);
+    if (e != cudaSuccess) return e;
+    z_convolve_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nky), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+// power-of-two pz with every physical plane in the lower half: the pruned fused kernel
+bool z_fused_ok(const Grid &g) {
+    const int pz = g.pz;
+    return (pz == 16 || pz == 32 || pz == 64 || pz == 128 || pz == 256 || pz == 512) && 2 * g.nz <= pz;
+}
+}  // namespace
+
+size_t z_convolve_smem(const Grid &g, int tx) {
+    const size_t one = sizeof(float2) * (size_t)2 * 3 * tx * skewed_len(g.pz);
+    return z_fused_ok(g) ? one : 2 * one;
+}
+
 cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
+    if (z_fused_ok(p.g)) {
+        switch (p.g.pz) {
+            case 16: return launch_z_fused<4, 4>(p, s);
+            case 32: return launch_z_fused<8, 4>(p, s);
+            case 64: return launch_z_fused<8, 8>(p, s);
+            case 128: return launch_z_fused<16, 8>(p, s);
+            case 256: return launch_z_fused<16, 16>(p, s);
+            default: return launch_z_fused<32, 16>(p, s);
+        }
+    }
     // room for a y-frequency pair: 2 x 3 lines per kx column, two ping-pong buffers
     const size_t sm = 2 * sizeof(float2) * (size_t)2 * 3 * p.tx * skewed_len(p.g.pz);
     cudaError_t e = ensure_smem((const void *)z_convolve_kernel, sm);

@@ -1558,12 +1558,25 @@ bool Engine::autotune() {
             }
             tx_z = best;
         } else {
-            tx_yf = best_tx(1, g.py, [&](int tx) { return launch_y_forward(col_pass(plan_y, tx, X, Y), stream) == cudaSuccess; },
-                            tx_yf);
-            tx_z = best_tx(6, g.pz, [&](int tx) { return launch_z_convolve(col_pass(plan_z, tx, Y, Y), stream) == cudaSuccess; },
-                           tx_z);
-            tx_yi = best_tx(1, g.py, [&](int tx) { return launch_y_inverse(col_pass(plan_y, tx, Y, X), stream) == cudaSuccess; },
-                            tx_yi);
+            // tile widths of the three column passes, each timed on its own
+            auto tune = [&](int cur_tx, const std::function<size_t(int)> &smem, const std::function<bool(int)> &run) {
+                int best = cur_tx;
+                float bt = 1e30f;
+                for (int tx : {1, 2, 4, 8, 16}) {
+                    if (tx > std::max(1, g.nkx) || smem(tx) > 200u * 1024u) continue;
+                    const float t = time_ms([&] { return run(tx); });
+                    if (t < bt) {
+                        bt = t;
+                        best = tx;
+                    }
+                }
+                return best;
+            };
+            auto ysm = [&](int tx) { return y_pass_smem(g, tx); };
+            tx_yf = tune(tx_yf, ysm, [&](int tx) { return launch_y_forward(col_pass(plan_y, tx, X, Y), stream) == cudaSuccess; });
+            tx_z = tune(tx_z, [&](int tx) { return z_convolve_smem(g, tx); },
+                        [&](int tx) { return launch_z_convolve(col_pass(plan_z, tx, Y, Y), stream) == cudaSuccess; });
+            tx_yi = tune(tx_yi, ysm, [&](int tx) { return launch_y_inverse(col_pass(plan_y, tx, Y, X), stream) == cudaSuccess; });
         }
     }
     if (!std::getenv("FULLMAG_FDM_ROWS_PER_CTA")) {

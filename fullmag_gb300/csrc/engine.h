@@ -122,6 +122,8 @@ cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
 cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s);  // X -> X (small 3-D, uses plan2 for z)
 size_t yz_convolve_smem(const Grid &g, int tx);
+size_t z_convolve_smem(const Grid &g, int tx);
+size_t y_pass_smem(const Grid &g, int tx);
 size_t y_convolve_2d_smem(const Grid &g, int tx);
 
 // Adjoint (reverse-mode RK4) element-wise passes (adjoint.cu); all fields SoA.

@@ -41,7 +41,27 @@ CASES = {
     "line_9x1x1": dict(nx=9, ny=1, nz=1),
     "single_1x1x1": dict(nx=1, ny=1, nz=1),
     "slab_12x10x2": dict(nx=12, ny=10, nz=2, d=(2e-9, 2e-9, 2e-9)),
+    # (y, z) planes too large for the fused y+z pass: y-forward / z-convolve / y-inverse,
+    # the z pass on its pruned two-level path for pz = 16, 32, 64, 128 and on the
+    # general path for pz = 24
+    "zcols_4x120x8": dict(nx=4, ny=120, nz=8, d=(2e-9, 2e-9, 2e-9)),
+    "zcols_4x64x16": dict(nx=4, ny=64, nz=16, d=(2e-9, 2e-9, 2e-9)),
+    "zcols_8x32x32": dict(nx=8, ny=32, nz=32, d=(2e-9, 2e-9, 2e-9)),
+    "zcols_8x16x64": dict(nx=8, ny=16, nz=64, d=(2e-9, 2e-9, 2e-9)),
+    "zcols_4x84x12": dict(nx=4, ny=84, nz=12, d=(2e-9, 2e-9, 2e-9)),
 }
+
+
+@pytest.mark.parametrize("name", [k for k in CASES if k.startswith("zcols")])
+def test_three_pass_columns_are_used(gpu_lib, oracle, name):
+    c = dict(CASES[name])
+    d = c.pop("d")
+    kw = problem(c["nx"], c["ny"], c["nz"], d=d, seed=3)
+    gpu = FdmBackend(**kw)
+    gpu.set_kernel_timing(True)
+    gpu.refresh()
+    kt = gpu.kernel_times()
+    assert kt["z_convolve"][1] >= 1 and kt["yz_convolve"][1] == 0, kt
 
 
 @pytest.mark.parametrize("name", list(CASES))
