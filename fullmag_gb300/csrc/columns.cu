@@ -479,7 +479,106 @@ __device__ __forceinline__ void yz_convolve_body(const ColPass &p, const int til
 
 // Thin film: forward y-transform of ny physical rows (zero-padded to py), multiply by
 // the 2-D kernel, inverse, keep ny rows.  X -> X in place.
+// Thin film, power-of-two py = N1 * N2 (2 ny <= py): the pruned two-level form of the
+// y convolution -- half-input outer pass from global memory, inner passes with the
+// 4-component multiply in registers, half-output outer inverse to global memory.
+template <int N1, int N2>
+__device__ __forceinline__ void y_convolve_2d_fused_body(const ColPass &p, const int tile) {
+    constexpr int N = N1 * N2, H1 = N1 / 2;
+    constexpr int ls = skewed_len(N);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *buf = reinterpret_cast<float2 *>(smem);  // line (c, col) at (c*tx + col)*ls
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
+    const size_t cstride = (size_t)g.ny * g.nkx;
+    const float2 *__restrict__ tw = p.plan.tw;
+    const int n13 = 3 * N2 * tx;
+    for (int it = threadIdx.x; it < n13; it += blockDim.x) {
+        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        const int n2 = rz & (N2 - 1), c = rz / N2;
+        const float2 *src = p.in + c * cstride + kx0 + col;
+        const bool okc = col < ncol;
+        float2 e[H1];
+#pragma unroll
+        for (int n1 = 0; n1 < H1; ++n1) {
+            const int y = N2 * n1 + n2;
+            e[n1] = (okc && y < g.ny) ? src[(size_t)y * g.nkx] : make_float2(0.f, 0.f);
+        }
+        half_dft_store<N1, N2>(e, n2, buf + (c * tx + col) * ls, tw);
+    }
+    __syncthreads();
+    const size_t kc = (size_t)g.nky * g.nkx;
+    for (int it = threadIdx.x; it < N1 * tx; it += blockDim.x) {
+        const int k1 = p.fd_tx.div(it), col = it - k1 * tx;
+        float2 m[3][N2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 *line = buf + (c * tx + col) * ls;
+#pragma unroll
+            for (int n2 = 0; n2 < N2; ++n2) m[c][n2] = line[sk(k1 * N2 + n2)];
+            dft_small<N2>(m[c], false);
+        }
+        const int kx = min(kx0 + col, g.nkx - 1);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+            int kym;
+            float sy;
+            kernel_mirror(k1 + N1 * k2, N, kym, sy);
+            const float *K = p.kern + (size_t)kym * g.nkx + kx;
+            const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc), kxy = sy * __ldg(K + 3 * kc);
+            const float2 mx = m[0][k2], my = m[1][k2], mz = m[2][k2];
+            m[0][k2] = make_float2(-(kxx * mx.x + kxy * my.x), -(kxx * mx.y + kxy * my.y));
+            m[1][k2] = make_float2(-(kxy * mx.x + kyy * my.x), -(kxy * mx.y + kyy * my.y));
+            m[2][k2] = make_float2(-(kzz * mz.x), -(kzz * mz.y));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            dft_small<N2>(m[c], true);
+            float2 *line = buf + (c * tx + col) * ls;
+#pragma unroll
+            for (int n2 = 0; n2 < N2; ++n2)
+                line[sk(k1 * N2 + n2)] = (n2 && k1) ? cmul(m[c][n2], cconj(__ldg(tw + n2 * k1))) : m[c][n2];
+        }
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < n13; it += blockDim.x) {
+        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        const int n2 = rz & (N2 - 1), c = rz / N2;
+        float2 e[H1];
+        half_idft_load<N1, N2>(e, n2, buf + (c * tx + col) * ls, tw);
+        if (col < ncol) {
+            float2 *dst = p.out + c * cstride + kx0 + col;
+#pragma unroll
+            for (int n1 = 0; n1 < H1; ++n1) {
+                const int y = N2 * n1 + n2;
+                if (y < g.ny) dst[(size_t)y * g.nkx] = e[n1];
+            }
+        }
+    }
+}
+
+// (py = 512 keeps the general path: its inner pass would hold 3 x 16 complex values)
+__host__ __device__ __forceinline__ bool y2d_fused_ok(const Grid &g) {
+    const int py = g.py;
+    return (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py;
+}
+
+__device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, const int tile);
+
 __device__ __forceinline__ void y_convolve_2d_body(const ColPass &p, const int tile) {
+    if (y2d_fused_ok(p.g)) {
+        switch (p.g.py) {
+            case 16: y_convolve_2d_fused_body<4, 4>(p, tile); return;
+            case 32: y_convolve_2d_fused_body<8, 4>(p, tile); return;
+            case 64: y_convolve_2d_fused_body<8, 8>(p, tile); return;
+            case 128: y_convolve_2d_fused_body<16, 8>(p, tile); return;
+            default: y_convolve_2d_fused_body<32, 8>(p, tile); return;
+        }
+    }
+    y_convolve_2d_general_body(p, tile);
+}
+
+__device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, const int tile) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
@@ -550,45 +649,71 @@ __global__ void __launch_bounds__(kThreads) col_batched_kernel(const ColPass *__
 }
 
 // Deterministic final reduction of the per-block partials (layout [stat][block] of
-// float-float pairs): 1024 threads stride over the blocks with compensated TwoSum
-// accumulation for the energies and max for the norms, then a fixed-order tree
-// combines the threads.  GB300's FP64 rate is a small fraction of its FP32 rate, so
-// the compensation runs on FP32 pipes; only the final hi + lo is formed in FP64.
+// float-float pairs): the threads stride over the blocks with compensated TwoSum
+// accumulation for the energies and max for the norms, all nine statistics at once;
+// warp butterflies and one barrier combine the threads in a fixed order.  GB300's FP64
+// rate is a small fraction of its FP32 rate, so the compensation runs on FP32 pipes;
+// only the final hi + lo is formed in FP64.
 constexpr int kFinThreads = 1024;
 
-__device__ __forceinline__ void finalize_body(const float2 *__restrict__ partials, int nblocks, double *__restrict__ out) {
-    __shared__ float2 sh[kFinThreads];
+// One butterfly level: float-float sums combined in lane order (every lane ends with
+// the same bits), maxima by fmaxf.
+__device__ __forceinline__ void fin_level(float (&h)[kNumStats], float (&l)[kNumStats], int o) {
+    const bool low = (threadIdx.x & o) == 0;
+#pragma unroll
     for (int s = 0; s < kNumStats; ++s) {
-        const bool is_sum = s < 5;
-        const float2 *src = partials + (size_t)s * nblocks;
-        float h = 0.f, l = 0.f;
-        for (int b = threadIdx.x; b < nblocks; b += kFinThreads) {
-            const float2 v = src[b];
-            if (is_sum) {
-                ff_add(h, l, v.x);
-                l += v.y;
+        const float oh = __shfl_xor_sync(0xffffffffu, h[s], o);
+        const float ol = __shfl_xor_sync(0xffffffffu, l[s], o);
+        if (s < 5) {
+            float ah = low ? h[s] : oh, al = low ? l[s] : ol;
+            ff_add(ah, al, low ? oh : h[s]);
+            al += low ? ol : l[s];
+            h[s] = ah;
+            l[s] = al;
+        } else {
+            h[s] = fmaxf(h[s], oh);
+        }
+    }
+}
+
+__device__ __forceinline__ void finalize_body(const float2 *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    __shared__ float2 sh[kFinThreads / 32][kNumStats];
+    float h[kNumStats], l[kNumStats];
+#pragma unroll
+    for (int s = 0; s < kNumStats; ++s) h[s] = l[s] = 0.f;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+        for (int s = 0; s < kNumStats; ++s) {
+            const float2 v = partials[(size_t)s * nblocks + b];
+            if (s < 5) {
+                ff_add(h[s], l[s], v.x);
+                l[s] += v.y;
             } else {
-                h = fmaxf(h, v.x);
+                h[s] = fmaxf(h[s], v.x);
             }
         }
-        sh[threadIdx.x] = make_float2(h, l);
-        __syncthreads();
-        for (int w = kFinThreads / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) {
-                float2 a = sh[threadIdx.x];
-                const float2 b = sh[threadIdx.x + w];
-                if (is_sum) {
-                    ff_add(a.x, a.y, b.x);
-                    a.y += b.y;
-                } else {
-                    a.x = fmaxf(a.x, b.x);
-                }
-                sh[threadIdx.x] = a;
-            }
-            __syncthreads();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fin_level(h, l, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < kNumStats; ++s) sh[wid][s] = make_float2(h[s], l[s]);
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int s = 0; s < kNumStats; ++s) {
+            const float2 v = lane < nw ? sh[lane][s] : make_float2(0.f, 0.f);
+            h[s] = v.x;
+            l[s] = v.y;
         }
-        if (threadIdx.x == 0) out[s] = (double)sh[0].x + (double)sh[0].y;
-        __syncthreads();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) fin_level(h, l, o);
+        if (lane == 0) {
+#pragma unroll
+            for (int s = 0; s < kNumStats; ++s) out[s] = (double)h[s] + (double)l[s];
+        }
     }
 }
 
@@ -725,7 +850,10 @@ cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-size_t y_convolve_2d_smem(const Grid &g, int tx) { return 2 * sizeof(float2) * (size_t)3 * tx * skewed_len(g.py); }
+size_t y_convolve_2d_smem(const Grid &g, int tx) {
+    const size_t one = sizeof(float2) * (size_t)3 * tx * skewed_len(g.py);
+    return y2d_fused_ok(g) ? one : 2 * one;
+}
 
 cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, int kind, size_t smem, cudaStream_t s) {
     cudaError_t e = ensure_smem((const void *)col_batched_kernel, smem);
@@ -740,7 +868,7 @@ cudaError_t launch_finalize_batched(const FinDesc *fd, int nproblems, double *ou
 }
 
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s) {
-    const size_t sm = 2 * sizeof(float2) * (size_t)3 * p.tx * skewed_len(p.g.py);
+    const size_t sm = y_convolve_2d_smem(p.g, p.tx);
     cudaError_t e = ensure_smem((const void *)y_convolve_2d_kernel, sm);
     if (e != cudaSuccess) return e;
     y_convolve_2d_kernel<<<tiles(p), kThreads, sm, s>>>(p);

@@ -1543,8 +1543,17 @@ bool Engine::autotune() {
     };
     if (demag) {
         if (g.thin) {
-            tx_2d = best_tx(3, g.py, [&](int tx) { return launch_y_convolve_2d(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; },
-                            tx_2d);
+            int best = tx_2d;
+            float bt = 1e30f;
+            for (int tx : {1, 2, 4, 8, 16}) {
+                if (tx > std::max(1, g.nkx) || y_convolve_2d_smem(g, tx) > 200u * 1024u) continue;
+                const float t = time_ms([&] { return launch_y_convolve_2d(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; });
+                if (t < bt) {
+                    bt = t;
+                    best = tx;
+                }
+            }
+            tx_2d = best;
         } else if (use_yz) {
             int best = tx_z;
             float bt = 1e30f;
