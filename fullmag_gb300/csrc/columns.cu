@@ -163,49 +163,7 @@ __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
     }
 }
 
-// ---- pruned two-level transforms (power-of-two lengths N = N1 * N2) ----
-// With n = N2 n1 + n2 and k = k1 + N1 k2:
-//   X[k1 + N1 k2] = sum_n2 W_N2^{n2 k2} W_N^{n2 k1} sum_n1 x[N2 n1 + n2] W_N1^{n1 k1}.
-// Inputs vanish for n >= N/2 (n1 >= N1/2) on the forward side and only n < N/2 is kept
-// on the inverse side, so the outer N1-point passes run on half lines.
-
-// Half-input N1-point DFT of e[0..N1/2) (two N1/2-point DFTs: even and odd outputs),
-// times W_N^{n2 k1}, stored at line[sk(k1 * N2 + n2)].
-template <int N1, int N2>
-__device__ __forceinline__ void half_dft_store(float2 (&e)[N1 / 2], int n2, float2 *line, const float2 *__restrict__ tw) {
-    constexpr int H1 = N1 / 2;
-    float2 o[H1];
-    o[0] = e[0];
-#pragma unroll
-    for (int n1 = 1; n1 < H1; ++n1) o[n1] = cmul(e[n1], __ldg(tw + n1 * N2));
-    dft_small<H1>(e, false);
-    dft_small<H1>(o, false);
-#pragma unroll
-    for (int u = 0; u < H1; ++u) {
-        const int ka = 2 * u, kb = 2 * u + 1;
-        line[sk(ka * N2 + n2)] = (n2 && ka) ? cmul(e[u], __ldg(tw + n2 * ka)) : e[u];
-        line[sk(kb * N2 + n2)] = n2 ? cmul(o[u], __ldg(tw + n2 * kb)) : o[u];
-    }
-}
-
-// Half-output inverse N1-point DFT over line[sk(k1 * N2 + n2)], k1 in [0, N1): returns
-// y[n1] for n1 < N1/2 in e (two N1/2-point inverses combined with W_N1^{-n1}).
-template <int N1, int N2>
-__device__ __forceinline__ void half_idft_load(float2 (&e)[N1 / 2], int n2, const float2 *line,
-                                               const float2 *__restrict__ tw) {
-    constexpr int H1 = N1 / 2;
-    float2 o[H1];
-#pragma unroll
-    for (int u = 0; u < H1; ++u) {
-        e[u] = line[sk(2 * u * N2 + n2)];
-        o[u] = line[sk((2 * u + 1) * N2 + n2)];
-    }
-    dft_small<H1>(e, true);
-    dft_small<H1>(o, true);
-    e[0] = cadd(e[0], o[0]);
-#pragma unroll
-    for (int n1 = 1; n1 < H1; ++n1) e[n1] = cadd(e[n1], cmul(o[n1], cconj(__ldg(tw + n1 * N2))));
-}
+// ---- pruned two-level transforms (half_dft_store / half_idft_load in fft_smem.cuh) ----
 
 // X[c][z][y<ny][kx] -> Y[c][z][ky<py][kx], py = N1 * N2: half-input outer pass from
 // global memory, inner N2-point pass straight to global memory, one barrier.

@@ -56,6 +56,134 @@ __device__ __forceinline__ float warp_maxf(float v) {
     return v;
 }
 
+// ---- x-transforms in the pruned two-level form (half = px/2 = N1 * N2, a power of two) ----
+// The real x line of length px is carried as the half-length complex line
+// z[j] = s[2j] + i s[2j+1]; its nonzero samples are j < nx/2 <= half/2 and only those
+// are needed after the inverse, so both outer passes run on half lines
+// (half_dft_store / half_idft_load).
+
+__host__ __device__ __forceinline__ bool row_x_fused_ok(const Grid &g) {
+    const int h = g.half;
+    return (h == 16 || h == 32 || h == 64 || h == 128 || h == 256) && g.nx <= h;
+}
+
+// X rows (global, nkx = half + 1 values per line) -> H_d samples in
+// hd[line*lsx + sk(x/2)] (.x for even x, .y for odd x), x < nx.  Phase A (line, k1):
+// Z[k] = (a + b') + i (a - b') conj(e^{-2 pi i k/px}), a = X[k], b' = conj(X[half-k]),
+// for k = k1 + N1 k2 from global loads, inverse N2-point DFT, conjugate twiddle;
+// phase B (line, n2): half-output outer inverse.
+template <int N1, int N2>
+__device__ __forceinline__ void row_inverse_x(const RowPass &p, int rows, int row0, float2 *slots, float2 *hd) {
+    constexpr int half = N1 * N2, H1 = N1 / 2;
+    constexpr int lsx = skewed_len(half);
+    const Grid &g = p.g;
+    const int nkx = g.nkx, nrows = g.ny * g.nz, nl = rows * 3;
+    const float2 *__restrict__ tw = p.xplan.tw;
+    for (int it = threadIdx.x; it < nl * N1; it += blockDim.x) {
+        const int line = it / N1, k1 = it & (N1 - 1);
+        const int rr = line / 3, c = line - 3 * rr;
+        const float2 *X = p.x_in + ((size_t)c * nrows + row0 + rr) * nkx;
+        float2 v[N2];
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+            const int k = k1 + N1 * k2;
+            const float2 a = X[k];
+            const float2 b = cconj(X[half - k]);
+            const float2 O = cmul(csub(a, b), cconj(__ldg(p.xpost + k)));
+            v[k2] = cadd(cadd(a, b), mul_i(O));
+        }
+        dft_small<N2>(v, true);
+        float2 *sl = slots + line * lsx;
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) sl[sk(k1 * N2 + n2)] = (n2 && k1) ? cmul(v[n2], cconj(__ldg(tw + n2 * k1))) : v[n2];
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nl * N2; it += blockDim.x) {
+        const int line = it / N2, n2 = it & (N2 - 1);
+        float2 e[H1];
+        half_idft_load<N1, N2>(e, n2, slots + line * lsx, tw);
+        float2 *h = hd + line * lsx;
+#pragma unroll
+        for (int j1 = 0; j1 < H1; ++j1) h[sk(N2 * j1 + n2)] = e[j1];
+    }
+    __syncthreads();
+}
+
+// Next-stage samples s[x], x < nx, in pack[line*lsx + sk(x/2)] -> X rows (global).
+// Phase 1 (line, n2): half-input outer DFT of z[j], j < half/2 (samples x >= nx read
+// as zero); phase 2 (line, k1): inner N2-point DFTs into natural order; phase 3
+// (line, k): the real-to-half-spectrum split
+// X[k] = (Z[k] + Z'[k])/2 + e^{-2 pi i k/px} (Z[k] - Z'[k])/(2i), Z'[k] = conj(Z[half-k]).
+template <int N1, int N2>
+__device__ __forceinline__ void row_forward_x(const RowPass &p, int rows, int row0, float2 *pack, float2 *slots) {
+    constexpr int half = N1 * N2, H1 = N1 / 2;
+    constexpr int lsx = skewed_len(half);
+    const Grid &g = p.g;
+    const int nx = g.nx, nkx = g.nkx, nrows = g.ny * g.nz, nl = rows * 3;
+    const float2 *__restrict__ tw = p.xplan.tw;
+    for (int it = threadIdx.x; it < nl * N2; it += blockDim.x) {
+        const int line = it / N2, n2 = it & (N2 - 1);
+        const float2 *src = pack + line * lsx;
+        float2 e[H1];
+#pragma unroll
+        for (int j1 = 0; j1 < H1; ++j1) {
+            const int j = N2 * j1 + n2;
+            float2 v = src[sk(j)];
+            if (2 * j + 1 >= nx) {
+                v.y = 0.f;
+                if (2 * j >= nx) v.x = 0.f;
+            }
+            e[j1] = v;
+        }
+        half_dft_store<N1, N2>(e, n2, slots + line * lsx, tw);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nl * N1; it += blockDim.x) {
+        const int line = it / N1, k1 = it & (N1 - 1);
+        const float2 *sl = slots + line * lsx;
+        float2 v[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) v[n2] = sl[sk(k1 * N2 + n2)];
+        dft_small<N2>(v, false);
+        float2 *z = pack + line * lsx;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) z[sk(k1 + N1 * k2)] = v[k2];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nl * nkx; idx += blockDim.x) {
+        const int line = g.fd_nkx.div(idx);
+        const int k = idx - line * nkx;
+        const int rr = line / 3;
+        const int c = line - rr * 3;
+        const float2 *zl = pack + line * lsx;
+        const float2 a = zl[sk(k == half ? 0 : k)];
+        const float2 b = cconj(zl[sk(k == 0 ? 0 : half - k)]);
+        const float2 E = cscale(cadd(a, b), 0.5f);
+        const float2 O = div2i(csub(a, b));
+        p.x_out[((size_t)c * nrows + row0 + rr) * nkx + k] = cadd(E, cmul(__ldg(p.xpost + k), O));
+    }
+}
+
+__device__ __forceinline__ void row_inverse_x_fused(const RowPass &p, int rows, int row0, float2 *slots, float2 *hd) {
+    switch (p.g.half) {
+        case 16: row_inverse_x<4, 4>(p, rows, row0, slots, hd); break;
+        case 32: row_inverse_x<8, 4>(p, rows, row0, slots, hd); break;
+        case 64: row_inverse_x<8, 8>(p, rows, row0, slots, hd); break;
+        case 128: row_inverse_x<16, 8>(p, rows, row0, slots, hd); break;
+        default: row_inverse_x<16, 16>(p, rows, row0, slots, hd); break;
+    }
+}
+
+__device__ __forceinline__ void row_forward_x_fused(const RowPass &p, int rows, int row0, float2 *pack, float2 *slots) {
+    switch (p.g.half) {
+        case 16: row_forward_x<4, 4>(p, rows, row0, pack, slots); break;
+        case 32: row_forward_x<8, 4>(p, rows, row0, pack, slots); break;
+        case 64: row_forward_x<8, 8>(p, rows, row0, pack, slots); break;
+        case 128: row_forward_x<16, 8>(p, rows, row0, pack, slots); break;
+        default: row_forward_x<16, 16>(p, rows, row0, pack, slots); break;
+    }
+}
+
 // Body of the row pass for CTA `bid` of `nblk`; shared by the single-problem kernel
 // and the batched kernel that walks a (problem, block) work table.
 __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, const int nblk) {
@@ -75,7 +203,11 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
 
     // ---- (1) inverse x-transform of the demag spectrum ----
     float2 *hd = nullptr;
-    if (p.x_in) {
+    const bool fused_x = row_x_fused_ok(g);
+    if (p.x_in && fused_x) {
+        row_inverse_x_fused(p, rows, row0, fa, fb);
+        hd = fb;
+    } else if (p.x_in) {
         // stage the spectrum rows in smem (batched loads), then form the half-length input
         batched_copy<8>(
             rows * 3 * nkx,
@@ -100,7 +232,7 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
         __syncthreads();
         hd = fft_lines(fa, fb, rows * 3, lsx, p.xplan, true);
     }
-    float2 *pack = (hd == fb) ? fa : fb;  // free buffer for the forward transform input
+    float2 *pack = (fused_x || hd == fb) ? fa : fb;  // free buffer for the forward transform input
 
     // ---- (2)-(4) per-cell work ----
     // statistics: compensated float-float sums (TwoSum) for the energies, FP32 maxima
@@ -355,7 +487,10 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     }
 
     // ---- (5) forward x-transform of the next stage input ----
-    if (p.x_out) {
+    if (p.x_out && fused_x) {
+        __syncthreads();  // every sample packed, every H_d sample of fb read
+        row_forward_x_fused(p, rows, row0, pack, fb);
+    } else if (p.x_out) {
         // zero the padded half x in [nx, px) of every packed line
         float *pk = reinterpret_cast<float *>(pack);
         const int padw = 2 * half - nx;
