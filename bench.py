@@ -346,6 +346,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over all ranks (the slowest replica's time); x itself
+    without a process group.  `device` is "cuda" under NCCL, "cpu" under gloo."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Aggregate throughput of `world` replicas that each processed `units_per_rank`
+    units, timed by the slowest one (the path does not shard: N independent replicas)."""
+    return world * units_per_rank / seconds
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -493,12 +510,10 @@ def main():
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
     ms_per_step = ms / args.steps
-    value = world * n * args.steps / (ms * 1e-3)
+    value = whole_job_rate(world, n * args.steps, ms * 1e-3)
 
     # ---- e2e through the C ABI with host buffers ----
     if args.profile:
@@ -518,10 +533,8 @@ def main():
     m_out = be.copy_field(_abi.OBSERVABLE_M)
     t_e2e = time.perf_counter() - t0
     if dist:
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = world * n * args.steps / t_e2e
+        t_e2e = max_over_ranks(t_e2e, dist, "cuda")
+    e2e = whole_job_rate(world, n * args.steps, t_e2e)
     h2d = 24.0 * n / args.steps
     d2h = 24.0 * n / args.steps + 120.0
 
