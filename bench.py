@@ -225,20 +225,29 @@ def run_adjoint(args):
     b = torch.tensor(bmap, requires_grad=True)
     free0 = torch.cuda.mem_get_info()[0]
 
+    split = [0.0, 0.0]  # seconds in the checkpointed forward, in the backward sweep
+
     def gradient():
         b.grad = None
+        ta = time.perf_counter()
         m_t = rk4_final_state(m0, b, be, dt, nsteps)
         loss = ((m_t - tgt) ** 2).mean()
+        tb = time.perf_counter()
         loss.backward()
+        tc = time.perf_counter()
+        split[0] += tb - ta
+        split[1] += tc - tb
         return float(loss.detach())
 
     for _ in range(max(1, args.warmup)):
         loss = gradient()
     free1 = torch.cuda.mem_get_info()[0]
+    split[0] = split[1] = 0.0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         loss = gradient()
     t_grad = (time.perf_counter() - t0) / args.steps
+    t_fwd_ck, t_bwd = split[0] / args.steps, split[1] / args.steps
     g = b.grad.numpy().copy()
     # forward-only cost of the same run (CUDA-graph fixed steps), for the cost ratio
     be.upload(kw["m0"])
@@ -260,6 +269,7 @@ def run_adjoint(args):
            "e2e": {"value": 1.0 / t_grad, "unit": "gradients/s", "h2d_bytes_per_step": 24 * n + 8 * 2 * n + 24 * n,
                    "d2h_bytes_per_step": 24 * n + 24 * n + 24 * n},
            "forward_only_s": t_fwd, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+           "checkpointed_forward_s": t_fwd_ck, "backward_s": t_bwd, "backward_over_forward": t_bwd / t_fwd,
            "memory": {"checkpoints_bytes": state * ((nsteps + C - 1) // C), "segment_bytes": state * 12 * C,
                       "work_bytes": state * 12, "device_bytes_observed": int(free0 - free1),
                       "store_everything_bytes": state * 12 * nsteps},

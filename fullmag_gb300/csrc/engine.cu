@@ -324,6 +324,18 @@ struct Engine {
         kt_used = 0;
     }
 
+    bool run_row_adj(RowPass &p) {
+        if (!demag) {
+            p.x_in = nullptr;
+            p.x_out = nullptr;
+        }
+        launches += 1;
+        kt_begin(KT_ROW);
+        const cudaError_t rc = launch_row_pass_adj(p, stream);
+        kt_end();
+        return !cuda_fail("adjoint row pass", rc);
+    }
+
     bool run_row(RowPass &p) {
         if (!demag) {
             p.x_in = nullptr;
@@ -799,11 +811,14 @@ struct Engine {
     // adjoint_forward integrates n steps from the current state, keeping the state
     // every C steps (C ~ sqrt(n)).  adjoint_backward walks the segments backwards:
     // it recomputes a segment from its checkpoint while storing every stage input
-    // y0..y3, effective field H0..H3 and k1..k4, then applies the transposed step
-    // (adjoint.cu) in reverse, accumulating d loss / d field map in float-float.
+    // y0..y3, effective field H0..H3 and k1..k4, then applies the transposed step in
+    // reverse (equations in adjoint.cu): per stage one row pass computes the local VJP
+    // and forward-transforms lambda_H, the column passes convolve it, and a second row
+    // pass adds H_lin(lambda_H) and pushes the result through the stage normalisation.
+    // d loss / d field map accumulates in float-float.
     float *adj_ckpt = nullptr;  // [n_ckpt][3n]
     float *adj_seg = nullptr;   // [C][12][3n]: y0 y1 y2 y3 H0 H1 H2 H3 k1 k2 k3 k4
-    float *adj_work = nullptr;  // [12][3n]: lam_next lam_y0 lk1 lk2 lk3 lk4 lam_h lam_m lin g_hi g_lo spare
+    float *adj_work = nullptr;  // [12][3n]: lam_next lam_y0 lk1 lk2 lk3 lk4 lam_h[0] lam_m lam_h[1] g_hi g_lo spare
     uint64_t adj_nsteps = 0;
     uint32_t adj_C = 0;
     size_t adj_nck = 0;
@@ -895,20 +910,6 @@ struct Engine {
         return eval_state(false) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
     }
 
-    // lin <- H_lin(v): exchange stencil + Newell convolution applied to an arbitrary field.
-    bool apply_linear(const float *v, float *lin) {
-        if (!pass_forward(v)) return false;
-        RowPass p = row_base();
-        p.mat.has_ext = 0;
-        p.mat.has_uni = 0;
-        p.mat.has_cub = 0;
-        p.hmap = nullptr;
-        p.x_in = X;
-        p.m_in = v;
-        p.h_eff_out = lin;
-        return run_row(p);
-    }
-
     int adjoint_backward(const double *lam_T, double *grad_out, double *lam0_out) {
         if (!adj_ckpt) {
             last_error = "adjoint_backward needs a preceding adjoint_forward";
@@ -927,7 +928,7 @@ struct Engine {
         float *W[12];
         for (int i = 0; i < 12; ++i) W[i] = adj_work + i * v3;
         float *lam_next = W[0], *lam_y0 = W[1], *lk[5] = {nullptr, W[2], W[3], W[4], W[5]};
-        float *lam_h = W[6], *lam_m = W[7], *lin = W[8], *g_hi = W[9], *g_lo = W[10], *spare = W[11];
+        float *lam_hb[2] = {W[6], W[8]}, *lam_m = W[7], *g_hi = W[9], *g_lo = W[10], *spare = W[11];
         if (!ensure_staging()) return FULLMAG_FDM_ERR_CUDA;
         if (cuda_fail("cudaMemcpy(lambda)", cudaMemcpyAsync(staging, lam_T, sizeof(double) * v3, cudaMemcpyHostToDevice, stream)))
             return FULLMAG_FDM_ERR_CUDA;
@@ -954,28 +955,43 @@ struct Engine {
                 AdjFinal af{n, lam_next, slot(t, 0), slot(t, 8), slot(t, 9), slot(t, 10), slot(t, 11), hf,
                             lam_y0, lk[1], lk[2], lk[3], lk[4]};
                 ok = !cuda_fail("adjoint final", launch_adj_final(af, stream));
-                for (int s = 3; s >= 0 && ok; --s) {
-                    AdjLocal al{};
-                    al.n = n;
-                    al.m = slot(t, s);
-                    al.H = slot(t, 4 + s);
-                    al.w = lk[s + 1];
-                    al.lam_h = lam_h;
-                    al.lam_m = lam_m;
-                    al.g_hi = g_hi;
-                    al.g_lo = g_lo;
-                    al.gbar = mat.gbar;
-                    al.alpha = mat.alpha;
-                    al.prec = mat.prec;
-                    al.has_uni = mat.has_uni;
-                    al.ku1c = mat.ku1c;
-                    al.ku2c = mat.ku2c;
-                    for (int c = 0; c < 3; ++c) al.u[c] = mat.u[c];
-                    ok = !cuda_fail("adjoint local", launch_adj_local(al, stream)) && apply_linear(lam_h, lin);
-                    if (!ok) break;
-                    AdjStage as{n, lam_m, lin, slot(t, 0), s >= 1 ? slot(t, 8 + s - 1) : nullptr, cs[s] * hf, lam_y0,
-                                s >= 1 ? lk[s] : nullptr};
-                    ok = !cuda_fail("adjoint stage", launch_adj_stage(as, stream));
+                // Five row passes per step, like a forward step: the local VJP of stage s - 1
+                // (bit 1) shares a pass with the stage-s update after H_lin (bit 2), because the
+                // cotangent of k_s it needs is complete at each cell once bit 2 has run there.
+                // lambda_H alternates between two buffers (the stencil reads its neighbours).
+                int lh = 0;
+                for (int s = 4; s >= 0 && ok; --s) {
+                    RowPass b = row_base();
+                    b.mat.has_ext = 0;
+                    b.mat.has_uni = 0;
+                    b.mat.has_cub = 0;
+                    b.hmap = nullptr;
+                    b.adj_uni = mat.has_uni;
+                    b.adj_mode = 0;
+                    if (s <= 3) {  // bit 2: update of stage s from H_lin(lambda_H of stage s)
+                        b.adj_mode |= 2;
+                        b.x_in = X;
+                        b.m_in = lam_hb[lh];
+                        b.adj_lam_m = lam_m;
+                        b.adj_y0 = slot(t, 0);
+                        b.adj_k = s >= 1 ? slot(t, 8 + s - 1) : nullptr;
+                        b.adj_ch = cs[s] * hf;
+                        b.adj_lam_y0 = lam_y0;
+                        b.adj_lam_k = s >= 1 ? lk[s] : nullptr;
+                    }
+                    if (s >= 1) {  // bit 1: local VJP of stage s - 1, forward x-transform of its lambda_H
+                        b.adj_mode |= 1;
+                        b.adj_m = slot(t, s - 1);
+                        b.adj_H = slot(t, 4 + s - 1);
+                        b.adj_w = lk[s];
+                        b.adj_lam_h = lam_hb[1 - lh];
+                        b.adj_lam_m = lam_m;
+                        b.adj_g_hi = g_hi;
+                        b.adj_g_lo = g_lo;
+                        b.x_out = X;
+                    }
+                    ok = run_row_adj(b) && (s == 0 || run_columns());
+                    lh = 1 - lh;
                 }
                 std::swap(lam_next, lam_y0);
             }

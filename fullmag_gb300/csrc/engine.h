@@ -99,6 +99,21 @@ struct RowPass {
     // observables
     float *h_ex_out, *h_d_out, *h_eff_out;  // NULL: not written
     int rows;                // rows per CTA
+    // adjoint passes (launch_row_pass_adj only; see adjoint.cu for the equations); adj_mode
+    // is a bit set, bit 2 runs before bit 1 at each cell:
+    //   bit 2, after H_lin(lambda_H) (m_in = lambda_H, local terms off): lambda_y = adj_lam_m
+    //          + H_lin; through y_s = N(y0 + ch k) into adj_lam_y0 and adj_lam_k (adj_k NULL:
+    //          stage 0, lambda_y added to adj_lam_y0)
+    //   bit 1, local VJP of k = f(m, H) with cotangent w (adj_uni: uniaxial Jacobian term):
+    //          lambda_H -> adj_lam_h and the forward x-transform, lambda_m -> adj_lam_m
+    //          (in place after bit 2 read it), lambda_H added to (adj_g_hi, adj_g_lo)
+    int adj_mode;
+    int adj_uni;
+    const float *adj_m, *adj_H, *adj_w;
+    float *adj_lam_h, *adj_lam_m, *adj_g_hi, *adj_g_lo;
+    const float *adj_y0, *adj_k;
+    float adj_ch;
+    float *adj_lam_y0, *adj_lam_k;
 };
 
 struct ColPass {
@@ -116,6 +131,7 @@ struct ColPass {
 // Launchers (kernels.cu)
 size_t row_pass_smem(const RowPass &p);
 cudaError_t launch_row_pass(const RowPass &p, cudaStream_t s);
+cudaError_t launch_row_pass_adj(const RowPass &p, cudaStream_t s);  // adjoint modes 1 and 2
 cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s);     // X -> Y  (3-D)
 cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s);    // Y -> Y  (3-D, z FFT, multiply, inverse)
 cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (3-D)
@@ -126,31 +142,14 @@ size_t z_convolve_smem(const Grid &g, int tx);
 size_t y_pass_smem(const Grid &g, int tx);
 size_t y_convolve_2d_smem(const Grid &g, int tx);
 
-// Adjoint (reverse-mode RK4) element-wise passes (adjoint.cu); all fields SoA.
-struct AdjLocal {
-    long long n;
-    const float *m, *H, *w;     // stage input, its effective field, cotangent of k
-    float *lam_h, *lam_m;       // outputs
-    float *g_hi, *g_lo;         // float-float accumulator of d loss / d field map (NULL: none)
-    float gbar, alpha, prec;
-    int has_uni;
-    float ku1c, ku2c, u[3];
-};
-struct AdjStage {
-    long long n;
-    const float *lam_m, *lin;   // local VJP and H_lin(lambda_H)
-    const float *y0, *k;        // k == NULL: stage 0 (no normalisation to undo)
-    float ch;                   // c * h of y_s = N(y0 + c h k_s)
-    float *lam_y0, *lam_k;      // accumulators
-};
+// Adjoint (reverse-mode RK4): the final-combination pass (adjoint.cu); all fields SoA.
+// The local VJP and the stage update are the row pass's adjoint modes.
 struct AdjFinal {
     long long n;
     const float *lam_next, *y0, *k1, *k2, *k3, *k4;
     float h;
     float *lam_y0, *lk1, *lk2, *lk3, *lk4;
 };
-cudaError_t launch_adj_local(const AdjLocal &a, cudaStream_t s);
-cudaError_t launch_adj_stage(const AdjStage &a, cudaStream_t s);
 cudaError_t launch_adj_final(const AdjFinal &a, cudaStream_t s);
 
 // Batched launches: one grid covering many problems through a (problem, block) table.

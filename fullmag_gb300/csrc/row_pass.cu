@@ -184,8 +184,26 @@ __device__ __forceinline__ void row_forward_x_fused(const RowPass &p, int rows, 
     }
 }
 
+// Adjoint helpers (the element-wise equations of adjoint.cu, inlined into the row pass)
+struct A3 {
+    float x, y, z;
+};
+__device__ __forceinline__ A3 a3_ld(const float *a, long long n, long long i) { return {a[i], a[n + i], a[2 * n + i]}; }
+__device__ __forceinline__ void a3_st(float *a, long long n, long long i, A3 v) {
+    a[i] = v.x;
+    a[n + i] = v.y;
+    a[2 * n + i] = v.z;
+}
+__device__ __forceinline__ A3 a3_cross(A3 a, A3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float a3_dot(A3 a, A3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ A3 a3_axpy(float s, A3 a, A3 b) { return {s * a.x + b.x, s * a.y + b.y, s * a.z + b.z}; }
+
 // Body of the row pass for CTA `bid` of `nblk`; shared by the single-problem kernel
-// and the batched kernel that walks a (problem, block) work table.
+// and the batched kernel that walks a (problem, block) work table.  ADJ compiles the
+// adjoint modes (a separate kernel, so the forward kernel's registers are unaffected).
+template <bool ADJ>
 __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, const int nblk) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
@@ -411,10 +429,63 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
                 p.h_d_out[n + i] = dy_;
                 p.h_d_out[2 * n + i] = dz_;
             }
+            if constexpr (ADJ) {
+                if (p.adj_mode & 2) {
+                    // lambda_y = lambda_m + H_lin(lambda_H), then through the stage normalisation
+                    const A3 ly = a3_axpy(1.f, a3_ld(p.adj_lam_m, n, i), A3{hx, hy, hz});
+                    const A3 ly0 = a3_ld(p.adj_lam_y0, n, i);
+                    if (p.adj_k) {
+                        const A3 v = a3_axpy(p.adj_ch, a3_ld(p.adj_k, n, i), a3_ld(p.adj_y0, n, i));
+                        const float nn = sqrtf(a3_dot(v, v));
+                        A3 mu{0.f, 0.f, 0.f};
+                        if (nn > 0.f) {
+                            const float inv = 1.0f / nn;
+                            const A3 u{v.x * inv, v.y * inv, v.z * inv};
+                            const A3 t = a3_axpy(-a3_dot(u, ly), u, ly);
+                            mu = {t.x * inv, t.y * inv, t.z * inv};
+                        }
+                        a3_st(p.adj_lam_y0, n, i, a3_axpy(1.f, mu, ly0));
+                        a3_st(p.adj_lam_k, n, i, a3_axpy(p.adj_ch, mu, a3_ld(p.adj_lam_k, n, i)));
+                    } else {
+                        a3_st(p.adj_lam_y0, n, i, a3_axpy(1.f, ly, ly0));
+                    }
+                }
+            }
         }
         // ---- (4) next stage input ----
         float nxv = 0.f, nyv = 0.f, nzv = 0.f;
-        if (p.m0) {
+        bool adj_local = false;
+        if constexpr (ADJ) adj_local = (p.adj_mode & 1) != 0;
+        if (adj_local) {
+            if constexpr (ADJ) {
+                // local VJP of k = -gbar [prec m x H + alpha m x (m x H)] with cotangent w
+                const A3 m = a3_ld(p.adj_m, n, i), H = a3_ld(p.adj_H, n, i), w = a3_ld(p.adj_w, n, i);
+                const A3 q = a3_axpy(M.alpha, a3_cross(w, m), A3{M.prec * w.x, M.prec * w.y, M.prec * w.z});
+                const A3 pv = a3_cross(m, H);
+                const A3 t = a3_axpy(M.alpha, a3_cross(pv, w), a3_cross(H, q));
+                A3 lm{-M.gbar * t.x, -M.gbar * t.y, -M.gbar * t.z};
+                const A3 qm = a3_cross(q, m);
+                const A3 lh{-M.gbar * qm.x, -M.gbar * qm.y, -M.gbar * qm.z};
+                if (p.adj_uni) {
+                    const A3 u{M.u[0], M.u[1], M.u[2]};
+                    const float mu = a3_dot(m, u);
+                    lm = a3_axpy((M.ku1c + 3.0f * M.ku2c * mu * mu) * a3_dot(u, lh), u, lm);
+                }
+                a3_st(p.adj_lam_m, n, i, lm);
+                a3_st(p.adj_lam_h, n, i, lh);
+                const float lv[3] = {lh.x, lh.y, lh.z};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float hi = p.adj_g_hi[c * n + i], lo = p.adj_g_lo[c * n + i];
+                    ff_add(hi, lo, lv[c]);
+                    p.adj_g_hi[c * n + i] = hi;
+                    p.adj_g_lo[c * n + i] = lo;
+                }
+                nxv = lh.x;
+                nyv = lh.y;
+                nzv = lh.z;
+            }
+        } else if (p.m0) {
             float sx = 0.f, sy = 0.f, sz = 0.f;
             for (int t = 0; t < p.n_comb; ++t) {
                 const float *kk = p.comb_k[t];
@@ -517,7 +588,8 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     }
 }
 
-__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) { row_pass_body(p, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) { row_pass_body<false>(p, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kThreads) row_pass_adj_kernel(const RowPass p) { row_pass_body<true>(p, blockIdx.x, gridDim.x); }
 
 // One launch for many problems: work[blockIdx.x] = (problem, block within problem).
 __global__ void __launch_bounds__(kThreads) row_pass_batched_kernel(const RowPass *__restrict__ ps,
@@ -531,7 +603,7 @@ __global__ void __launch_bounds__(kThreads) row_pass_batched_kernel(const RowPas
         reinterpret_cast<int *>(desc)[i] = src[i];
     __syncthreads();
     const RowPass &p = *reinterpret_cast<const RowPass *>(desc);
-    row_pass_body(p, w.y, (p.g.ny * p.g.nz + p.rows - 1) / p.rows);
+    row_pass_body<false>(p, w.y, (p.g.ny * p.g.nz + p.rows - 1) / p.rows);
 }
 
 }  // namespace
@@ -570,6 +642,14 @@ cudaError_t launch_row_pass(const RowPass &p, cudaStream_t s) {
     cudaError_t e = ensure_smem((const void *)row_pass_kernel, sm);
     if (e != cudaSuccess) return e;
     row_pass_kernel<<<row_pass_blocks(p), kThreads, sm, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_pass_adj(const RowPass &p, cudaStream_t s) {
+    const size_t sm = row_pass_smem(p);
+    cudaError_t e = ensure_smem((const void *)row_pass_adj_kernel, sm);
+    if (e != cudaSuccess) return e;
+    row_pass_adj_kernel<<<row_pass_blocks(p), kThreads, sm, s>>>(p);
     return cudaGetLastError();
 }
 
