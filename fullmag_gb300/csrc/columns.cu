@@ -352,12 +352,159 @@ __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve
     }
 }
 
+// Register-resident z convolution of one (kx column, ky) for pz <= 8: forward z DFT of
+// the nz physical planes (zero above), -N(k) multiply, inverse DFT, planes z < nz
+// written back.  Component c, plane z of the column sits at line[(c*nz + z)*lstride].
+template <int PZ>
+__device__ __forceinline__ void z_small_convolve(float2 *line, size_t lstride, int nz, const float *__restrict__ kern,
+                                                 size_t kc, int nky, int nkx, int ky, int py, int kx) {
+    float2 v[3][PZ];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int z = 0; z < PZ; ++z) v[c][z] = z < nz ? line[(c * nz + z) * lstride] : make_float2(0.f, 0.f);
+        dft_small<PZ>(v[c], false);
+    }
+    int kym;
+    float sy;
+    kernel_mirror(ky, py, kym, sy);
+#pragma unroll
+    for (int kz = 0; kz < PZ; ++kz) {
+        int kzm;
+        float sz;
+        kernel_mirror(kz, PZ, kzm, sz);
+        const float *K = kern + ((size_t)kzm * nky + kym) * nkx + kx;
+        const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
+        const float kxy = sy * __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz = sy * sz * __ldg(K + 5 * kc);
+        const float2 mx = v[0][kz], my = v[1][kz], mz = v[2][kz];
+        v[0][kz] = make_float2(-(kxx * mx.x + kxy * my.x + kxz * mz.x), -(kxx * mx.y + kxy * my.y + kxz * mz.y));
+        v[1][kz] = make_float2(-(kxy * mx.x + kyy * my.x + kyz * mz.x), -(kxy * mx.y + kyy * my.y + kyz * mz.y));
+        v[2][kz] = make_float2(-(kxz * mx.x + kyz * my.x + kzz * mz.x), -(kxz * mx.y + kyz * my.y + kzz * mz.y));
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        dft_small<PZ>(v[c], true);
+#pragma unroll
+        for (int z = 0; z < PZ; ++z)
+            if (z < nz) line[(c * nz + z) * lstride] = v[c][z];
+    }
+}
+
+__host__ __device__ __forceinline__ bool yz_fused_ok(const Grid &g) {
+    const int py = g.py, pz = g.pz;
+    return (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py &&
+           (pz == 2 || pz == 4 || pz == 8) && 2 * g.nz <= pz;
+}
+
+// Small 3-D grids, py = N1 * N2 and pz <= 8: the pruned two-level y transforms of
+// the nz physical planes around a register-resident z convolution.  Lines (c, z, col)
+// at L = (c*nz + z)*tx + col in two buffers: A holds the outer-pass slots, B the
+// natural-order y spectrum.  Phases: outer half-input DFT from global memory -> A;
+// inner DFTs A -> B; per (col, ky) z convolution in B; inner inverse B -> A; outer
+// half-output inverse A -> global memory.
+template <int N1, int N2>
+__device__ __forceinline__ void yz_convolve_fused_body(const ColPass &p, const int tile) {
+    constexpr int N = N1 * N2, H1 = N1 / 2;
+    constexpr int ls = skewed_len(N);
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid &g = p.g;
+    const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
+    const int nz = g.nz, nl = 3 * nz * tx;
+    float2 *A = reinterpret_cast<float2 *>(smem);
+    float2 *B = A + (size_t)nl * ls;
+    const size_t zstride = (size_t)g.ny * g.nkx, cstride = (size_t)nz * zstride;
+    const float2 *__restrict__ tw = p.plan.tw;
+    for (int it = threadIdx.x; it < nl * N2; it += blockDim.x) {
+        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+        const int n2 = rest & (N2 - 1), cz = rest / N2;  // cz = c*nz + z
+        const float2 *src = p.in + cz * zstride + kx0 + col;
+        const bool okc = col < ncol;
+        float2 e[H1];
+#pragma unroll
+        for (int y1 = 0; y1 < H1; ++y1) {
+            const int y = N2 * y1 + n2;
+            e[y1] = (okc && y < g.ny) ? src[(size_t)y * g.nkx] : make_float2(0.f, 0.f);
+        }
+        half_dft_store<N1, N2>(e, n2, A + (cz * tx + col) * ls, tw);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nl * N1; it += blockDim.x) {
+        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+        const int k1 = rest & (N1 - 1), cz = rest / N1;
+        const float2 *sl = A + (cz * tx + col) * ls;
+        float2 v[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) v[n2] = sl[sk(k1 * N2 + n2)];
+        dft_small<N2>(v, false);
+        float2 *bl = B + (cz * tx + col) * ls;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) bl[sk(k1 + N1 * k2)] = v[k2];
+    }
+    __syncthreads();
+    const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
+    for (int it = threadIdx.x; it < N * tx; it += blockDim.x) {
+        const int ky = p.fd_tx.div(it), col = it - ky * tx;
+        const int kx = min(kx0 + col, g.nkx - 1);
+        float2 *line = B + (size_t)col * ls + sk(ky);
+        const size_t lstride = (size_t)tx * ls;
+        if (g.pz == 2) z_small_convolve<2>(line, lstride, nz, p.kern, kc, g.nky, g.nkx, ky, N, kx);
+        else if (g.pz == 4) z_small_convolve<4>(line, lstride, nz, p.kern, kc, g.nky, g.nkx, ky, N, kx);
+        else z_small_convolve<8>(line, lstride, nz, p.kern, kc, g.nky, g.nkx, ky, N, kx);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nl * N1; it += blockDim.x) {
+        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+        const int k1 = rest & (N1 - 1), cz = rest / N1;
+        const float2 *bl = B + (cz * tx + col) * ls;
+        float2 v[N2];
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) v[k2] = bl[sk(k1 + N1 * k2)];
+        dft_small<N2>(v, true);
+        float2 *sl = A + (cz * tx + col) * ls;
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) sl[sk(k1 * N2 + n2)] = (n2 && k1) ? cmul(v[n2], cconj(__ldg(tw + n2 * k1))) : v[n2];
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nl * N2; it += blockDim.x) {
+        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+        const int n2 = rest & (N2 - 1), cz = rest / N2;
+        float2 e[H1];
+        half_idft_load<N1, N2>(e, n2, A + (cz * tx + col) * ls, tw);
+        if (col < ncol) {
+            float2 *dst = p.out + cz * zstride + kx0 + col;
+#pragma unroll
+            for (int y1 = 0; y1 < H1; ++y1) {
+                const int y = N2 * y1 + n2;
+                if (y < g.ny) dst[(size_t)y * g.nkx] = e[y1];
+            }
+        }
+    }
+    (void)cstride;
+}
+
+__device__ __forceinline__ void yz_convolve_general_body(const ColPass &p, const int tile);
+
+__device__ __forceinline__ void yz_convolve_fused_dispatch(const ColPass &p, const int tile) {
+    switch (p.g.py) {
+        case 16: yz_convolve_fused_body<4, 4>(p, tile); return;
+        case 32: yz_convolve_fused_body<8, 4>(p, tile); return;
+        case 64: yz_convolve_fused_body<8, 8>(p, tile); return;
+        case 128: yz_convolve_fused_body<16, 8>(p, tile); return;
+        default: yz_convolve_fused_body<16, 16>(p, tile); return;
+    }
+}
+
+__device__ __forceinline__ void yz_convolve_body(const ColPass &p, const int tile) {
+    if (yz_fused_ok(p.g)) yz_convolve_fused_dispatch(p, tile);
+    else yz_convolve_general_body(p, tile);
+}
+
 // 3-D grids whose (y, z) plane fits in shared memory: forward y-transform of the nz
 // physical planes, in-smem transpose, forward z, multiply, inverse z, transpose back,
 // inverse y -- X -> X in place, one pass instead of three and no Y round trip.
 // Lines: y-lines (c, col, z) at ((c*tx + col)*nz + z), z-lines (c, col, ky) at
 // ((c*tx + col)*py + ky); both layouts share two ping-pong buffers of `half_buf`.
-__device__ __forceinline__ void yz_convolve_body(const ColPass &p, const int tile) {
+__device__ __forceinline__ void yz_convolve_general_body(const ColPass &p, const int tile) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const FftPlan &plan_z = p.plan2;
@@ -523,17 +670,19 @@ __host__ __device__ __forceinline__ bool y2d_fused_ok(const Grid &g) {
 
 __device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, const int tile);
 
-__device__ __forceinline__ void y_convolve_2d_body(const ColPass &p, const int tile) {
-    if (y2d_fused_ok(p.g)) {
-        switch (p.g.py) {
-            case 16: y_convolve_2d_fused_body<4, 4>(p, tile); return;
-            case 32: y_convolve_2d_fused_body<8, 4>(p, tile); return;
-            case 64: y_convolve_2d_fused_body<8, 8>(p, tile); return;
-            case 128: y_convolve_2d_fused_body<16, 8>(p, tile); return;
-            default: y_convolve_2d_fused_body<32, 8>(p, tile); return;
-        }
+__device__ __forceinline__ void y_convolve_2d_fused_dispatch(const ColPass &p, const int tile) {
+    switch (p.g.py) {
+        case 16: y_convolve_2d_fused_body<4, 4>(p, tile); return;
+        case 32: y_convolve_2d_fused_body<8, 4>(p, tile); return;
+        case 64: y_convolve_2d_fused_body<8, 8>(p, tile); return;
+        case 128: y_convolve_2d_fused_body<16, 8>(p, tile); return;
+        default: y_convolve_2d_fused_body<32, 8>(p, tile); return;
     }
-    y_convolve_2d_general_body(p, tile);
+}
+
+__device__ __forceinline__ void y_convolve_2d_body(const ColPass &p, const int tile) {
+    if (y2d_fused_ok(p.g)) y_convolve_2d_fused_dispatch(p, tile);
+    else y_convolve_2d_general_body(p, tile);
 }
 
 __device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, const int tile) {
@@ -591,10 +740,12 @@ __device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, con
 __global__ void __launch_bounds__(kThreads) yz_convolve_kernel(const ColPass p) { yz_convolve_body(p, blockIdx.x); }
 __global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p) { y_convolve_2d_body(p, blockIdx.x); }
 
-// One launch for many problems: work[blockIdx.x] = (problem, kx tile); kind 0 thin
-// film, 1 fused y+z.
-__global__ void __launch_bounds__(kThreads) col_batched_kernel(const ColPass *__restrict__ ps,
-                                                               const int2 *__restrict__ work, int kind) {
+// One launch for many problems: work[blockIdx.x] = (problem, kx tile).  KIND (see
+// col_batched_kind): 0 thin film pruned, 1 fused y+z pruned, 2 thin film general,
+// 3 fused y+z general -- one kernel per kind, so each gets its own register allocation.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, KIND < 2 ? 2 : 4) col_batched_kernel(const ColPass *__restrict__ ps,
+                                                               const int2 *__restrict__ work) {
     __shared__ __align__(16) unsigned char desc[sizeof(ColPass)];  // descriptor staged once per CTA
     const int2 w = work[blockIdx.x];
     const int *src = reinterpret_cast<const int *>(ps + w.x);
@@ -602,8 +753,10 @@ __global__ void __launch_bounds__(kThreads) col_batched_kernel(const ColPass *__
         reinterpret_cast<int *>(desc)[i] = src[i];
     __syncthreads();
     const ColPass &p = *reinterpret_cast<const ColPass *>(desc);
-    if (kind == 0) y_convolve_2d_body(p, w.y);
-    else yz_convolve_body(p, w.y);
+    if constexpr (KIND == 0) y_convolve_2d_fused_dispatch(p, w.y);
+    else if constexpr (KIND == 1) yz_convolve_fused_dispatch(p, w.y);
+    else if constexpr (KIND == 2) y_convolve_2d_general_body(p, w.y);
+    else yz_convolve_general_body(p, w.y);
 }
 
 // Deterministic final reduction of the per-block partials (layout [stat][block] of
@@ -796,6 +949,7 @@ cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
 
 size_t yz_convolve_smem(const Grid &g, int tx) {
     const size_t a = (size_t)3 * tx * g.nz * skewed_len(g.py);
+    if (yz_fused_ok(g)) return 2 * sizeof(float2) * a;
     const size_t b = (size_t)3 * tx * g.py * skewed_len(g.pz);
     return 2 * sizeof(float2) * (a > b ? a : b);
 }
@@ -808,15 +962,28 @@ cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+int col_batched_kind(const Grid &g) {
+    if (g.thin) return y2d_fused_ok(g) ? 0 : 2;
+    return yz_fused_ok(g) ? 1 : 3;
+}
+
 size_t y_convolve_2d_smem(const Grid &g, int tx) {
     const size_t one = sizeof(float2) * (size_t)3 * tx * skewed_len(g.py);
     return y2d_fused_ok(g) ? one : 2 * one;
 }
 
 cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, int kind, size_t smem, cudaStream_t s) {
-    cudaError_t e = ensure_smem((const void *)col_batched_kernel, smem);
+    const void *fns[4] = {(const void *)col_batched_kernel<0>, (const void *)col_batched_kernel<1>,
+                          (const void *)col_batched_kernel<2>, (const void *)col_batched_kernel<3>};
+    if (kind < 0 || kind > 3) return cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem(fns[kind], smem);
     if (e != cudaSuccess) return e;
-    col_batched_kernel<<<nwork, kThreads, smem, s>>>(ps, work, kind);
+    switch (kind) {
+        case 0: col_batched_kernel<0><<<nwork, kThreads, smem, s>>>(ps, work); break;
+        case 1: col_batched_kernel<1><<<nwork, kThreads, smem, s>>>(ps, work); break;
+        case 2: col_batched_kernel<2><<<nwork, kThreads, smem, s>>>(ps, work); break;
+        default: col_batched_kernel<3><<<nwork, kThreads, smem, s>>>(ps, work); break;
+    }
     return cudaGetLastError();
 }
 

@@ -262,7 +262,7 @@ struct Engine {
     }
 
     // Recording mode (batched execution): passes are appended as descriptors instead
-    // of being launched; column passes record their kind (0 thin film, 1 fused y+z).
+    // of being launched; column passes record their batched kind (col_batched_kind).
     std::vector<RowPass> *rec_rows = nullptr;
     std::vector<int> *rec_cols = nullptr;
 
@@ -379,7 +379,7 @@ struct Engine {
                 last_error = "grid too large for the batched passes";
                 return false;
             }
-            rec_cols->push_back(g.thin ? 0 : 1);
+            rec_cols->push_back(col_batched_kind(g));
             return true;
         }
         cudaError_t rc;
@@ -1038,6 +1038,33 @@ struct Engine {
     // to S[1]; an accepted proposal is committed on the device at the start of the
     // next round (S0 <- S1, K0 <- K6), so the recorded pass descriptors never change
     // and every round of the batch replays one CUDA graph.
+    // Tiles for batched rounds.  The autotuner picks tiles that make one small grid fill
+    // the GPU (many thin CTAs); in a batched round the problems fill the GPU together, so
+    // each CTA takes more work instead: row passes of at least ~512 cells, and the widest
+    // kx tile of the fused column pass within 64 KB of shared memory.
+    void batch_tiling() {
+        const int nrows = g.ny * g.nz;
+        int r = 1;
+        while (r < 16 && r * g.nx < 512 && 2 * r <= nrows) {
+            RowPass t = row_base();
+            t.rows = 2 * r;
+            t.x_in = demag ? X : nullptr;
+            t.x_out = demag ? X : nullptr;
+            if (row_pass_smem(t) > 64u * 1024u) break;
+            r *= 2;
+        }
+        if (r > row_rows) {
+            row_rows = r;
+            row_blocks = (nrows + row_rows - 1) / row_rows;
+        }
+        if (!demag) return;
+        int tx = 1;
+        auto smem = [&](int t) { return g.thin ? y_convolve_2d_smem(g, t) : yz_convolve_smem(g, t); };
+        while (tx < 16 && 2 * tx <= g.nkx && smem(2 * tx) <= 64u * 1024u) tx *= 2;
+        if (g.thin) tx_2d = std::max(tx_2d, tx);
+        else if (use_yz) tx_z = std::max(tx_z, tx);
+    }
+
     bool batch_prepare() {
         if (cur != 0) {  // bring the committed state to S[0]
             if (cuda_fail("state copy", cudaMemcpyAsync(S[0], S[1], sizeof(float) * 3 * (size_t)g.n,
@@ -2162,11 +2189,12 @@ struct FdmBatch {
             return b <= 24u * 1024u ? 0 : b <= 48u * 1024u ? 1 : b <= 96u * 1024u ? 2 : b <= 150u * 1024u ? 3 : 4;
         };
         std::vector<RowPass> rows[7];
-        std::vector<ColPass> cols[2 * NC];
-        std::vector<int2> row_work[NC], col_work[2 * NC];
+        constexpr int NK = 4;  // column kernel kinds (col_batched_kind)
+        std::vector<ColPass> cols[NK * NC];
+        std::vector<int2> row_work[NC], col_work[NK * NC];
         std::vector<FinDesc> fin(n);
         std::vector<CommitDesc> com(n);
-        size_t row_smem[NC] = {0, 0, 0, 0, 0}, col_smem[2 * NC] = {};
+        size_t row_smem[NC] = {0, 0, 0, 0, 0}, col_smem[NK * NC] = {};
         std::vector<RowPass> rec;
         std::vector<int> kinds;
         for (int k = 0; k < n; ++k) {
@@ -2187,8 +2215,9 @@ struct FdmBatch {
             for (int b = 0; b < nb; ++b) row_work[rb].push_back(make_int2(k, b));
             if (e->demag) {
                 const int kind = kinds[0];
-                const int tx = kind == 0 ? e->tx_2d : e->tx_z;
-                const size_t cs = kind == 0 ? y_convolve_2d_smem(e->g, tx) : yz_convolve_smem(e->g, tx);
+                const bool thin = e->g.thin != 0;
+                const int tx = thin ? e->tx_2d : e->tx_z;
+                const size_t cs = thin ? y_convolve_2d_smem(e->g, tx) : yz_convolve_smem(e->g, tx);
                 const int cg = kind * NC + smem_class(cs);
                 ColPass c = e->col_pass(e->plan_y, tx, e->X, e->X);
                 const int idx = (int)cols[cg].size();
@@ -2203,11 +2232,11 @@ struct FdmBatch {
         // one device blob for every descriptor array
         size_t off = 0;
         auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-        size_t o_rows[7], o_cols[2 * NC], o_rw[NC], o_cw[2 * NC], o_fin, o_com;
+        size_t o_rows[7], o_cols[NK * NC], o_rw[NC], o_cw[NK * NC], o_fin, o_com;
         for (int s = 0; s < 7; ++s) { o_rows[s] = off; off += al(sizeof(RowPass) * rows[s].size()); }
-        for (int k = 0; k < 2 * NC; ++k) { o_cols[k] = off; off += al(sizeof(ColPass) * cols[k].size()); }
+        for (int k = 0; k < NK * NC; ++k) { o_cols[k] = off; off += al(sizeof(ColPass) * cols[k].size()); }
         for (int k = 0; k < NC; ++k) { o_rw[k] = off; off += al(sizeof(int2) * row_work[k].size()); }
-        for (int k = 0; k < 2 * NC; ++k) { o_cw[k] = off; off += al(sizeof(int2) * col_work[k].size()); }
+        for (int k = 0; k < NK * NC; ++k) { o_cw[k] = off; off += al(sizeof(int2) * col_work[k].size()); }
         o_fin = off; off += al(sizeof(FinDesc) * n);
         o_com = off; off += al(sizeof(CommitDesc) * n);
         if (cudaMalloc(&round.d_blob, off) != cudaSuccess) {
@@ -2217,9 +2246,9 @@ struct FdmBatch {
         char *blob = (char *)round.d_blob;
         std::vector<char> hb(off);
         for (int s = 0; s < 7; ++s) memcpy(hb.data() + o_rows[s], rows[s].data(), sizeof(RowPass) * rows[s].size());
-        for (int k = 0; k < 2 * NC; ++k) memcpy(hb.data() + o_cols[k], cols[k].data(), sizeof(ColPass) * cols[k].size());
+        for (int k = 0; k < NK * NC; ++k) memcpy(hb.data() + o_cols[k], cols[k].data(), sizeof(ColPass) * cols[k].size());
         for (int k = 0; k < NC; ++k) memcpy(hb.data() + o_rw[k], row_work[k].data(), sizeof(int2) * row_work[k].size());
-        for (int k = 0; k < 2 * NC; ++k) memcpy(hb.data() + o_cw[k], col_work[k].data(), sizeof(int2) * col_work[k].size());
+        for (int k = 0; k < NK * NC; ++k) memcpy(hb.data() + o_cw[k], col_work[k].data(), sizeof(int2) * col_work[k].size());
         memcpy(hb.data() + o_fin, fin.data(), sizeof(FinDesc) * n);
         memcpy(hb.data() + o_com, com.data(), sizeof(CommitDesc) * n);
         if (cudaMemcpy(blob, hb.data(), off, cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -2232,9 +2261,10 @@ struct FdmBatch {
         // set the shared-memory limits outside the capture
         size_t max_row = 0, max_col = 0;
         for (int k = 0; k < NC; ++k) max_row = std::max(max_row, row_smem[k]);
-        for (int k = 0; k < 2 * NC; ++k) max_col = std::max(max_col, col_smem[k]);
+        for (int k = 0; k < NK * NC; ++k) max_col = std::max(max_col, col_smem[k]);
         launch_row_pass_batched((const RowPass *)(blob + o_rows[0]), (const int2 *)(blob + o_rw[0]), 0, max_row, bstream);
-        launch_col_batched((const ColPass *)(blob + o_cols[0]), (const int2 *)(blob + o_cw[0]), 0, 0, max_col, bstream);
+        for (int kd = 0; kd < NK; ++kd)
+            launch_col_batched((const ColPass *)(blob + o_cols[0]), (const int2 *)(blob + o_cw[0]), 0, kd, max_col, bstream);
         cudaGetLastError();
         cudaGraph_t graph = nullptr;
         if (cudaStreamBeginCapture(bstream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
@@ -2253,7 +2283,7 @@ struct FdmBatch {
                     ok = launch_row_pass_batched((const RowPass *)(blob + o_rows[s]), (const int2 *)(blob + o_rw[rb]),
                                                  (int)row_work[rb].size(), row_smem[rb], bstream) == cudaSuccess;
             if (s < 6)
-                for (int cg = 0; cg < 2 * NC && ok; ++cg)
+                for (int cg = 0; cg < NK * NC && ok; ++cg)
                     if (!col_work[cg].empty())
                         ok = launch_col_batched((const ColPass *)(blob + o_cols[cg]), (const int2 *)(blob + o_cw[cg]),
                                                 (int)col_work[cg].size(), cg / NC, col_smem[cg], bstream) == cudaSuccess;
@@ -2297,6 +2327,7 @@ fullmag_fdm_batch *fullmag_fdm_batch_create(const fullmag_fdm_plan_desc *plans, 
             b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
             break;
         }
+        e->batch_tiling();
     }
     b->next_dt.assign(b->items.size(), 0.0);
     return reinterpret_cast<fullmag_fdm_batch *>(b);

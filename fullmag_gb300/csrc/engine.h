@@ -163,6 +163,9 @@ cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, i
 cudaError_t launch_finalize_batched(const FinDesc *fd, int nproblems, double *out, cudaStream_t s);
 cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s);
 int row_pass_blocks(const RowPass &p);
+// Kernel of the batched column pass for a grid: 0 thin film pruned, 1 fused y+z pruned,
+// 2 thin film general, 3 fused y+z general.
+int col_batched_kind(const Grid &g);
 int col_tile(const Grid &g, int lines_per_col, int len);
 
 }  // namespace fm

@@ -41,6 +41,9 @@ CASES = {
     "line_9x1x1": dict(nx=9, ny=1, nz=1),
     "single_1x1x1": dict(nx=1, ny=1, nz=1),
     "slab_12x10x2": dict(nx=12, ny=10, nz=2, d=(2e-9, 2e-9, 2e-9)),
+    # fused y+z pass on its pruned two-level path (py = 256, pz = 4; py = 128, pz = 8)
+    "yzf_8x128x2": dict(nx=8, ny=128, nz=2, d=(4e-9, 4e-9, 4e-9)),
+    "yzf_16x64x4": dict(nx=16, ny=64, nz=4, d=(4e-9, 4e-9, 4e-9)),
     # (y, z) planes too large for the fused y+z pass: y-forward / z-convolve / y-inverse,
     # the z pass on its pruned two-level path for pz = 16, 32, 64, 128 and on the
     # general path for pz = 24
