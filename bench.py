@@ -87,6 +87,10 @@ def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
     S = 24.0 * (nx + 1) / nx if demag else 0.0
     if integrator == "rk4":
         per_cell = [36 + S, 48 + 2 * S, 48 + 2 * S, 72 + 2 * S, 24 + S]
+    elif integrator == "dp45":
+        # first pass m0 + k1 -> y2; stages s = 1..5 read y_s, m0 and s earlier k's, write
+        # k_s and y_{s+1}; the last pass writes k7 and reads the 7 k's of the error norm
+        per_cell = [36 + S] + [48 + 12 * s + 2 * S for s in range(1, 6)] + [108 + S]
     else:
         per_cell = [36 + S, 60 + 2 * S, 24 + S]
     return sum(per_cell) / len(per_cell) * n
@@ -105,6 +109,12 @@ WORKLOADS = {
                              b_mt=(10.0, 5.0, 0.0), dt=5e-14, integrator="heun", seed=0),
     "film_256x64x1_rk4": dict(nx=256, ny=64, nz=1, d=4e-9, ms=8e5, a_ex=1.3e-11, alpha=0.05,
                               b_mt=(5.0, 0.0, 0.0), dt=5e-14, integrator="rk4", seed=2),
+    # thin film, adaptive Dormand-Prince (max error 1e-5), Ku = 5e3 J/m^3 along x, driven at
+    # (-24.6, 4.3, 0) mT from m0 = +x with a seeded uniform +-5 degree tilt per cell; every
+    # step is offered dt = 2e-13 s and the controller may shrink it
+    "film_512x128x1_dp45": dict(nx=512, ny=128, nz=1, d=(3.90625e-9, 3.90625e-9, 3e-9), ms=8e5, a_ex=1.3e-11,
+                                alpha=0.02, ku1=5e3, b_mt=(-24.6, 4.3, 0.0), dt=2e-13, integrator="dp45",
+                                max_error=1e-5, m0="tilt5", seed=4),
 }
 DEFAULT_WORKLOAD = "volume_256x256x64_rk4"
 SWEEP_WORKLOAD = "sweep_384_films_dp45"
@@ -299,17 +309,45 @@ def smoothed_random_unit(nx, ny, nz, seed, passes=3):
     return m.reshape(-1, 3)
 
 
+def tilted_x(n, seed, deg=5.0):
+    """+x with a seeded uniform tilt of up to `deg` degrees per cell (uniform azimuth)."""
+    rng = np.random.default_rng(seed)
+    th = np.deg2rad(deg) * rng.uniform(0.0, 1.0, n)
+    ph = rng.uniform(0.0, 2 * np.pi, n)
+    return np.stack([np.cos(th), np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph)], axis=1)
+
+
 def plan_kwargs(w):
     from fullmag_gb300 import _abi
-    kw = dict(nx=w["nx"], ny=w["ny"], nz=w["nz"], dx=w["d"], dy=w["d"], dz=w["d"], ms=w["ms"],
-              a_ex=w["a_ex"], alpha=w["alpha"], gamma=2.211e5,
-              m0=smoothed_random_unit(w["nx"], w["ny"], w["nz"], w["seed"]))
+    d = w["d"] if isinstance(w["d"], tuple) else (w["d"],) * 3
+    n = w["nx"] * w["ny"] * w["nz"]
+    m0 = tilted_x(n, w["seed"]) if w.get("m0") == "tilt5" else smoothed_random_unit(w["nx"], w["ny"], w["nz"], w["seed"])
+    kw = dict(nx=w["nx"], ny=w["ny"], nz=w["nz"], dx=d[0], dy=d[1], dz=d[2], ms=w["ms"],
+              a_ex=w["a_ex"], alpha=w["alpha"], gamma=2.211e5, m0=m0)
     if "b_mt" in w:
         kw["h_ext"] = tuple(b * 1e-3 / MU0 for b in w["b_mt"])
     if "kc1" in w:
         kw.update(kc1=w["kc1"], c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0))
-    integ = {"rk4": _abi.INTEGRATOR_RK4, "heun": _abi.INTEGRATOR_HEUN}[w["integrator"]]
+    if "ku1" in w:
+        kw.update(ku1=w["ku1"], u_axis=(1.0, 0.0, 0.0))
+    integ = {"rk4": _abi.INTEGRATOR_RK4, "heun": _abi.INTEGRATOR_HEUN, "dp45": _abi.INTEGRATOR_DP45}[w["integrator"]]
     return kw, integ
+
+
+def gpu_plan(w):
+    """Plan keywords of the GPU engine (adds the DP45 error bound)."""
+    kw, integ = plan_kwargs(w)
+    if w["integrator"] == "dp45":
+        kw["adaptive_max_error"] = w["max_error"]
+    return kw, integ
+
+
+def oracle_problem(O, w, sx, sy, sz):
+    """The oracle on a (sx, sy, sz) sample of the workload."""
+    kw, _ = plan_kwargs(dict(w, nx=sx, ny=sy, nz=sz))
+    integ = {"rk4": O.RK4, "heun": O.HEUN, "dp45": O.DP45}[w["integrator"]]
+    extra = {"max_error": w["max_error"]} if w["integrator"] == "dp45" else {}
+    return O.Problem(**kw, integrator=integ, **extra)
 
 
 class ClockSampler:
@@ -393,10 +431,7 @@ def cpu_baseline(w, threads):
         sx, sy, sz = max(nx // 2, 1), max(ny // 2, 1), max(nz // 2, 1)
     else:
         sx, sy, sz = nx, ny, nz
-    ws = dict(w, nx=sx, ny=sy, nz=sz)
-    kw, _ = plan_kwargs(ws)
-    integ = {"rk4": O.RK4, "heun": O.HEUN}[w["integrator"]]
-    pr = O.Problem(**kw, integrator=integ)
+    pr = oracle_problem(O, w, sx, sy, sz)
     pr.step(w["dt"])
     t0 = time.perf_counter()
     steps = 0
@@ -421,9 +456,7 @@ def run_reference(args, w, name, rank, world):
     O.set_threads(threads)
     nx, ny, nz = w["nx"], w["ny"], w["nz"]
     sx, sy, sz = (max(nx // 2, 1), max(ny // 2, 1), max(nz // 2, 1)) if nz > 1 else (nx, ny, nz)
-    kw, _ = plan_kwargs(dict(w, nx=sx, ny=sy, nz=sz))
-    integ = {"rk4": O.RK4, "heun": O.HEUN}[w["integrator"]]
-    pr = O.Problem(**kw, integrator=integ)
+    pr = oracle_problem(O, w, sx, sy, sz)
     for _ in range(args.warmup):
         pr.step(w["dt"])
     t0 = time.perf_counter()
@@ -491,7 +524,7 @@ def main():
     from fullmag_gb300 import FdmBackend, _abi
     from fullmag_gb300.build import build
     build()
-    kw, integ = plan_kwargs(w)
+    kw, integ = gpu_plan(w)
     n = w["nx"] * w["ny"] * w["nz"]
     dt = w["dt"]
 
@@ -564,6 +597,8 @@ def main():
         dom_bytes = row_pass_bytes_per_launch(w["integrator"], w["nx"], w["ny"], w["nz"])
     else:
         dom_bytes = kernel_bytes_per_launch(dominant, w["nx"], w["ny"], w["nz"], padded)
+    if not dom_avg_s > 0:
+        dom_bytes = None  # no timed launches
     traffic = NCU_TRAFFIC.get((args.workload, dominant))
 
     peak, peak_kind = load_peaks()
@@ -594,7 +629,7 @@ def main():
         "m_norm_max_dev": float(np.abs(np.linalg.norm(m_out, axis=1) - 1).max()),
     }
     be.close()
-    if not args.no_plain:
+    if not args.no_plain and w["integrator"] != "dp45":  # the plain path has Heun and RK4 only
         # the cuFFT + unfused path (reference per-step kernel structure), same workload;
         # each of its steps ends in blocking copies, so wall clock is its device time
         from fullmag_gb300.plain import PlainBaseline

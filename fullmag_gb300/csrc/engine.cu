@@ -734,7 +734,7 @@ struct Engine {
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
         dp45_dt = dt;
-        if (poll == nullptr && use_graphs) {
+        if (poll == nullptr && use_graphs && !ktime) {
             if (!dexec[cur] && !capture_dp45()) {
                 cudaGetLastError();
                 use_graphs = false;
@@ -761,6 +761,7 @@ struct Engine {
         if (!dp45_pending) return -1;
         dp45_pending = false;
         if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
+        kt_collect();
         const double dt = dp45_dt;
         const double err = sqrt(hstats[8]);
         if (err <= max_error || dt <= dt_min) {
