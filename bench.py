@@ -188,6 +188,51 @@ def run_sweep(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sweep_reference(args):
+    """The reference's way to run a sweep: one problem after another on the CPU engine
+    (the FP64 oracle, all host threads), each to t_end with its own DP45 controller
+    (dt0 = 1e-13 s, max error 1e-5).  Bounded: evenly strided problems until about 150 s
+    of CPU time; problems/s over the problems solved."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    plans = sweep_plans(args.sweep_count)
+    t_end, budget = args.sweep_t_end, 150.0
+    stride = max(1, len(plans) // 16)
+    solved, spent = 0, 0.0
+    for kw in plans[::stride]:
+        p = dict(kw)
+        p.pop("integrator")
+        me = p.pop("adaptive_max_error")
+        pr = O.Problem(**p, integrator=O.DP45, max_error=me)
+        t0 = time.perf_counter()
+        t, dt = 0.0, 1e-13
+        while t < t_end * (1 - 1e-12):
+            st = pr.step(min(dt, t_end - t))
+            t, dt = st["time"], st["suggested_next_dt"]
+            if time.perf_counter() - t0 > budget:
+                break
+        el = time.perf_counter() - t0
+        pr.close()
+        if t < t_end * (1 - 1e-12):
+            break  # this problem alone exceeds the budget: not counted
+        solved += 1
+        spent += el
+        if spent > budget:
+            break
+    v = solved / spent if spent > 0 else 0.0
+    print(json.dumps({"metric": "problems/s (batched sweep, DP45 to %.2g s)" % t_end, "value": v,
+                      "unit": "problems/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+                      "data": "synthetic (seeded)", "impl": "reference",
+                      "config": {"workload": SWEEP_WORKLOAD, "problems_solved": solved, "stride": stride,
+                                 "threads": threads},
+                      "cpu_baseline": {"value": v, "unit": "problems/s", "cores": threads, "kind": "port",
+                                       "sample": f"{solved} problems, every {stride}th, solved one at a time"},
+                      "e2e": {"value": v, "unit": "problems/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 ADJOINT_WORKLOAD = "adjoint_256x64x1_rk4_4000"
 
 
@@ -512,11 +557,15 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload == SWEEP_WORKLOAD:
         if rank == 0:
-            run_sweep(args)
+            run_sweep_reference(args) if args.impl == "reference" else run_sweep(args)
         return
     if args.workload == ADJOINT_WORKLOAD:
         if rank == 0:
-            run_adjoint(args)
+            if args.impl == "reference":
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint (gradients "
+                                  "of an LLG run are a capability only this engine provides)"}), flush=True)
+            else:
+                run_adjoint(args)
         return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
