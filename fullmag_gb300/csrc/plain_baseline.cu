@@ -383,6 +383,10 @@ bool setup(Plain &e, const fullmag_fdm_plan_desc *plan) {
         e.err = "plain path supports HEUN and RK4";
         return false;
     }
+    if (plan->active_mask || plan->region_mask) {
+        e.err = "plain path has no active or region masks";
+        return false;
+    }
     e.integrator = plan->integrator;
     e.dx = plan->grid.dx;
     e.dy = plan->grid.dy;

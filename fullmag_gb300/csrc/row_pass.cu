@@ -588,7 +588,7 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 4) row_pass_kernel(const RowPass p) { row_pass_body<false>(p, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) { row_pass_body<false>(p, blockIdx.x, gridDim.x); }
 __global__ void __launch_bounds__(kThreads) row_pass_adj_kernel(const RowPass p) { row_pass_body<true>(p, blockIdx.x, gridDim.x); }
 
 // One launch for many problems: work[blockIdx.x] = (problem, block within problem).

@@ -419,6 +419,8 @@ struct fo_problem {
     double *m0, *mst, *heff, *hscr, *k[7], *fsal;
     int fsal_valid;
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
+    uint32_t *region; /* optional region ids */
+    double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
 };
 
 static inline int active(const fo_problem *pr, long i) { return pr->mask == NULL || pr->mask[i] != 0; }
@@ -440,6 +442,7 @@ void fo_destroy(fo_problem *pr) {
     for (int c = 0; c < 6; ++c) free(pr->kern[c]);
     for (int c = 0; c < 3; ++c) { free(pr->bm[c]); free(pr->bh[c]); }
     free(pr->m0); free(pr->mst); free(pr->heff); free(pr->hscr); free(pr->fsal); free(pr->hmap);
+    free(pr->region); free(pr->lut);
     for (int s = 0; s < 7; ++s) free(pr->k[s]);
     free(pr);
 }
@@ -450,11 +453,20 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     if (!pr) return NULL;
     pr->p = *p;
     pr->p.active_mask = NULL;
+    pr->p.region_mask = NULL;
+    pr->p.exchange_lut = NULL;
     pr->n = (long)p->nx * p->ny * p->nz;
     const long n3 = 3 * pr->n;
     if (p->active_mask) {
         pr->mask = (uint8_t *)malloc((size_t)pr->n);
         memcpy(pr->mask, p->active_mask, (size_t)pr->n);
+    }
+    if (p->region_mask) {  /* api.cpp:405-420: default table A on the diagonal */
+        pr->region = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)pr->n);
+        memcpy(pr->region, p->region_mask, sizeof(uint32_t) * (size_t)pr->n);
+        pr->lut = dalloc((long)FO_MAX_REGIONS * FO_MAX_REGIONS);
+        if (p->exchange_lut) memcpy(pr->lut, p->exchange_lut, sizeof(double) * FO_MAX_REGIONS * FO_MAX_REGIONS);
+        else for (int r = 0; r < FO_MAX_REGIONS; ++r) pr->lut[r * FO_MAX_REGIONS + r] = p->a_ex;
     }
     pr->m = dalloc(n3);
     pr->m0 = dalloc(n3); pr->mst = dalloc(n3); pr->heff = dalloc(n3); pr->hscr = dalloc(n3);
@@ -531,6 +543,19 @@ static void exchange_add(const fo_problem *pr, const double *m, double *h) {
         nb[5] = i + (z < nz - 1 ? (long)nx * ny : 0);
         for (int q = 0; q < 6; ++q)
             if (!active(pr, nb[q])) nb[q] = i;
+        if (pr->region) {  /* exchange_fp32.cu:48-104: 2/(mu0 Ms) sum_q A[r_i][r_q] (m_q - m_i)/d^2 */
+            const double w[6] = {ix2, ix2, iy2, iy2, iz2, iz2};
+            const double s = 2.0 / (FO_MU0 * p->ms);
+            const uint32_t rc = pr->region[i];
+            for (int c = 0; c < 3; ++c) {
+                const double mc = m[3 * i + c];
+                double acc = 0.0;
+                for (int q = 0; q < 6; ++q)
+                    acc += pr->lut[rc * FO_MAX_REGIONS + pr->region[nb[q]]] * (m[3 * nb[q] + c] - mc) * w[q];
+                h[3 * i + c] += s * acc;
+            }
+            continue;
+        }
         for (int c = 0; c < 3; ++c) {
             const double mc = m[3 * i + c];
             h[3 * i + c] += pref * ((m[3 * nb[1] + c] - 2.0 * mc + m[3 * nb[0] + c]) * ix2 +
@@ -696,7 +721,8 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
             for (int q = 0; q < 3; ++q) {
                 if (nb[q] < 0 || !active(pr, nb[q])) continue;
                 const double a = m[3 * nb[q]] - mi[0], b = m[3 * nb[q] + 1] - mi[1], c = m[3 * nb[q] + 2] - mi[2];
-                epair += p->a_ex * V * (a * a + b * b + c * c) * w[q];
+                const double A = pr->region ? pr->lut[pr->region[i] * FO_MAX_REGIONS + pr->region[nb[q]]] : p->a_ex;
+                epair += A * V * (a * a + b * b + c * c) * w[q];
             }
             exf += -0.5 * FO_MU0 * p->ms * V * (mi[0] * h_ex[3 * i] + mi[1] * h_ex[3 * i + 1] + mi[2] * h_ex[3 * i + 2]);
         }

@@ -56,7 +56,14 @@ typedef struct {
     int32_t dp45_norm;           /* 0: ABI absolute max-norm, 1: CPU mixed atol/rtol norm */
     int32_t pad0;
     const uint8_t *active_mask;  /* optional, copied at create */
+    /* optional region ids (< FO_MAX_REGIONS) and the inter-region exchange table
+     * A[r_i * FO_MAX_REGIONS + r_j] in J/m (NULL with regions: A on the diagonal, 0 off
+     * it), copied at create; native/backends/fdm/src/exchange_fp32.cu:48-104, api.cpp:405-420 */
+    const uint32_t *region_mask;
+    const double *exchange_lut;
 } fo_params;
+
+#define FO_MAX_REGIONS 256
 
 typedef struct {
     double step, time, dt_used, suggested_next_dt;

@@ -45,6 +45,7 @@ class Params(C.Structure):
         ("shrink_limit", C.c_double),
         ("dp45_norm", C.c_int32), ("pad0", C.c_int32),
         ("active_mask", C.c_void_p),
+        ("region_mask", C.c_void_p), ("exchange_lut", C.c_void_p),
     ]
 
 
@@ -146,7 +147,7 @@ class Problem:
                  kc1=None, kc2=0.0, kc3=0.0, c1=(1, 0, 0), c2=(0, 1, 0),
                  max_error=1e-5, dt_min=1e-18, dt_max=1e-10, headroom=0.8, rtol=0.0,
                  growth_limit=float("inf"), shrink_limit=0.0, dp45_norm=0,
-                 active_mask=None, m0=None):
+                 active_mask=None, m0=None, region_mask=None, exchange_lut=None):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -169,6 +170,16 @@ class Problem:
         if active_mask is not None:
             self._mask = np.ascontiguousarray(active_mask, dtype=np.uint8)
             p.active_mask = self._mask.ctypes.data
+        if region_mask is not None:
+            self._regions = np.ascontiguousarray(region_mask, dtype=np.uint32).reshape(-1)
+            if self._regions.size != nx * ny * nz or (self._regions.size and self._regions.max() >= 256):
+                raise ValueError("region_mask needs one id below 256 per cell")
+            p.region_mask = self._regions.ctypes.data
+            if exchange_lut is not None:
+                self._lut = np.ascontiguousarray(exchange_lut, dtype=np.float64).reshape(-1)
+                if self._lut.size != 256 * 256:
+                    raise ValueError("exchange_lut needs 256 x 256 entries")
+                p.exchange_lut = self._lut.ctypes.data
         self.n = nx * ny * nz
         self.shape = (nz, ny, nx)
         self.params = p
