@@ -11,6 +11,8 @@
 // every octant kernel value is read from HBM once per evaluation.
 #include "engine.h"
 
+#include <algorithm>
+
 namespace fm {
 
 namespace {
@@ -373,7 +375,7 @@ __device__ __forceinline__ void z_small_convolve(float2 *line, size_t lstride, i
         int kzm;
         float sz;
         kernel_mirror(kz, PZ, kzm, sz);
-        const float *K = kern + ((size_t)kzm * nky + kym) * nkx + kx;
+        const float *K = kern + ((size_t)kzm * nkx + kx) * nky + kym;  // ky-fastest layout
         const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
         const float kxy = sy * __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz = sy * sz * __ldg(K + 5 * kc);
         const float2 mx = v[0][kz], my = v[1][kz], mz = v[2][kz];
@@ -551,7 +553,7 @@ __device__ __forceinline__ void yz_convolve_general_body(const ColPass &p, const
         float sy, sz;
         kernel_mirror(ky, g.py, kym, sy);
         kernel_mirror(kz, g.pz, kzm, sz);
-        const float *K = p.kern + ((size_t)kzm * g.nky + kym) * g.nkx + kx;
+        const float *K = p.kern + ((size_t)kzm * g.nkx + kx) * g.nky + kym;  // ky-fastest layout
         const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
         const float kxy = sy * __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz = sy * sz * __ldg(K + 5 * kc);
         float2 *lx = R2 + ((0 * tx + col) * g.py + ky) * lsz + sk(kz);
@@ -748,6 +750,10 @@ __global__ void __launch_bounds__(kThreads, KIND < 2 ? 2 : 4) col_batched_kernel
                                                                const int2 *__restrict__ work) {
     __shared__ __align__(16) unsigned char desc[sizeof(ColPass)];  // descriptor staged once per CTA
     const int2 w = work[blockIdx.x];
+    // a finished problem (step size 0) keeps its tiles in the table until the round is
+    // rebuilt; the whole CTA leaves before its first barrier
+    const double *skip = ps[w.x].skip_dt;
+    if (skip && *skip <= 0.0) return;
     const int *src = reinterpret_cast<const int *>(ps + w.x);
     for (int i = threadIdx.x; i < (int)(sizeof(ColPass) / sizeof(int)); i += blockDim.x)
         reinterpret_cast<int *>(desc)[i] = src[i];
@@ -1002,6 +1008,26 @@ cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s) {
 
 cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s) {
     finalize_stats_kernel<<<1, kFinThreads, 0, s>>>(partials, nblocks, out);
+    return cudaGetLastError();
+}
+
+namespace {
+// [c][kz][ky][kx] -> [c][kz][kx][ky]; one launch at setup
+__global__ void kern_ky_fast_kernel(const float *__restrict__ in, float *__restrict__ out, long long planes, int nky,
+                                    int nkx) {
+    const long long per = (long long)nky * nkx;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < planes * per; i += (long long)gridDim.x * blockDim.x) {
+        const long long pl = i / per;
+        const int r = (int)(i - pl * per), ky = r / nkx, kx = r - ky * nkx;
+        out[pl * per + (long long)kx * nky + ky] = in[i];
+    }
+}
+}  // namespace
+
+cudaError_t launch_kern_ky_fast(const float *in, float *out, int ncomp, int nkz, int nky, int nkx, cudaStream_t s) {
+    const long long total = (long long)ncomp * nkz * nky * nkx;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
+    kern_ky_fast_kernel<<<blocks, 256, 0, s>>>(in, out, (long long)ncomp * nkz, nky, nkx);
     return cudaGetLastError();
 }
 

@@ -1529,6 +1529,15 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         } else if (!upload_spectra(plan, thin)) {
             return false;
         }
+        if (use_yz) {  // the fused y+z passes read the kernel ky-fastest
+            float *tmp = nullptr;
+            if (cuda_fail("cudaMalloc(kernel transpose)", cudaMalloc((void **)&tmp, klen))) return false;
+            const bool ok = !cuda_fail("kernel transpose", launch_kern_ky_fast(kern, tmp, 6, g.nkz, g.nky, g.nkx, stream)) &&
+                            !cuda_fail("kernel transpose copy", cudaMemcpyAsync(kern, tmp, klen, cudaMemcpyDeviceToDevice, stream)) &&
+                            !cuda_fail("kernel transpose sync", cudaStreamSynchronize(stream));
+            cudaFree(tmp);
+            if (!ok) return false;
+        }
     }
     if (cuda_fail("setup sync", cudaStreamSynchronize(stream))) return false;
     const char *no_tune = std::getenv("FULLMAG_FDM_NO_TUNE");
@@ -1569,22 +1578,6 @@ bool Engine::autotune() {
             return true;
         }
     }
-    auto fits = [&](int lines_per_col, int len, int tx) {
-        return tx <= std::max(1, g.nkx) && (size_t)2 * lines_per_col * tx * skewed_len(len) * sizeof(float2) <= 200u * 1024u;
-    };
-    auto best_tx = [&](int lines_per_col, int len, const std::function<bool(int)> &run, int fallback) {
-        int best = fallback;
-        float bt = 1e30f;
-        for (int tx : {1, 2, 4, 8, 16}) {
-            if (!fits(lines_per_col, len, tx)) continue;
-            const float t = time_ms([&] { return run(tx); });
-            if (t < bt) {
-                bt = t;
-                best = tx;
-            }
-        }
-        return best;
-    };
     if (demag) {
         if (g.thin) {
             int best = tx_2d;
@@ -2156,12 +2149,50 @@ struct FdmBatch {
     std::vector<double> next_dt;  // per problem: suggested step (DP45) or 0 before the first step
     std::string last_error;
     cudaStream_t bstream = nullptr;
+    // Branches of a captured round: the buckets of one pass (row buckets, column groups)
+    // are independent launches, captured as parallel graph branches so that a bucket of
+    // a few dozen CTAs runs beside the large ones instead of after them.
+    static constexpr int kSide = 8;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[kSide] = {};
     BatchRound round;
     ~FdmBatch() {
         if (bstream) cudaStreamSynchronize(bstream);
         round.release();
+        for (int j = 0; j < kSide; ++j) {
+            if (side[j]) cudaStreamDestroy(side[j]);
+            if (join_ev[j]) cudaEventDestroy(join_ev[j]);
+        }
+        if (fork_ev) cudaEventDestroy(fork_ev);
         if (bstream) cudaStreamDestroy(bstream);
         for (Engine *e : items) delete e;
+    }
+
+    bool ensure_branches() {
+        if (fork_ev) return true;
+        for (int j = 0; j < kSide; ++j)
+            if (cudaStreamCreateWithFlags(&side[j], cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&join_ev[j], cudaEventDisableTiming) != cudaSuccess)
+                return false;
+        return cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess;
+    }
+
+    // Enqueues launch(id, stream) for every id as parallel branches that fork from and
+    // join back into bstream (inside a capture: graph nodes with no edges between them).
+    template <typename F>
+    bool fan_out(const std::vector<int> &ids, F &&launch) {
+        if (ids.empty()) return true;
+        if (ids.size() == 1) return launch(ids[0], bstream) == cudaSuccess;
+        const int ns = std::min<int>((int)ids.size(), kSide);
+        if (cudaEventRecord(fork_ev, bstream) != cudaSuccess) return false;
+        for (int j = 0; j < ns; ++j)
+            if (cudaStreamWaitEvent(side[j], fork_ev, 0) != cudaSuccess) return false;
+        for (size_t j = 0; j < ids.size(); ++j)
+            if (launch(ids[j], side[j % ns]) != cudaSuccess) return false;
+        for (int j = 0; j < ns; ++j)
+            if (cudaEventRecord(join_ev[j], side[j]) != cudaSuccess || cudaStreamWaitEvent(bstream, join_ev[j], 0) != cudaSuccess)
+                return false;
+        return true;
     }
 
     // Builds (and captures) the round for `act`; false when a member cannot run batched.
@@ -2221,6 +2252,7 @@ struct FdmBatch {
                 const size_t cs = thin ? y_convolve_2d_smem(e->g, tx) : yz_convolve_smem(e->g, tx);
                 const int cg = kind * NC + smem_class(cs);
                 ColPass c = e->col_pass(e->plan_y, tx, e->X, e->X);
+                c.skip_dt = &round.d_ctl[k].dt;
                 const int idx = (int)cols[cg].size();
                 cols[cg].push_back(c);
                 const int ntiles = (e->g.nkx + tx - 1) / tx;
@@ -2267,6 +2299,15 @@ struct FdmBatch {
         for (int kd = 0; kd < NK; ++kd)
             launch_col_batched((const ColPass *)(blob + o_cols[0]), (const int2 *)(blob + o_cw[0]), 0, kd, max_col, bstream);
         cudaGetLastError();
+        if (!ensure_branches()) {
+            err = "batch stream or event creation failed";
+            return false;
+        }
+        std::vector<int> row_ids, col_ids;
+        for (int rb = 0; rb < NC; ++rb)
+            if (!row_work[rb].empty()) row_ids.push_back(rb);
+        for (int cg = 0; cg < NK * NC; ++cg)
+            if (!col_work[cg].empty()) col_ids.push_back(cg);
         cudaGraph_t graph = nullptr;
         if (cudaStreamBeginCapture(bstream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             err = "batch capture failed";
@@ -2279,15 +2320,15 @@ struct FdmBatch {
             ok = cudaGetLastError() == cudaSuccess;
         }
         for (int s = 0; s < 7 && ok; ++s) {
-            for (int rb = 0; rb < NC && ok; ++rb)
-                if (!row_work[rb].empty())
-                    ok = launch_row_pass_batched((const RowPass *)(blob + o_rows[s]), (const int2 *)(blob + o_rw[rb]),
-                                                 (int)row_work[rb].size(), row_smem[rb], bstream) == cudaSuccess;
-            if (s < 6)
-                for (int cg = 0; cg < NK * NC && ok; ++cg)
-                    if (!col_work[cg].empty())
-                        ok = launch_col_batched((const ColPass *)(blob + o_cols[cg]), (const int2 *)(blob + o_cw[cg]),
-                                                (int)col_work[cg].size(), cg / NC, col_smem[cg], bstream) == cudaSuccess;
+            ok = fan_out(row_ids, [&](int rb, cudaStream_t st) {
+                return launch_row_pass_batched((const RowPass *)(blob + o_rows[s]), (const int2 *)(blob + o_rw[rb]),
+                                               (int)row_work[rb].size(), row_smem[rb], st);
+            });
+            if (ok && s < 6)
+                ok = fan_out(col_ids, [&](int cg, cudaStream_t st) {
+                    return launch_col_batched((const ColPass *)(blob + o_cols[cg]), (const int2 *)(blob + o_cw[cg]),
+                                              (int)col_work[cg].size(), cg / NC, col_smem[cg], st);
+                });
         }
         if (ok) ok = launch_finalize_batched((const FinDesc *)(blob + o_fin), n, round.d_stats, bstream) == cudaSuccess;
         if (ok)
@@ -2347,8 +2388,9 @@ uint32_t fullmag_fdm_batch_size(fullmag_fdm_batch *batch) {
 // Batched-kernel path (all problems DP45 and small enough for the fused column
 // passes).  Each round replays one graph for all unfinished problems, waits once,
 // then applies the accept/reject rule per problem on the host.  Problems that reached
-// t_end keep computing discarded proposals until the round is rebuilt without them
-// (when a quarter of its members have finished).  Returns 1 when not batchable.
+// t_end stay in the round's work tables with step size 0, which makes their row and
+// column CTAs return at once, until the round is rebuilt without them (when a tenth
+// of its members have finished).  Returns 1 when not batchable.
 static int batch_step_until_batched(FdmBatch *b, double t_end, double dt0, uint64_t *out_steps, uint64_t *out_wall_ns) {
     const size_t n = b->items.size();
     const auto t0 = std::chrono::steady_clock::now();
@@ -2387,7 +2429,8 @@ static int batch_step_until_batched(FdmBatch *b, double t_end, double dt0, uint6
         const std::vector<size_t> &mem = b->round.members;
         for (size_t k = 0; k < mem.size(); ++k) {
             Engine *e = b->items[mem[k]];
-            b->round.h_ctl[k].dt = done[mem[k]] ? e->dt_min : std::min(b->next_dt[mem[k]], t_end - e->time);
+            // a finished problem gets step size 0: its row and column CTAs return at once
+            b->round.h_ctl[k].dt = done[mem[k]] ? 0.0 : std::min(b->next_dt[mem[k]], t_end - e->time);
         }
         if (cudaGraphLaunch(b->round.exec, b->bstream) != cudaSuccess || cudaStreamSynchronize(b->bstream) != cudaSuccess) {
             b->last_error = "batch round launch failed";

@@ -9,6 +9,10 @@
 //   demag kernel  : real, octant-unique, pre-scaled by Ms/P:
 //                   3-D K[6][pz/2+1][py/2+1][kx]   (xx yy zz xy xz yz)
 //                   2-D K[4][py/2+1][kx]           (xx yy zz xy)
+//                   engines on the fused y+z path (small 3-D grids, every batched
+//                   3-D problem) hold K[6][pz/2+1][kx][py/2+1]: their CTAs take one
+//                   or a few kx columns and spread the threads over ky, so ky-fastest
+//                   loads coalesce
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -126,6 +130,7 @@ struct ColPass {
     float2 *out;
     const float *kern;       // demag kernel (multiply passes)
     int inverse;
+    const double *skip_dt;   // batched rounds: the problem's step size; <= 0 skips its tiles
 };
 
 // Launchers (kernels.cu)
@@ -138,6 +143,8 @@ cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
 cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s);  // X -> X (small 3-D, uses plan2 for z)
 size_t yz_convolve_smem(const Grid &g, int tx);
+// K[c][kz][ky][kx] -> K[c][kz][kx][ky] (the fused y+z path's layout), out of place
+cudaError_t launch_kern_ky_fast(const float *in, float *out, int ncomp, int nkz, int nky, int nkx, cudaStream_t s);
 size_t z_convolve_smem(const Grid &g, int tx);
 size_t y_pass_smem(const Grid &g, int tx);
 size_t y_convolve_2d_smem(const Grid &g, int tx);

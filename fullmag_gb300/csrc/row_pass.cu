@@ -598,6 +598,10 @@ __global__ void __launch_bounds__(kThreads) row_pass_batched_kernel(const RowPas
     // fields in every loop, and global reads could not be hoisted past the stores
     __shared__ __align__(16) unsigned char desc[sizeof(RowPass)];
     const int2 w = work[blockIdx.x];
+    // a finished problem (step size 0 in its control block) keeps its blocks in the table
+    // until the round is rebuilt; the whole CTA leaves before its first barrier
+    const double *dtp = ps[w.x].dt_dev;
+    if (dtp && *dtp <= 0.0) return;
     const int *src = reinterpret_cast<const int *>(ps + w.x);
     for (int i = threadIdx.x; i < (int)(sizeof(RowPass) / sizeof(int)); i += blockDim.x)
         reinterpret_cast<int *>(desc)[i] = src[i];
