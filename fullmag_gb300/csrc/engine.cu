@@ -18,6 +18,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -46,6 +47,46 @@ __global__ void aos_to_soa_kernel(const double *__restrict__ in_d, const float *
         }
     }
 }
+// Box-average preview of a SoA float field: preview cell o = px + pnx (py + pny pz) averages
+// x in [px nx/pnx, (px+1) nx/pnx), the same for y, and z in [z0 + pz zst, z0 + (pz+1) zst)
+// (each range at least one cell, clamped to the grid).  FP64 sums in z, y, x order: the
+// operations of a host loop over the field converted to double, so the output does not
+// depend on where it is computed.  Output AoS.
+template <typename T>
+__global__ void preview_kernel(const float *__restrict__ f, long long n, unsigned fx, unsigned fy, unsigned fz,
+                               unsigned pnx, unsigned pny, unsigned pnz, unsigned z0, unsigned zst, T *__restrict__ out) {
+    const long long np = (long long)pnx * pny * pnz;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < np; o += (long long)gridDim.x * blockDim.x) {
+        const unsigned px = (unsigned)(o % pnx);
+        const unsigned py = (unsigned)((o / pnx) % pny);
+        const unsigned pz = (unsigned)(o / ((long long)pnx * pny));
+        unsigned zs0 = z0 + pz * zst;
+        if (zs0 >= fz) zs0 = fz - 1;
+        unsigned ze = z0 + (pz + 1) * zst;
+        if (ze <= zs0) ze = zs0 + 1;
+        if (ze > fz) ze = fz;
+        unsigned ys = (unsigned)(((unsigned long long)py * fy) / pny), ye = (unsigned)(((unsigned long long)(py + 1) * fy) / pny);
+        if (ye <= ys) ye = ys + 1;
+        if (ye > fy) ye = fy;
+        unsigned xs = (unsigned)(((unsigned long long)px * fx) / pnx), xe = (unsigned)(((unsigned long long)(px + 1) * fx) / pnx);
+        if (xe <= xs) xe = xs + 1;
+        if (xe > fx) xe = fx;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, cnt = 0.0;
+        for (unsigned z = zs0; z < ze; ++z)
+            for (unsigned y = ys; y < ye; ++y)
+                for (unsigned x = xs; x < xe; ++x) {
+                    const long long i = ((long long)z * fy + y) * fx + x;
+                    a0 += (double)f[i];
+                    a1 += (double)f[n + i];
+                    a2 += (double)f[2 * n + i];
+                    cnt += 1.0;
+                }
+        out[3 * o] = (T)(a0 / cnt);
+        out[3 * o + 1] = (T)(a1 / cnt);
+        out[3 * o + 2] = (T)(a2 / cnt);
+    }
+}
+
 // Control block of a batched DP45 attempt (host-pinned, copied to the device by the
 // first node of the attempt graph).
 struct BatchCtl {
@@ -93,6 +134,58 @@ __global__ void soa_to_aos_kernel(const float *__restrict__ in, double *__restri
         }
     }
 }
+
+// Pinned host buffers for snapshot payloads.  Page-locking tens of MB takes
+// milliseconds, so buffers are reused: a snapshot takes one at begin and returns it
+// at destroy.  Shared between a backend and its snapshots, since a snapshot may
+// outlive the backend.
+struct PinnedPool {
+    std::mutex mu;
+    std::vector<std::pair<void *, size_t>> free_bufs;
+    void *take(size_t bytes, size_t &cap) {
+        std::lock_guard<std::mutex> lk(mu);
+        size_t best = free_bufs.size();
+        for (size_t k = 0; k < free_bufs.size(); ++k)
+            if (free_bufs[k].second >= bytes && (best == free_bufs.size() || free_bufs[k].second < free_bufs[best].second))
+                best = k;
+        if (best < free_bufs.size()) {
+            void *p = free_bufs[best].first;
+            cap = free_bufs[best].second;
+            free_bufs.erase(free_bufs.begin() + (long)best);
+            return p;
+        }
+        void *p = nullptr;
+        if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+        cap = bytes;
+        return p;
+    }
+    void give(void *p, size_t cap) {
+        std::lock_guard<std::mutex> lk(mu);
+        free_bufs.emplace_back(p, cap);
+    }
+    ~PinnedPool() {
+        for (auto &b : free_bufs) cudaFreeHost(b.first);
+    }
+};
+
+// Snapshot payload: host-synthesised bytes, or a pinned buffer that a device-to-host
+// copy on the backend's snapshot stream fills; `done` marks the end of that copy.
+struct SnapshotPayload {
+    std::vector<unsigned char> bytes;
+    std::shared_ptr<PinnedPool> pool;
+    void *pinned = nullptr;
+    size_t cap = 0, len = 0;
+    cudaEvent_t done = nullptr;
+    fullmag_fdm_snapshot_desc desc{};
+    bool ok = false;
+    ~SnapshotPayload() {
+        if (done) {
+            cudaEventSynchronize(done);  // the copy must finish before the buffer is reused
+            cudaEventDestroy(done);
+        }
+        if (pinned && pool) pool->give(pinned, cap);
+    }
+};
 
 struct Engine {
     // ---- configuration ----
@@ -151,6 +244,11 @@ struct Engine {
 
     void release() {
         if (stream) cudaStreamSynchronize(stream);
+        if (snap_stream) {
+            cudaStreamSynchronize(snap_stream);
+            cudaStreamDestroy(snap_stream);
+            snap_stream = nullptr;
+        }
         drop_graphs();
         kt_free();
         adj_free();
@@ -1221,12 +1319,83 @@ struct Engine {
         return !cuda_fail("download sync", cudaStreamSynchronize(stream));
     }
 
+    // ---- asynchronous snapshots ----
+    cudaStream_t snap_stream = nullptr;  // device-to-host copies of snapshot payloads
+    std::shared_ptr<PinnedPool> pinned_pool = std::make_shared<PinnedPool>();
+
+    // `produce(dev)` enqueues a payload of `bytes` into a stream-ordered device buffer on
+    // the engine stream; a copy on the snapshot stream then fills a pinned buffer of s,
+    // and s->done marks its end.  Later steps run on the engine stream meanwhile.
+    template <typename F>
+    bool begin_snapshot(size_t bytes, F &&produce, SnapshotPayload *s) {
+        if (!snap_stream &&
+            cuda_fail("cudaStreamCreate(snapshot)", cudaStreamCreateWithFlags(&snap_stream, cudaStreamNonBlocking)))
+            return false;
+        s->pool = pinned_pool;
+        s->pinned = pinned_pool->take(bytes, s->cap);
+        if (!s->pinned) {
+            last_error = "cudaMallocHost(snapshot) failed";
+            return false;
+        }
+        s->len = bytes;
+        cudaEvent_t ready = nullptr;
+        if (cuda_fail("cudaEventCreate(snapshot)", cudaEventCreateWithFlags(&ready, cudaEventDisableTiming))) return false;
+        if (cuda_fail("cudaEventCreate(snapshot)", cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming))) {
+            cudaEventDestroy(ready);
+            return false;
+        }
+        void *dev = nullptr;
+        bool ok = !cuda_fail("cudaMallocAsync(snapshot)", cudaMallocAsync(&dev, bytes, stream));
+        if (ok) {
+            ok = produce(dev) && !cuda_fail("snapshot event", cudaEventRecord(ready, stream)) &&
+                 !cuda_fail("snapshot stream wait", cudaStreamWaitEvent(snap_stream, ready, 0)) &&
+                 !cuda_fail("cudaMemcpy(snapshot)", cudaMemcpyAsync(s->pinned, dev, bytes, cudaMemcpyDeviceToHost, snap_stream));
+            cudaFreeAsync(dev, ok ? snap_stream : stream);
+            if (ok) ok = !cuda_fail("snapshot event", cudaEventRecord(s->done, snap_stream));
+        }
+        cudaEventDestroy(ready);
+        return ok;
+    }
+
+    // Device-resident observable `obs` made current (fields evaluated if stale); NULL for
+    // H_EXT (synthesised on the host) and unknown observables (last_error set).
+    const float *current_field(int obs) {
+        if (obs < FULLMAG_FDM_OBSERVABLE_M || obs > FULLMAG_FDM_OBSERVABLE_H_EFF || obs == FULLMAG_FDM_OBSERVABLE_H_EXT) {
+            if (obs != FULLMAG_FDM_OBSERVABLE_H_EXT) last_error = "unknown observable " + std::to_string(obs);
+            return nullptr;
+        }
+        if (obs != FULLMAG_FDM_OBSERVABLE_M && !fields_valid && !eval_state(true)) return nullptr;
+        return field_ptr(obs);
+    }
+
+    // Box-average preview of a device field into dev_out (AoS T) on stream s.
+    template <typename T>
+    bool enqueue_preview(const float *field, uint32_t pnx, uint32_t pny, uint32_t pnz, uint32_t z0, uint32_t zs, T *dev_out,
+                         cudaStream_t s) {
+        const long long np = (long long)pnx * pny * pnz;
+        preview_kernel<T><<<(unsigned)std::min<long long>((np + 255) / 256, 4096), 256, 0, s>>>(
+            field, g.n, (unsigned)g.nx, (unsigned)g.ny, (unsigned)g.nz, pnx, pny, pnz, z0, zs, dev_out);
+        return !cuda_fail("preview", cudaGetLastError());
+    }
+
     template <typename T>
     bool preview(int obs, uint32_t pnx, uint32_t pny, uint32_t pnz, uint32_t z0, uint32_t zs, T *out) {
         if (z0 >= (uint32_t)g.nz) {
             last_error = "preview z_origin out of range";
             return false;
         }
+        if (obs != FULLMAG_FDM_OBSERVABLE_H_EXT) {
+            const float *field = current_field(obs);
+            if (!field) return false;
+            const size_t bytes = sizeof(T) * 3 * (size_t)pnx * pny * pnz;
+            void *dev = nullptr;
+            if (cuda_fail("cudaMallocAsync(preview)", cudaMallocAsync(&dev, bytes, stream))) return false;
+            const bool ok = enqueue_preview<T>(field, pnx, pny, pnz, z0, zs, (T *)dev, stream) &&
+                            !cuda_fail("cudaMemcpy(preview)", cudaMemcpyAsync(out, dev, bytes, cudaMemcpyDeviceToHost, stream));
+            cudaFreeAsync(dev, stream);
+            return !cuda_fail("preview sync", cudaStreamSynchronize(stream)) && ok;
+        }
+        // H_EXT lives on the host: the same box average over the synthesised field
         std::vector<double> full(3 * (size_t)g.n);
         if (!download<double>(obs, full.data())) return false;
         const uint32_t fx = g.nx, fy = g.ny, fz = g.nz;
@@ -1717,20 +1886,16 @@ static int preview_impl(fullmag_fdm_backend *handle, fullmag_fdm_observable obs,
     return e->preview<T>(obs, pnx, pny, pnz, z0, zs, out) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
 }
 
-// Snapshots: the payload is produced at begin time into memory owned by the
-// snapshot (component-major SoA for field snapshots, AoS for previews), so
-// wait never touches the backend and may run on another thread.
-struct SnapshotPayload {
-    std::vector<unsigned char> bytes;
-    fullmag_fdm_snapshot_desc desc{};
-    bool ok = false;
-};
-
+// Snapshots (context.cu:1073-1745 semantics): begin captures the observable as it is at
+// that moment (component-major SoA for field snapshots, AoS for previews) into memory
+// owned by the snapshot, without waiting for the device-to-host copy; wait blocks on the
+// copy only, never touches the backend and may run on another thread.
 static int snap_wait(SnapshotPayload *s, const void **out_data, uint64_t *out_len, fullmag_fdm_snapshot_desc *out_desc) {
     if (!s || !out_data || !out_len || !out_desc) return FULLMAG_FDM_ERR_INVALID;
     if (!s->ok) return FULLMAG_FDM_ERR_CUDA;
-    *out_data = s->bytes.data();
-    *out_len = s->bytes.size();
+    if (s->done && cudaEventSynchronize(s->done) != cudaSuccess) return FULLMAG_FDM_ERR_CUDA;
+    *out_data = s->pinned ? s->pinned : (const void *)s->bytes.data();
+    *out_len = s->pinned ? s->len : s->bytes.size();
     *out_desc = s->desc;
     return FULLMAG_FDM_OK;
 }
@@ -1860,15 +2025,32 @@ fullmag_fdm_field_snapshot *fullmag_fdm_backend_begin_field_snapshot(fullmag_fdm
     auto *s = new (std::nothrow) SnapshotPayload();
     if (!s) return nullptr;
     const size_t n = (size_t)e->g.n;
-    std::vector<float> aos(3 * n);
-    if (!e->download<float>(observable, aos.data())) {
-        delete s;
-        return nullptr;
+    if (observable == FULLMAG_FDM_OBSERVABLE_H_EXT) {  // synthesised on the host
+        std::vector<float> aos(3 * n);
+        if (!e->download<float>(observable, aos.data())) {
+            delete s;
+            return nullptr;
+        }
+        s->bytes.resize(sizeof(float) * 3 * n);
+        float *soa = reinterpret_cast<float *>(s->bytes.data());
+        for (size_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) soa[c * n + i] = aos[3 * i + c];
+    } else {
+        // the device field is SoA already: one device copy on the engine stream pins the
+        // state of this moment, the copy to the host runs on the snapshot stream
+        const float *field = e->current_field(observable);
+        const size_t bytes = sizeof(float) * 3 * n;
+        if (!field || !e->begin_snapshot(
+                          bytes,
+                          [&](void *dev) {
+                              return !e->cuda_fail("cudaMemcpy(snapshot field)",
+                                                   cudaMemcpyAsync(dev, field, bytes, cudaMemcpyDeviceToDevice, e->stream));
+                          },
+                          s)) {
+            delete s;
+            return nullptr;
+        }
     }
-    s->bytes.resize(sizeof(float) * 3 * n);
-    float *soa = reinterpret_cast<float *>(s->bytes.data());
-    for (size_t i = 0; i < n; ++i)
-        for (int c = 0; c < 3; ++c) soa[c * n + i] = aos[3 * i + c];
     s->desc.cell_count = n;
     s->desc.component_count = 3;
     s->desc.scalar_bytes = 4;
@@ -1887,11 +2069,31 @@ fullmag_fdm_preview_snapshot *fullmag_fdm_backend_begin_preview_snapshot(fullmag
     auto *s = new (std::nothrow) SnapshotPayload();
     if (!s) return nullptr;
     const size_t n = (size_t)preview_nx * preview_ny * preview_nz;
-    s->bytes.resize(sizeof(float) * 3 * n);
-    if (!e->preview<float>(observable, preview_nx, preview_ny, preview_nz, z_origin, z_stride,
-                           reinterpret_cast<float *>(s->bytes.data()))) {
+    if (z_origin >= (uint32_t)e->g.nz) {
+        e->last_error = "preview z_origin out of range";
         delete s;
         return nullptr;
+    }
+    if (observable == FULLMAG_FDM_OBSERVABLE_H_EXT) {  // synthesised on the host
+        s->bytes.resize(sizeof(float) * 3 * n);
+        if (!e->preview<float>(observable, preview_nx, preview_ny, preview_nz, z_origin, z_stride,
+                               reinterpret_cast<float *>(s->bytes.data()))) {
+            delete s;
+            return nullptr;
+        }
+    } else {
+        // downsampled on the device into the snapshot's buffer, copied out on the snapshot stream
+        const float *field = e->current_field(observable);
+        if (!field || !e->begin_snapshot(
+                          sizeof(float) * 3 * n,
+                          [&](void *dev) {
+                              return e->enqueue_preview<float>(field, preview_nx, preview_ny, preview_nz, z_origin,
+                                                               z_stride, (float *)dev, e->stream);
+                          },
+                          s)) {
+            delete s;
+            return nullptr;
+        }
     }
     s->desc.cell_count = n;
     s->desc.component_count = 3;
