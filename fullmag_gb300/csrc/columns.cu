@@ -89,6 +89,18 @@ __global__ void __launch_bounds__(kThreads) y_inverse_kernel(const ColPass p) {
     }
 }
 
+// Work item `it` of a kx tile -> (row, col), col fastest over the tile's ncol live
+// columns.  nkx = px/2 + 1 is odd, so the last tile of a grid usually holds one live
+// column; iterating rows * ncol items (not rows * tx) lets it skip the padding columns
+// instead of computing them.  Only the last tile can be partial, so the divider is
+// either the tile width's or the last tile's (fd_last, precomputed on the host).
+// Shared-memory lines stay indexed by col within tx.
+__device__ __forceinline__ void tile_item(const ColPass &p, int ncol, int it, int &row, int &col) {
+    const FastDiv &fd = ncol == p.tx ? p.fd_tx : p.fd_last;
+    row = fd.div(it);
+    col = it - row * ncol;
+}
+
 // Number of y-frequencies a CTA handles: ky and py - ky (1 for ky = 0 and the Nyquist row).
 __device__ __forceinline__ int ky_pair(int kya, int py, int &kyb) {
     kyb = py - kya;
@@ -180,30 +192,29 @@ __global__ void __launch_bounds__(kThreads, 2) y_forward_fused_kernel(const ColP
     const int z = blockIdx.y, c = blockIdx.z;
     const float2 *__restrict__ tw = p.plan.tw;
     const float2 *src = p.in + ((size_t)c * g.nz + z) * g.ny * g.nkx + kx0;
-    for (int it = threadIdx.x; it < N2 * tx; it += blockDim.x) {
-        const int n2 = p.fd_tx.div(it), col = it - n2 * tx;
-        const bool okc = col < ncol;
+    for (int it = threadIdx.x; it < N2 * ncol; it += blockDim.x) {
+        int n2, col;
+        tile_item(p, ncol, it, n2, col);
         float2 e[H1];
 #pragma unroll
         for (int n1 = 0; n1 < H1; ++n1) {
             const int y = N2 * n1 + n2;
-            e[n1] = (okc && y < g.ny) ? src[(size_t)y * g.nkx + col] : make_float2(0.f, 0.f);
+            e[n1] = y < g.ny ? src[(size_t)y * g.nkx + col] : make_float2(0.f, 0.f);
         }
         half_dft_store<N1, N2>(e, n2, buf + col * ls, tw);
     }
     __syncthreads();
     float2 *dst = p.out + ((size_t)c * g.nz + z) * g.py * g.nkx + kx0;
-    for (int it = threadIdx.x; it < N1 * tx; it += blockDim.x) {
-        const int k1 = p.fd_tx.div(it), col = it - k1 * tx;
+    for (int it = threadIdx.x; it < N1 * ncol; it += blockDim.x) {
+        int k1, col;
+        tile_item(p, ncol, it, k1, col);
         const float2 *line = buf + col * ls;
         float2 v[N2];
 #pragma unroll
         for (int n2 = 0; n2 < N2; ++n2) v[n2] = line[sk(k1 * N2 + n2)];
         dft_small<N2>(v, false);
-        if (col < ncol) {
 #pragma unroll
-            for (int k2 = 0; k2 < N2; ++k2) dst[(size_t)(k1 + N1 * k2) * g.nkx + col] = v[k2];
-        }
+        for (int k2 = 0; k2 < N2; ++k2) dst[(size_t)(k1 + N1 * k2) * g.nkx + col] = v[k2];
     }
 }
 
@@ -220,12 +231,12 @@ __global__ void __launch_bounds__(kThreads, 2) y_inverse_fused_kernel(const ColP
     const int z = blockIdx.y, c = blockIdx.z;
     const float2 *__restrict__ tw = p.plan.tw;
     const float2 *src = p.in + ((size_t)c * g.nz + z) * g.py * g.nkx + kx0;
-    for (int it = threadIdx.x; it < N1 * tx; it += blockDim.x) {
-        const int k1 = p.fd_tx.div(it), col = it - k1 * tx;
-        const bool okc = col < ncol;
+    for (int it = threadIdx.x; it < N1 * ncol; it += blockDim.x) {
+        int k1, col;
+        tile_item(p, ncol, it, k1, col);
         float2 v[N2];
 #pragma unroll
-        for (int k2 = 0; k2 < N2; ++k2) v[k2] = okc ? src[(size_t)(k1 + N1 * k2) * g.nkx + col] : make_float2(0.f, 0.f);
+        for (int k2 = 0; k2 < N2; ++k2) v[k2] = src[(size_t)(k1 + N1 * k2) * g.nkx + col];
         dft_small<N2>(v, true);
         float2 *line = buf + col * ls;
 #pragma unroll
@@ -234,16 +245,15 @@ __global__ void __launch_bounds__(kThreads, 2) y_inverse_fused_kernel(const ColP
     }
     __syncthreads();
     float2 *dst = p.out + ((size_t)c * g.nz + z) * g.ny * g.nkx + kx0;
-    for (int it = threadIdx.x; it < N2 * tx; it += blockDim.x) {
-        const int n2 = p.fd_tx.div(it), col = it - n2 * tx;
+    for (int it = threadIdx.x; it < N2 * ncol; it += blockDim.x) {
+        int n2, col;
+        tile_item(p, ncol, it, n2, col);
         float2 e[H1];
         half_idft_load<N1, N2>(e, n2, buf + col * ls, tw);
-        if (col < ncol) {
 #pragma unroll
-            for (int n1 = 0; n1 < H1; ++n1) {
-                const int y = N2 * n1 + n2;
-                if (y < g.ny) dst[(size_t)y * g.nkx + col] = e[n1];
-            }
+        for (int n1 = 0; n1 < H1; ++n1) {
+            const int y = N2 * n1 + n2;
+            if (y < g.ny) dst[(size_t)y * g.nkx + col] = e[n1];
         }
     }
 }
@@ -276,19 +286,19 @@ __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve
     const float2 *__restrict__ tw = p.plan.tw;        // e^{-2 pi i e / N}
 
     // phase 1: item (r2, z2, col), col fastest
-    const int n13 = np * 3 * N2 * tx;
+    const int n13 = np * 3 * N2 * ncol;
     for (int it = threadIdx.x; it < n13; it += blockDim.x) {
-        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        int rz, col;
+        tile_item(p, ncol, it, rz, col);
         const int z2 = rz & (N2 - 1), r2 = rz / N2;
         const int q = r2 >= 3, c = r2 - 3 * q;
         const int ky = q ? kyb : kya;
         const float2 *src = p.in + c * cstride + (size_t)ky * g.nkx + kx0 + col;
-        const bool okc = col < ncol;
         float2 e[H1];
 #pragma unroll
         for (int z1 = 0; z1 < H1; ++z1) {
             const int z = N2 * z1 + z2;
-            e[z1] = (okc && z < nz) ? src[(size_t)z * zstride] : make_float2(0.f, 0.f);
+            e[z1] = z < nz ? src[(size_t)z * zstride] : make_float2(0.f, 0.f);
         }
         half_dft_store<N1, N2>(e, z2, buf + (r2 * tx + col) * ls, tw);
     }
@@ -296,9 +306,10 @@ __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve
 
     // phase 2: item (q, k1, col), col fastest; all three components of one frequency column
     const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
-    const int n2 = np * N1 * tx;
+    const int n2 = np * N1 * ncol;
     for (int it = threadIdx.x; it < n2; it += blockDim.x) {
-        const int qk = p.fd_tx.div(it), col = it - qk * tx;
+        int qk, col;
+        tile_item(p, ncol, it, qk, col);
         const int k1 = qk & (N1 - 1), q = qk / N1;
         float2 m[3][N2];
 #pragma unroll
@@ -337,19 +348,18 @@ __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve
 
     // phase 3: item (r2, z2, col), col fastest; outputs z1 < N1/2 with z < nz
     for (int it = threadIdx.x; it < n13; it += blockDim.x) {
-        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        int rz, col;
+        tile_item(p, ncol, it, rz, col);
         const int z2 = rz & (N2 - 1), r2 = rz / N2;
         const int q = r2 >= 3, c = r2 - 3 * q;
         const int ky = q ? kyb : kya;
         float2 e[H1];
         half_idft_load<N1, N2>(e, z2, buf + (r2 * tx + col) * ls, tw);
-        if (col < ncol) {
-            float2 *dst = p.out + c * cstride + (size_t)ky * g.nkx + kx0 + col;
+        float2 *dst = p.out + c * cstride + (size_t)ky * g.nkx + kx0 + col;
 #pragma unroll
-            for (int z1 = 0; z1 < H1; ++z1) {
-                const int z = N2 * z1 + z2;
-                if (z < nz) dst[(size_t)z * zstride] = e[z1];
-            }
+        for (int z1 = 0; z1 < H1; ++z1) {
+            const int z = N2 * z1 + z2;
+            if (z < nz) dst[(size_t)z * zstride] = e[z1];
         }
     }
 }
@@ -411,27 +421,28 @@ __device__ __forceinline__ void yz_convolve_fused_body(const ColPass &p, const i
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
-    const int nz = g.nz, nl = 3 * nz * tx;
+    const int nz = g.nz, nl = 3 * nz * tx, nlive = 3 * nz * ncol;  // lines in the buffers / live lines
     float2 *A = reinterpret_cast<float2 *>(smem);
     float2 *B = A + (size_t)nl * ls;
     const size_t zstride = (size_t)g.ny * g.nkx, cstride = (size_t)nz * zstride;
     const float2 *__restrict__ tw = p.plan.tw;
-    for (int it = threadIdx.x; it < nl * N2; it += blockDim.x) {
-        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+    for (int it = threadIdx.x; it < nlive * N2; it += blockDim.x) {
+        int rest, col;
+        tile_item(p, ncol, it, rest, col);
         const int n2 = rest & (N2 - 1), cz = rest / N2;  // cz = c*nz + z
         const float2 *src = p.in + cz * zstride + kx0 + col;
-        const bool okc = col < ncol;
         float2 e[H1];
 #pragma unroll
         for (int y1 = 0; y1 < H1; ++y1) {
             const int y = N2 * y1 + n2;
-            e[y1] = (okc && y < g.ny) ? src[(size_t)y * g.nkx] : make_float2(0.f, 0.f);
+            e[y1] = y < g.ny ? src[(size_t)y * g.nkx] : make_float2(0.f, 0.f);
         }
         half_dft_store<N1, N2>(e, n2, A + (cz * tx + col) * ls, tw);
     }
     __syncthreads();
-    for (int it = threadIdx.x; it < nl * N1; it += blockDim.x) {
-        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+    for (int it = threadIdx.x; it < nlive * N1; it += blockDim.x) {
+        int rest, col;
+        tile_item(p, ncol, it, rest, col);
         const int k1 = rest & (N1 - 1), cz = rest / N1;
         const float2 *sl = A + (cz * tx + col) * ls;
         float2 v[N2];
@@ -444,8 +455,9 @@ __device__ __forceinline__ void yz_convolve_fused_body(const ColPass &p, const i
     }
     __syncthreads();
     const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
-    for (int it = threadIdx.x; it < N * tx; it += blockDim.x) {
-        const int ky = p.fd_tx.div(it), col = it - ky * tx;
+    for (int it = threadIdx.x; it < N * ncol; it += blockDim.x) {
+        int ky, col;
+        tile_item(p, ncol, it, ky, col);
         const int kx = min(kx0 + col, g.nkx - 1);
         float2 *line = B + (size_t)col * ls + sk(ky);
         const size_t lstride = (size_t)tx * ls;
@@ -454,8 +466,9 @@ __device__ __forceinline__ void yz_convolve_fused_body(const ColPass &p, const i
         else z_small_convolve<8>(line, lstride, nz, p.kern, kc, g.nky, g.nkx, ky, N, kx);
     }
     __syncthreads();
-    for (int it = threadIdx.x; it < nl * N1; it += blockDim.x) {
-        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+    for (int it = threadIdx.x; it < nlive * N1; it += blockDim.x) {
+        int rest, col;
+        tile_item(p, ncol, it, rest, col);
         const int k1 = rest & (N1 - 1), cz = rest / N1;
         const float2 *bl = B + (cz * tx + col) * ls;
         float2 v[N2];
@@ -467,8 +480,9 @@ __device__ __forceinline__ void yz_convolve_fused_body(const ColPass &p, const i
         for (int n2 = 0; n2 < N2; ++n2) sl[sk(k1 * N2 + n2)] = (n2 && k1) ? cmul(v[n2], cconj(__ldg(tw + n2 * k1))) : v[n2];
     }
     __syncthreads();
-    for (int it = threadIdx.x; it < nl * N2; it += blockDim.x) {
-        const int rest = p.fd_tx.div(it), col = it - rest * tx;
+    for (int it = threadIdx.x; it < nlive * N2; it += blockDim.x) {
+        int rest, col;
+        tile_item(p, ncol, it, rest, col);
         const int n2 = rest & (N2 - 1), cz = rest / N2;
         float2 e[H1];
         half_idft_load<N1, N2>(e, n2, A + (cz * tx + col) * ls, tw);
@@ -599,24 +613,25 @@ __device__ __forceinline__ void y_convolve_2d_fused_body(const ColPass &p, const
     const int tx = p.tx, kx0 = tile * tx, ncol = min(tx, g.nkx - kx0);
     const size_t cstride = (size_t)g.ny * g.nkx;
     const float2 *__restrict__ tw = p.plan.tw;
-    const int n13 = 3 * N2 * tx;
+    const int n13 = 3 * N2 * ncol;
     for (int it = threadIdx.x; it < n13; it += blockDim.x) {
-        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        int rz, col;
+        tile_item(p, ncol, it, rz, col);
         const int n2 = rz & (N2 - 1), c = rz / N2;
         const float2 *src = p.in + c * cstride + kx0 + col;
-        const bool okc = col < ncol;
         float2 e[H1];
 #pragma unroll
         for (int n1 = 0; n1 < H1; ++n1) {
             const int y = N2 * n1 + n2;
-            e[n1] = (okc && y < g.ny) ? src[(size_t)y * g.nkx] : make_float2(0.f, 0.f);
+            e[n1] = y < g.ny ? src[(size_t)y * g.nkx] : make_float2(0.f, 0.f);
         }
         half_dft_store<N1, N2>(e, n2, buf + (c * tx + col) * ls, tw);
     }
     __syncthreads();
     const size_t kc = (size_t)g.nky * g.nkx;
-    for (int it = threadIdx.x; it < N1 * tx; it += blockDim.x) {
-        const int k1 = p.fd_tx.div(it), col = it - k1 * tx;
+    for (int it = threadIdx.x; it < N1 * ncol; it += blockDim.x) {
+        int k1, col;
+        tile_item(p, ncol, it, k1, col);
         float2 m[3][N2];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -649,7 +664,8 @@ __device__ __forceinline__ void y_convolve_2d_fused_body(const ColPass &p, const
     }
     __syncthreads();
     for (int it = threadIdx.x; it < n13; it += blockDim.x) {
-        const int rz = p.fd_tx.div(it), col = it - rz * tx;
+        int rz, col;
+        tile_item(p, ncol, it, rz, col);
         const int n2 = rz & (N2 - 1), c = rz / N2;
         float2 e[H1];
         half_idft_load<N1, N2>(e, n2, buf + (c * tx + col) * ls, tw);

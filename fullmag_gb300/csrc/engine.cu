@@ -464,6 +464,7 @@ struct Engine {
         c.plan = plan;
         c.tx = tx;
         c.fd_tx = FastDiv((uint32_t)tx);
+        c.fd_last = FastDiv((uint32_t)(g.nkx % tx ? g.nkx % tx : tx));
         c.in = in;
         c.out = out;
         c.plan2 = plan_z;

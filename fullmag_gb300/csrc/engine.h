@@ -126,6 +126,7 @@ struct ColPass {
     FftPlan plan2;           // z plan of the fused y+z pass
     int tx;                  // kx columns per CTA
     FastDiv fd_tx;
+    FastDiv fd_last;         // live columns of the last kx tile: nkx % tx, or tx
     const float2 *in;
     float2 *out;
     const float *kern;       // demag kernel (multiply passes)
