@@ -770,7 +770,36 @@ struct Engine {
     bool dp45_pending = false;
     double dp45_dt = 0.0;
 
+    // Adaptive integrators share the attempt machinery below: DP45 and RK23 differ in
+    // their passes, the stored derivative handed to the next attempt (first-same-as-last)
+    // and the exponent of the step-size rule.
+    bool adaptive() const {
+        return integrator == FULLMAG_FDM_INTEGRATOR_DP45 || integrator == FULLMAG_FDM_INTEGRATOR_RK23;
+    }
+    int fsal_index() const { return integrator == FULLMAG_FDM_INTEGRATOR_RK23 ? 3 : 6; }
+    double ctrl_exp() const { return integrator == FULLMAG_FDM_INTEGRATOR_RK23 ? 1.0 / 3.0 : 0.2; }
+
+    // Bogacki-Shampine 3(2) with FSAL (native/backends/fdm/src/llg_rk23_fp32.cu:150-265):
+    // N(m0 + dt/2 k1), N(m0 + 3dt/4 k2), the proposal N(m0 + dt (2/9 k1 + 1/3 k2 + 4/9 k3))
+    // into S[1-cur], then k4 at the proposal with the error dt (-5/72 k1 + 1/12 k2 + 1/9 k3
+    // - 1/8 k4) and the statistics.
+    int enqueue_rk23(double dt, bool poll_between) {
+        static const double a2[1] = {0.5}, a3[1] = {0.75};
+        static const double b[3] = {2.0 / 9.0, 1.0 / 3.0, 4.0 / 9.0};
+        static const double e[4] = {-5.0 / 72.0, 1.0 / 12.0, 1.0 / 9.0, -1.0 / 8.0};
+        const int nxt = 1 - cur;
+        const int k1[1] = {0}, self[1] = {-1}, kb[3] = {0, 1, -1}, ke[4] = {0, 1, 2, -1};
+        if (!stage(nullptr, nullptr, 1, k1, a2, dt, A[0])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[0], K[1], 1, self, a3, dt, A[1])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        if (!stage(A[1], K[2], 3, kb, b, dt, S[nxt])) return -1;
+        if (poll_between && poll_hit()) return 1;
+        return final_eval(S[nxt], K[3], 4, ke, e, dt, false) ? 0 : -1;
+    }
+
     int enqueue_dp45(double dt, bool poll_between) {
+        if (integrator == FULLMAG_FDM_INTEGRATOR_RK23) return enqueue_rk23(dt, poll_between);
         static const double a21[1] = {1.0 / 5.0};
         static const double a3[2] = {3.0 / 40.0, 9.0 / 40.0};
         static const double a4[3] = {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0};
@@ -865,9 +894,9 @@ struct Engine {
         const double err = sqrt(hstats[8]);
         if (err <= max_error || dt <= dt_min) {
             double dt_next = dt_max;
-            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
-            // first-same-as-last: k7 at the accepted state is the next step's k1
-            if (cuda_fail("fsal copy", cudaMemcpyAsync(K[0], K[6], sizeof(float) * 3 * (size_t)g.n,
+            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
+            // first-same-as-last: the last derivative (at the accepted state) is the next step's k1
+            if (cuda_fail("fsal copy", cudaMemcpyAsync(K[0], K[fsal_index()], sizeof(float) * 3 * (size_t)g.n,
                                                        cudaMemcpyDeviceToDevice, stream)))
                 return -1;
             commit(dt, hstats);
@@ -875,7 +904,7 @@ struct Engine {
             next_dt = dt_next;
             return 1;
         }
-        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
         return 0;
     }
 
@@ -1007,6 +1036,7 @@ struct Engine {
         step_count += nsteps;
         time += h * (double)nsteps;
         k1_valid = fields_valid = stats_valid = false;
+        abm_restart();
         return eval_state(false) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
     }
 
@@ -1118,6 +1148,7 @@ struct Engine {
             if (hmap) cudaFree(hmap);
             hmap = nullptr;
             k1_valid = fields_valid = stats_valid = false;
+            abm_restart();
             return true;
         }
         if (!hmap && cuda_fail("cudaMalloc(field map)", cudaMalloc((void **)&hmap, sizeof(float) * vec3()))) return false;
@@ -1130,6 +1161,7 @@ struct Engine {
         if (cuda_fail("field map convert", cudaGetLastError())) return false;
         drop_graphs();  // captured passes hold the previous map pointer
         k1_valid = fields_valid = stats_valid = false;
+        abm_restart();
         return !cuda_fail("field map sync", cudaStreamSynchronize(stream));
     }
 
@@ -1199,7 +1231,7 @@ struct Engine {
         const double err = sqrt(st[8]);
         if (err <= max_error || dt <= dt_min) {
             double dt_next = dt_max;
-            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
             memcpy(stat_raw, st, sizeof(stat_raw));
             step_count += 1;
             time += dt;
@@ -1215,7 +1247,7 @@ struct Engine {
             return 1;
         }
         ctl->accept_prev = 0;
-        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, 0.2), dt_min), dt_max);
+        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
         return 0;
     }
 
@@ -1225,7 +1257,7 @@ struct Engine {
         ctl->accept_prev = 0;
         const size_t b = sizeof(float) * 3 * (size_t)g.n;
         return !cuda_fail("commit copy", cudaMemcpyAsync(S[0], S[1], b, cudaMemcpyDeviceToDevice, s)) &&
-               !cuda_fail("commit copy", cudaMemcpyAsync(K[0], K[6], b, cudaMemcpyDeviceToDevice, s));
+               !cuda_fail("commit copy", cudaMemcpyAsync(K[0], K[fsal_index()], b, cudaMemcpyDeviceToDevice, s));
     }
 
     int step_dp45(double dt) {
@@ -1240,11 +1272,67 @@ struct Engine {
         }
     }
 
+    // ---- Adams-Bashforth-Moulton 3 (native/backends/fdm/src/llg_abm3_fp32.cu:115-266) ----
+    // History f_n, f_{n-1}, f_{n-2} in K[abm_hist[0..2]], K[abm_kf] receives f at the
+    // prediction; the indices rotate instead of the buffers.  While fewer than three steps
+    // built the history, or when dt moved by more than 10 % since the last step, a step is
+    // a Heun step and f at its accepted state (K[0] after the final evaluation) becomes
+    // f_n.  Otherwise: predictor N(m + dt (23 f_n - 16 f_{n-1} + 5 f_{n-2})/12), f_s at the
+    // prediction, corrector N(m + dt (5 f_s + 8 f_n - f_{n-1})/12), and f_s becomes f_n.
+    // A new state or field map restarts the history (the reference keeps it).
+    int abm_startup = 0;
+    double abm_last_dt = 0.0;
+    int abm_hist[3] = {1, 2, 3}, abm_kf = 4;
+
+    void abm_restart() {
+        abm_startup = 0;
+        abm_last_dt = 0.0;
+    }
+
+    int step_abm3(double dt) {
+        if (abm_last_dt > 0.0 && std::fabs(dt - abm_last_dt) / abm_last_dt > 0.1) abm_startup = 0;
+        if (!ensure_k1()) return -1;
+        if (poll_hit()) return 1;
+        const int nxt = 1 - cur;
+        if (abm_startup < 3) {
+            const int rc = enqueue_fixed_step(dt, true);  // the Heun sequence (ends with K[0] = f at S[nxt])
+            if (rc != 0) return rc;
+            const int slot = abm_hist[2];
+            abm_hist[2] = abm_hist[1];
+            abm_hist[1] = abm_hist[0];
+            abm_hist[0] = slot;
+            if (cuda_fail("history copy",
+                          cudaMemcpyAsync(K[slot], K[0], sizeof(float) * 3 * (size_t)g.n, cudaMemcpyDeviceToDevice, stream)))
+                return -1;
+            abm_startup += 1;
+        } else {
+            const int kp[3] = {abm_hist[0], abm_hist[1], abm_hist[2]};
+            const double cp[3] = {23.0 / 12.0, -16.0 / 12.0, 5.0 / 12.0};
+            if (!stage(nullptr, nullptr, 3, kp, cp, dt, A[0])) return -1;
+            if (poll_hit()) return 1;
+            const int kc[3] = {-1, abm_hist[0], abm_hist[1]};
+            const double cc[3] = {5.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0};
+            if (!stage(A[0], K[abm_kf], 3, kc, cc, dt, S[nxt])) return -1;
+            if (poll_hit()) return 1;
+            if (!final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt, true)) return -1;
+            const int freed = abm_hist[2];
+            abm_hist[2] = abm_hist[1];
+            abm_hist[1] = abm_hist[0];
+            abm_hist[0] = abm_kf;
+            abm_kf = freed;
+        }
+        abm_last_dt = dt;
+        commit(dt, hstats);
+        return 0;
+    }
+
     int step(double dt) {
         interrupted = false;
         switch (integrator) {
             case FULLMAG_FDM_INTEGRATOR_RK4: return step_fixed(dt);
-            case FULLMAG_FDM_INTEGRATOR_DP45: return step_dp45(dt);
+            case FULLMAG_FDM_INTEGRATOR_DP45:
+            case FULLMAG_FDM_INTEGRATOR_RK23: return step_dp45(dt);
+            case FULLMAG_FDM_INTEGRATOR_ABM3: return step_abm3(dt);
             default: return step_fixed(dt);
         }
     }
@@ -1266,6 +1354,7 @@ struct Engine {
         if (cuda_fail("upload convert", cudaGetLastError())) return false;
         if (cuda_fail("upload sync", cudaStreamSynchronize(stream))) return false;
         k1_valid = false;
+        abm_restart();
         fields_valid = false;
         stats_valid = false;
         return true;
@@ -1276,6 +1365,7 @@ struct Engine {
     bool upload_noalloc(const double *m_xyz) {
         if (cuda_fail("upload (no allocation)", noalloc_upload_f64(device, m_xyz, g.n, S[cur], mask, stream))) return false;
         k1_valid = false;
+        abm_restart();
         fields_valid = false;
         stats_valid = false;
         return true;
@@ -1487,8 +1577,9 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     }
     if (unsupported(*this, plan->precision == FULLMAG_FDM_PRECISION_DOUBLE, "double precision state (use SINGLE)") ||
         unsupported(*this, integrator != FULLMAG_FDM_INTEGRATOR_HEUN && integrator != FULLMAG_FDM_INTEGRATOR_RK4 &&
-                               integrator != FULLMAG_FDM_INTEGRATOR_DP45,
-                    "integrators other than HEUN, RK4, DP45") ||
+                               integrator != FULLMAG_FDM_INTEGRATOR_DP45 && integrator != FULLMAG_FDM_INTEGRATOR_RK23 &&
+                               integrator != FULLMAG_FDM_INTEGRATOR_ABM3,
+                    "integrators other than HEUN, RK4, DP45, RK23, ABM3") ||
         unsupported(*this, plan->has_interfacial_dmi || plan->has_bulk_dmi, "DMI") ||
         unsupported(*this, plan->has_magnetoelastic != 0, "magnetoelastic coupling") ||
         unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
@@ -1617,7 +1708,15 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     }
 
     // ---- arena ----
-    nk = integrator == FULLMAG_FDM_INTEGRATOR_DP45 ? 7 : (integrator == FULLMAG_FDM_INTEGRATOR_RK4 ? 3 : 1);
+    // stage derivatives: DP45 k1..k7, RK23 k1..k4, RK4 k1..k3 (k4 stays in registers),
+    // ABM3 k1 + three history entries + f at the prediction, Heun k1
+    switch (integrator) {
+        case FULLMAG_FDM_INTEGRATOR_DP45: nk = 7; break;
+        case FULLMAG_FDM_INTEGRATOR_ABM3: nk = 5; break;
+        case FULLMAG_FDM_INTEGRATOR_RK23: nk = 4; break;
+        case FULLMAG_FDM_INTEGRATOR_RK4: nk = 3; break;
+        default: nk = 1; break;
+    }
     const char *rr_env = std::getenv("FULLMAG_FDM_ROWS_PER_CTA");
     row_rows = rr_env ? std::max(1, std::atoi(rr_env)) : std::max(1, std::min(16, 512 / std::max(1, g.nx)));
     max_row_blocks = g.ny * g.nz;  // statistics partials sized for one row per CTA
@@ -1958,7 +2057,7 @@ int fullmag_fdm_backend_step_many(fullmag_fdm_backend *handle, double dt_seconds
     Engine *e = eng(handle);
     if (!e || !out_stats || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     e->last_error.clear();
-    if (e->integrator == FULLMAG_FDM_INTEGRATOR_DP45) {
+    if (e->adaptive()) {
         e->last_error = "step_many supports fixed-step integrators only";
         return FULLMAG_FDM_ERR_INVALID;
     }
@@ -2714,10 +2813,12 @@ int fullmag_fdm_batch_step_until(fullmag_fdm_batch *batch, double t_end, double 
         // issue one attempt for every unfinished problem, then collect
         for (size_t i : active) {
             Engine *e = b->items[i];
-            const bool adaptive = e->integrator == FULLMAG_FDM_INTEGRATOR_DP45;
+            const bool adaptive = e->adaptive();
             const double want = adaptive ? b->next_dt[i] : dt0;
             const double d = std::min(want, t_end - e->time);
-            const int rc = adaptive ? e->begin_dp45_attempt(d) : e->begin_fixed_step(d);
+            // ABM3 steps synchronously (its history rotates on the host after each step)
+            const int rc = adaptive ? e->begin_dp45_attempt(d)
+                                    : e->integrator == FULLMAG_FDM_INTEGRATOR_ABM3 ? e->step(d) : e->begin_fixed_step(d);
             if (rc != 0) {
                 b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
                 return FULLMAG_FDM_ERR_CUDA;
@@ -2726,9 +2827,10 @@ int fullmag_fdm_batch_step_until(fullmag_fdm_batch *batch, double t_end, double 
         still.clear();
         for (size_t i : active) {
             Engine *e = b->items[i];
-            const bool adaptive = e->integrator == FULLMAG_FDM_INTEGRATOR_DP45;
+            const bool adaptive = e->adaptive();
             double nd = b->next_dt[i];
-            const int rc = adaptive ? e->finish_dp45_attempt(nd) : e->finish_fixed_step();
+            const int rc = adaptive ? e->finish_dp45_attempt(nd)
+                                    : e->integrator == FULLMAG_FDM_INTEGRATOR_ABM3 ? 0 : e->finish_fixed_step();
             if (rc < 0) {
                 b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
                 return FULLMAG_FDM_ERR_CUDA;

@@ -418,6 +418,10 @@ struct fo_problem {
     /* integrator buffers (AoS) */
     double *m0, *mst, *heff, *hscr, *k[7], *fsal;
     int fsal_valid;
+    /* ABM3 history f_n, f_{n-1}, f_{n-2} and its start-up state (llg_abm3_fp32.cu:115-266) */
+    double *abm_h[3];
+    int abm_startup;
+    double abm_last_dt;
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
     uint32_t *region; /* optional region ids */
     double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
@@ -444,7 +448,15 @@ void fo_destroy(fo_problem *pr) {
     free(pr->m0); free(pr->mst); free(pr->heff); free(pr->hscr); free(pr->fsal); free(pr->hmap);
     free(pr->region); free(pr->lut);
     for (int s = 0; s < 7; ++s) free(pr->k[s]);
+    for (int s = 0; s < 3; ++s) free(pr->abm_h[s]);
     free(pr);
+}
+
+/* A new state or field invalidates the FSAL derivative and the ABM3 history. */
+static void invalidate_history(fo_problem *pr) {
+    pr->fsal_valid = 0;
+    pr->abm_startup = 0;
+    pr->abm_last_dt = 0.0;
 }
 
 fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
@@ -472,6 +484,8 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     pr->m0 = dalloc(n3); pr->mst = dalloc(n3); pr->heff = dalloc(n3); pr->hscr = dalloc(n3);
     pr->fsal = dalloc(n3);
     for (int s = 0; s < 7; ++s) pr->k[s] = dalloc(n3);
+    if (p->integrator == 3)
+        for (int s = 0; s < 3; ++s) pr->abm_h[s] = dalloc(n3);
     norm3(p->u_axis, pr->u);
     norm3(p->c1, pr->c1);
     norm3(p->c2, pr->c2);
@@ -501,7 +515,7 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
 int fo_set_m(fo_problem *pr, const double *m_aos) {
     for (long i = 0; i < pr->n; ++i)
         for (int c = 0; c < 3; ++c) pr->m[3 * i + c] = active(pr, i) ? m_aos[3 * i + c] : 0.0;
-    pr->fsal_valid = 0;
+    invalidate_history(pr);
     return 0;
 }
 
@@ -520,7 +534,7 @@ int fo_set_field_map(fo_problem *pr, const double *h_aos) {
         for (long i = 0; i < pr->n; ++i)
             for (int c = 0; c < 3; ++c) pr->hmap[3 * i + c] = active(pr, i) ? h_aos[3 * i + c] : 0.0;
     }
-    pr->fsal_valid = 0;
+    invalidate_history(pr);
     return 0;
 }
 
@@ -837,18 +851,98 @@ static double dp45_error(const fo_problem *pr, double dt) {
 
 static double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+/* Heun from pr->m0 into pr->m (fdm_integrators.rs:87-153). */
+static void heun_step(fo_problem *pr, double dt) {
+    rhs_of(pr, pr->m0, pr->k[0]);
+    const double c1[1] = {1.0};
+    stage_combine(pr, pr->mst, pr->m0, 1, pr->k, c1, dt);
+    rhs_of(pr, pr->mst, pr->k[1]);
+    const double c2[2] = {0.5, 0.5};
+    stage_combine(pr, pr->m, pr->m0, 2, pr->k, c2, dt);
+}
+
+/* Bogacki-Shampine 3(2) error max_i dt |sum_j E_j k_j| over k1..k4 (the ABI's absolute
+ * max-norm; native/backends/fdm/src/llg_rk23_fp32.cu:78-94,218). */
+static const double BS_E[4] = {-5.0 / 72.0, 1.0 / 12.0, 1.0 / 9.0, -1.0 / 8.0};
+static double rk23_error(const fo_problem *pr, double dt) {
+    double mx = 0.0;
+#pragma omp parallel for reduction(max : mx) schedule(static)
+    for (long i = 0; i < pr->n; ++i) {
+        double e[3] = {0, 0, 0};
+        for (int s = 0; s < 4; ++s)
+            for (int c = 0; c < 3; ++c) e[c] += BS_E[s] * pr->k[s][3 * i + c];
+        const double en = dt * sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        if (en > mx) mx = en;
+    }
+    return mx;
+}
+
 int fo_step(fo_problem *pr, double dt, fo_stats *st) {
     const fo_params *p = &pr->p;
     const long n3 = 3 * pr->n;
     memcpy(pr->m0, pr->m, sizeof(double) * n3);
     double rejected = 0.0, suggested = 0.0;
     if (p->integrator == 1) { /* Heun: fdm_integrators.rs:87-153 */
-        rhs_of(pr, pr->m0, pr->k[0]);
-        const double c1[1] = {1.0};
-        stage_combine(pr, pr->mst, pr->m0, 1, pr->k, c1, dt);
-        rhs_of(pr, pr->mst, pr->k[1]);
-        const double c2[2] = {0.5, 0.5};
-        stage_combine(pr, pr->m, pr->m0, 2, pr->k, c2, dt);
+        heun_step(pr, dt);
+    } else if (p->integrator == 3) {
+        /* ABM3 with the GPU backend's start-up rule (llg_abm3_fp32.cu:115-266): a Heun
+         * step while fewer than 3 steps built the history or when dt moved by more than
+         * 10 %; then the Adams-Bashforth predictor, f at the prediction, the
+         * Adams-Moulton corrector.  The newest history entry is f at the accepted state
+         * after a Heun step and f at the prediction after an ABM3 step. */
+        if (pr->abm_last_dt > 0.0 && fabs(dt - pr->abm_last_dt) / pr->abm_last_dt > 0.1) pr->abm_startup = 0;
+        double **h = pr->abm_h;
+        if (pr->abm_startup < 3) {
+            heun_step(pr, dt);
+            double *t = h[2];
+            h[2] = h[1];
+            h[1] = h[0];
+            h[0] = t;
+            rhs_of(pr, pr->m, h[0]);
+            pr->abm_startup += 1;
+        } else {
+            double *hp[3] = {h[0], h[1], h[2]};
+            const double cp[3] = {23.0 / 12.0, -16.0 / 12.0, 5.0 / 12.0};
+            stage_combine(pr, pr->mst, pr->m0, 3, hp, cp, dt);
+            rhs_of(pr, pr->mst, pr->k[0]);
+            double *hc[3] = {pr->k[0], h[0], h[1]};
+            const double cc[3] = {5.0 / 12.0, 8.0 / 12.0, -1.0 / 12.0};
+            stage_combine(pr, pr->m, pr->m0, 3, hc, cc, dt);
+            double *t = h[2];
+            h[2] = h[1];
+            h[1] = h[0];
+            h[0] = t;
+            memcpy(h[0], pr->k[0], sizeof(double) * n3);
+        }
+        pr->abm_last_dt = dt;
+    } else if (p->integrator == 5) {
+        /* Bogacki-Shampine 3(2) + FSAL with the ABI's step control
+         * (llg_rk23_fp32.cu:150-265): stages N(m0 + dt/2 k1), N(m0 + 3dt/4 k2), solution
+         * N(m0 + dt (2/9 k1 + 1/3 k2 + 4/9 k3)), k4 at the solution. */
+        static const double B[3] = {2.0 / 9.0, 1.0 / 3.0, 4.0 / 9.0};
+        for (;;) {
+            if (pr->fsal_valid) memcpy(pr->k[0], pr->fsal, sizeof(double) * n3);
+            else rhs_of(pr, pr->m0, pr->k[0]);
+            const double a2[1] = {0.5}, a3[1] = {0.75};
+            stage_combine(pr, pr->mst, pr->m0, 1, &pr->k[0], a2, dt);
+            rhs_of(pr, pr->mst, pr->k[1]);
+            stage_combine(pr, pr->mst, pr->m0, 1, &pr->k[1], a3, dt);
+            rhs_of(pr, pr->mst, pr->k[2]);
+            stage_combine(pr, pr->mst, pr->m0, 3, pr->k, B, dt);
+            rhs_of(pr, pr->mst, pr->k[3]);
+            const double err = rk23_error(pr, dt);
+            if (err <= p->max_error || dt <= p->dt_min) {
+                memcpy(pr->m, pr->mst, sizeof(double) * n3);
+                memcpy(pr->fsal, pr->k[3], sizeof(double) * n3);
+                pr->fsal_valid = 1;
+                suggested = err > 0.0 ? clampd(p->headroom * dt * pow(p->max_error / err, 1.0 / 3.0), p->dt_min, p->dt_max)
+                                      : p->dt_max;
+                break;
+            }
+            rejected += 1.0;
+            dt = clampd(p->headroom * dt * pow(p->max_error / err, 1.0 / 3.0), p->dt_min, p->dt_max);
+            pr->fsal_valid = 0;
+        }
     } else if (p->integrator == 4) { /* RK4: fdm_integrators.rs:155-262 */
         rhs_of(pr, pr->m0, pr->k[0]);
         const double h[1] = {0.5}, f[1] = {1.0};
@@ -1018,7 +1112,7 @@ int fo_tangent_rk4(fo_problem *pr, double dt, uint64_t n_steps, const double *dh
     }
     memcpy(pr->m, y0, sizeof(double) * n3);
     if (dm_out) memcpy(dm_out, dy0, sizeof(double) * n3);
-    pr->fsal_valid = 0;
+    invalidate_history(pr);
     free(dy0); free(dys); free(ha); free(hb); free(dha); free(dhb); free(ynext); free(dynext);
     for (int s = 0; s < 4; ++s) free(dks[s]);
     return 0;

@@ -7,7 +7,8 @@
  *   crates/fullmag-fdm-demag/src/newell.rs      (Newell f/g, 27-point stencil, octants)
  *   crates/fullmag-engine/src/fdm_fft.rs        (zero-padded FFT convolution)
  *   crates/fullmag-engine/src/fdm_fields.rs     (exchange, demag, local terms, RHS, energies)
- *   crates/fullmag-engine/src/fdm_integrators.rs (Heun, RK4, Dormand-Prince 5(4))
+ *   crates/fullmag-engine/src/fdm_integrators.rs (Heun, RK4, Dormand-Prince 5(4)),
+ *   native/backends/fdm/src/llg_rk23_fp32.cu, llg_abm3_fp32.cu (RK23, ABM3 as the ABI runs them)
  * and the step/stat semantics of native/backends/fdm (the C ABI this engine replaces).
  * The reference's FFT comes from rustfft 6.4.1 (Cargo.lock:3647-3649), which is not
  * in the reference tree; fo_fft1d is an own mixed-radix FFT validated against numpy.fft.
@@ -41,7 +42,7 @@ int fo_fft3d(double *data, int px, int py, int pz, int inverse);
 /* ---- Problem ---- */
 typedef struct {
     int32_t nx, ny, nz;
-    int32_t integrator;          /* 1 Heun, 2 DP45, 4 RK4 (ABI values) */
+    int32_t integrator;          /* 1 Heun, 2 DP45, 3 ABM3, 4 RK4, 5 RK23 (ABI values) */
     double dx, dy, dz;
     double ms, a_ex, alpha, gamma;
     int32_t enable_exchange, enable_demag, has_external_field, disable_precession;

@@ -17,7 +17,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libfdm_oracle.so"
 
-HEUN, DP45, RK4 = 1, 2, 4
+HEUN, DP45, ABM3, RK4, RK23 = 1, 2, 3, 4, 5
 
 
 def build(force: bool = False) -> Path:

@@ -25,7 +25,8 @@ def make_pair(oracle, kw, integrator=_abi.INTEGRATOR_HEUN, thin=None, mask=None,
     if spectra and kw.get("enable_demag", True):
         sp = oracle.newell_spectra(nx, ny, nz, kw["dx"], kw["dy"], kw["dz"], thin_film_2d=thin)
     okw = dict(kw)
-    oint = {_abi.INTEGRATOR_HEUN: oracle.HEUN, _abi.INTEGRATOR_RK4: oracle.RK4, _abi.INTEGRATOR_DP45: oracle.DP45}[integrator]
+    oint = {_abi.INTEGRATOR_HEUN: oracle.HEUN, _abi.INTEGRATOR_RK4: oracle.RK4, _abi.INTEGRATOR_DP45: oracle.DP45,
+            _abi.INTEGRATOR_RK23: oracle.RK23, _abi.INTEGRATOR_ABM3: oracle.ABM3}[integrator]
     for k in ("adaptive_max_error",):
         okw.pop(k, None)
     orc = oracle.Problem(**okw, integrator=oint, active_mask=mask,
