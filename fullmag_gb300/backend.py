@@ -71,6 +71,8 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               ku1: Optional[float] = None, ku2: float = 0.0, u_axis=(0.0, 0.0, 1.0),
               kc1: Optional[float] = None, kc2: float = 0.0, kc3: float = 0.0,
               c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0),
+              dmi_d_interfacial: Optional[float] = None, dmi_d_bulk: Optional[float] = None,
+              mel_b1: Optional[float] = None, mel_b2: float = 0.0, mel_strain=(0.0,) * 6,
               active_mask: Optional[np.ndarray] = None,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
@@ -105,6 +107,13 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
     p.cubic_Kc1, p.cubic_Kc2, p.cubic_Kc3 = (kc1 or 0.0), kc2, kc3
     p.cubic_axis1[:] = list(c1)
     p.cubic_axis2[:] = list(c2)
+    p.has_interfacial_dmi = int(dmi_d_interfacial is not None)
+    p.dmi_D_interfacial = dmi_d_interfacial or 0.0
+    p.has_bulk_dmi = int(dmi_d_bulk is not None)
+    p.dmi_D_bulk = dmi_d_bulk or 0.0
+    p.has_magnetoelastic = int(mel_b1 is not None)
+    p.mel_b1, p.mel_b2 = (mel_b1 or 0.0), mel_b2
+    p.mel_strain[:] = list(mel_strain)
     p.sot_sigma[:] = [0.0, 0.0, 1.0]
     p.sot_thickness = 1e-9
     p.oersted_axis[:] = [0.0, 0.0, 1.0]

@@ -32,6 +32,9 @@
 namespace fm {
 
 static constexpr double kMu0 = 4.0 * M_PI * 1e-7;
+// device statistics slots: the kNumStats row-pass statistics, the step size of graph
+// replays, and the extra field pass's Zeeman sum m.(H_ext + H_map) and DMI energy density
+static constexpr int kStatSlots = kNumStats + 3;
 
 bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
                          std::string &err);
@@ -211,6 +214,12 @@ struct Engine {
     int nk = 0;
     float *h_ex = nullptr, *h_d = nullptr, *h_eff = nullptr;
     float *hmap = nullptr;  // per-cell applied field map (SoA, A/m), allocated on first use
+    // DMI / magnetoelastic terms: their pass writes hextra (with the field map added), which
+    // the right-hand-side row passes take as their field map; xpart holds its per-CTA sums
+    bool has_extra = false;
+    ExtraField xf{};
+    float *hextra = nullptr;
+    double2 *xpart = nullptr;
     float2 *X = nullptr, *Y = nullptr;
     float *kern = nullptr;
     uint8_t *mask = nullptr;
@@ -229,7 +238,7 @@ struct Engine {
     bool k1_valid = false, fields_valid = false, stats_valid = false;
     uint64_t step_count = 0;
     double time = 0.0;
-    double stat_raw[kNumStats] = {};
+    double stat_raw[kStatSlots] = {};
     fullmag_fdm_step_stats cur_stats{};
 
     fullmag_fdm_interrupt_poll_fn poll = nullptr;
@@ -254,6 +263,10 @@ struct Engine {
         adj_free();
         if (hmap) cudaFree(hmap);
         hmap = nullptr;
+        if (hextra) cudaFree(hextra);
+        if (xpart) cudaFree(xpart);
+        hextra = nullptr;
+        xpart = nullptr;
         if (arena) cudaFree(arena);
         arena = nullptr;
         if (staging) cudaFree(staging);
@@ -434,7 +447,30 @@ struct Engine {
         return !cuda_fail("adjoint row pass", rc);
     }
 
+    // The extra field pass for a right-hand side at p.m_in, enqueued before its row pass
+    // (with the energy sums when that pass collects statistics); p then takes its output
+    // as the field map.
+    bool run_extra(RowPass &p) {
+        if (!has_extra || !p.m_in) return true;
+        if (rec_rows) {
+            last_error = "DMI and magnetoelastic problems run outside batched rounds";
+            return false;
+        }
+        ExtraField q = xf;
+        q.g = g;
+        q.mask = mask;
+        q.m = p.m_in;
+        q.hmap = hmap;
+        q.out = hextra;
+        q.partials = p.partials ? xpart : nullptr;
+        launches += 1;
+        if (cuda_fail("extra field", launch_extra_field(q, stream))) return false;
+        p.hmap = hextra;
+        return true;
+    }
+
     bool run_row(RowPass &p) {
+        if (!run_extra(p)) return false;
         if (!demag) {
             p.x_in = nullptr;
             p.x_out = nullptr;
@@ -552,8 +588,13 @@ struct Engine {
         const cudaError_t rc = launch_finalize_stats(partials, row_blocks, dstats, stream);
         kt_end();
         if (cuda_fail("finalize", rc)) return false;
+        if (has_extra) {  // the extra pass before this evaluation left its per-CTA sums
+            launches += 1;
+            if (cuda_fail("extra finalize", launch_extra_finalize(xpart, extra_field_blocks(g), dstats + kNumStats + 1, stream)))
+                return false;
+        }
         return !cuda_fail("stats copy",
-                          cudaMemcpyAsync(hstats, dstats, sizeof(double) * kNumStats, cudaMemcpyDeviceToHost, stream));
+                          cudaMemcpyAsync(hstats, dstats, sizeof(double) * kStatSlots, cudaMemcpyDeviceToHost, stream));
     }
 
     bool read_stats() {
@@ -566,10 +607,13 @@ struct Engine {
         const double V = dx * dy * dz;
         st.exchange_energy_joules = exchange ? a_ex * V * d[0] : 0.0;
         st.demag_energy_joules = demag ? -0.5 * kMu0 * ms * V * d[1] : 0.0;
-        st.external_energy_joules = (has_ext || hmap) ? -kMu0 * ms * V * d[2] : 0.0;
+        // with an extra pass, the row pass's field-map sum includes its terms; the Zeeman
+        // sum m.(H_ext + H_map) then comes from the extra pass (slot kNumStats + 1)
+        const double zeeman = has_extra ? d[kNumStats + 1] : d[2];
+        st.external_energy_joules = (has_ext || hmap) ? -kMu0 * ms * V * zeeman : 0.0;
         st.anisotropy_energy_joules = has_uni ? -V * d[3] : 0.0;
         st.cubic_energy_joules = has_cub ? V * d[4] : 0.0;
-        st.dmi_energy_joules = 0.0;
+        st.dmi_energy_joules = has_extra ? V * d[kNumStats + 2] : 0.0;
         st.total_energy_joules = st.exchange_energy_joules + st.demag_energy_joules + st.external_energy_joules +
                                  st.anisotropy_energy_joules + st.cubic_energy_joules + st.dmi_energy_joules;
         st.max_effective_field_amplitude = sqrt(d[5]);
@@ -1008,6 +1052,10 @@ struct Engine {
             last_error = "adjoint_forward needs n_steps > 0 and dt > 0";
             return FULLMAG_FDM_ERR_INVALID;
         }
+        if (has_extra) {
+            last_error = "the adjoint does not support DMI or magnetoelastic terms";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
         if (C == 0) C = (uint32_t)std::max<uint64_t>(1, (uint64_t)std::ceil(std::sqrt((double)nsteps)));
         adj_free();
         adj_nsteps = nsteps;
@@ -1047,6 +1095,10 @@ struct Engine {
         }
         if (has_cub) {
             last_error = "the adjoint does not support cubic anisotropy";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
+        if (has_extra) {
+            last_error = "the adjoint does not support DMI or magnetoelastic terms";
             return FULLMAG_FDM_ERR_INVALID;
         }
         const size_t v3 = vec3();
@@ -1145,6 +1197,7 @@ struct Engine {
 
     bool set_field_map(const double *h_xyz) {
         if (!h_xyz) {
+            drop_graphs();  // captured passes hold the map pointer freed here
             if (hmap) cudaFree(hmap);
             hmap = nullptr;
             k1_valid = fields_valid = stats_valid = false;
@@ -1214,6 +1267,7 @@ struct Engine {
     bool record_attempt(const double *dt_ptr, std::vector<RowPass> &rows, std::vector<int> &cols) {
         rows.clear();
         cols.clear();
+        if (has_extra) return false;  // the extra field pass is not part of the batched rounds
         rec_rows = &rows;
         rec_cols = &cols;
         pass_dt_dev = dt_ptr;
@@ -1232,7 +1286,7 @@ struct Engine {
         if (err <= max_error || dt <= dt_min) {
             double dt_next = dt_max;
             if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
-            memcpy(stat_raw, st, sizeof(stat_raw));
+            memcpy(stat_raw, st, sizeof(double) * kNumStats);  // batched rounds carry no extra-field sums
             step_count += 1;
             time += dt;
             stats_valid = true;
@@ -1580,8 +1634,6 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                                integrator != FULLMAG_FDM_INTEGRATOR_DP45 && integrator != FULLMAG_FDM_INTEGRATOR_RK23 &&
                                integrator != FULLMAG_FDM_INTEGRATOR_ABM3,
                     "integrators other than HEUN, RK4, DP45, RK23, ABM3") ||
-        unsupported(*this, plan->has_interfacial_dmi || plan->has_bulk_dmi, "DMI") ||
-        unsupported(*this, plan->has_magnetoelastic != 0, "magnetoelastic coupling") ||
         unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
         unsupported(*this, plan->current_density_x != 0 || plan->current_density_y != 0 || plan->current_density_z != 0,
                     "spin-transfer torque") ||
@@ -1690,6 +1742,34 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     mat.alpha = (float)alpha;
     mat.prec = plan->disable_precession ? 0.f : 1.f;
 
+    // DMI and magnetoelastic terms (api.cpp plan mapping; demag_fp32.cu:319-376,582-583)
+    xf = ExtraField{};
+    xf.has_int = plan->has_interfacial_dmi ? 1 : 0;
+    xf.has_bulk = plan->has_bulk_dmi ? 1 : 0;
+    xf.has_mel = plan->has_magnetoelastic ? 1 : 0;
+    xf.has_ext = has_ext ? 1 : 0;
+    for (int c = 0; c < 3; ++c) xf.hext[c] = (float)hext[c];
+    xf.d_int = plan->dmi_D_interfacial;
+    xf.d_bulk = plan->dmi_D_bulk;
+    xf.dmi_int = (float)(2.0 * plan->dmi_D_interfacial / mu0ms);
+    xf.dmi_bulk = (float)(2.0 * plan->dmi_D_bulk / mu0ms);
+    xf.dinv2dx = 0.5 / dx;
+    xf.dinv2dy = 0.5 / dy;
+    xf.dinv2dz = 0.5 / dz;
+    xf.inv2dx = (float)xf.dinv2dx;
+    xf.inv2dy = (float)xf.dinv2dy;
+    xf.inv2dz = (float)xf.dinv2dz;
+    xf.mel_pref = (float)(-1.0 / mu0ms);
+    xf.b1 = (float)plan->mel_b1;
+    xf.b2 = (float)plan->mel_b2;
+    xf.e11 = (float)plan->mel_strain[0];
+    xf.e22 = (float)plan->mel_strain[1];
+    xf.e33 = (float)plan->mel_strain[2];
+    xf.e23 = (float)(0.5 * plan->mel_strain[3]);  // Voigt 2 e23 -> e23
+    xf.e13 = (float)(0.5 * plan->mel_strain[4]);
+    xf.e12 = (float)(0.5 * plan->mel_strain[5]);
+    has_extra = ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel);
+
     // ---- device and stream ----
     if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;
     if (cuda_fail("cudaStreamCreate", cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking))) return false;
@@ -1749,7 +1829,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     take(xlen); take(ylen); take(klen);                     // spectra + kernel
     take(has_mask ? (size_t)g.n : 0);                       // mask
     take(sizeof(float2) * kNumStats * (size_t)max_row_blocks);
-    take(sizeof(double) * (kNumStats + 1));
+    take(sizeof(double) * kStatSlots);
     take(sizeof(float2) * tw.size());
     arena_bytes = off;
     if (cuda_fail("cudaMalloc(arena)", cudaMalloc((void **)&arena, arena_bytes))) return false;
@@ -1774,9 +1854,13 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     partials = (float2 *)(arena + o[q++]);
     dstats = (double *)(arena + o[q++]);
     twid = (float2 *)(arena + o[q++]);
-    if (cuda_fail("cudaMallocHost(stats)", cudaMallocHost((void **)&hstats, sizeof(double) * kNumStats))) return false;
+    if (cuda_fail("cudaMallocHost(stats)", cudaMallocHost((void **)&hstats, sizeof(double) * kStatSlots))) return false;
+    if (has_extra &&
+        (cuda_fail("cudaMalloc(extra field)", cudaMalloc((void **)&hextra, sizeof(float) * 3 * (size_t)g.n)) ||
+         cuda_fail("cudaMalloc(extra sums)", cudaMalloc((void **)&xpart, sizeof(double2) * (size_t)extra_field_blocks(g)))))
+        return false;
     if (cuda_fail("cudaMallocHost(dt)", cudaMallocHost((void **)&dt_host, sizeof(double)))) return false;
-    dt_dev = dstats + kNumStats;  // the stats slot reserves one extra double for dt
+    dt_dev = dstats + kNumStats;  // slot kNumStats holds dt (kStatSlots)
 
     if (cuda_fail("cudaMemcpy(twiddles)", cudaMemcpyAsync(twid, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, stream)))
         return false;

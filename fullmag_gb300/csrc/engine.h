@@ -150,6 +150,32 @@ size_t z_convolve_smem(const Grid &g, int tx);
 size_t y_pass_smem(const Grid &g, int tx);
 size_t y_convolve_2d_smem(const Grid &g, int tx);
 
+// Field terms computed by a pass of their own before each right-hand-side row pass
+// (extra_field.cu): interfacial and bulk DMI (central differences, Neumann clamp, mask)
+// and the magnetoelastic field of a prescribed strain, plus the applied field map.  The
+// row pass adds `out` as its field map; H = 0 at inactive cells.
+struct ExtraField {
+    Grid g;
+    const uint8_t *mask;
+    const float *m;            // stage input (SoA)
+    const float *hmap;         // applied field map or NULL
+    float *out;                // H_extra (SoA)
+    double2 *partials;         // NULL: no sums; else per CTA (Zeeman sum m.(H_ext + H_map), DMI energy density sum)
+    int has_ext;               // uniform applied field hext (A/m) in the Zeeman sum
+    float hext[3];
+    int has_int, has_bulk, has_mel;
+    float dmi_int, dmi_bulk;   // 2 D / (mu0 Ms), A/m per unit gradient
+    double d_int, d_bulk;      // D (J/m^2) for the energy sums
+    float inv2dx, inv2dy, inv2dz;     // 1/(2 d) for the field
+    double dinv2dx, dinv2dy, dinv2dz; // 1/(2 d) for the energy sums
+    float mel_pref;            // -1 / (mu0 Ms)
+    float b1, b2, e11, e22, e33, e23, e13, e12;  // B1, B2 (J/m^3), strain tensor (e_ij, i != j halved Voigt)
+};
+int extra_field_blocks(const Grid &g);
+cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);
+// sums the per-CTA partials into out[0], out[1] (fixed order)
+cudaError_t launch_extra_finalize(const double2 *partials, int nblocks, double *out, cudaStream_t s);
+
 // Adjoint (reverse-mode RK4): the final-combination pass (adjoint.cu); all fields SoA.
 // The local VJP and the stage update are the row pass's adjoint modes.
 struct AdjFinal {

@@ -663,6 +663,83 @@ static void rhs_cell(const fo_params *p, const double *m, const double *h, doubl
 }
 
 /* Full field evaluation: effective_field_into_ws (fdm_fields.rs:1153-1182). */
+/* Neighbours x-, x+, y-, y+, z-, z+ of cell i with the Neumann clamp and the active mask
+ * (a missing or inactive neighbour is the cell itself; demag_fp32.cu:324-340). */
+static void clamped_neighbours(const fo_problem *pr, long i, long nb[6]) {
+    const fo_params *p = &pr->p;
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+    const long sxy = (long)nx * ny;
+    nb[0] = x > 0 ? i - 1 : i;
+    nb[1] = x < nx - 1 ? i + 1 : i;
+    nb[2] = y > 0 ? i - nx : i;
+    nb[3] = y < ny - 1 ? i + nx : i;
+    nb[4] = z > 0 ? i - sxy : i;
+    nb[5] = z < nz - 1 ? i + sxy : i;
+    for (int q = 0; q < 6; ++q)
+        if (!active(pr, nb[q])) nb[q] = i;
+}
+
+/* Central differences d m_c / d axis over 2 d with the clamped neighbours: g[c][axis]. */
+static void central_gradient(const fo_problem *pr, const double *m, long i, double g[3][3]) {
+    const fo_params *p = &pr->p;
+    long nb[6];
+    clamped_neighbours(pr, i, nb);
+    const double inv[3] = {0.5 / p->dx, 0.5 / p->dy, 0.5 / p->dz};
+    for (int c = 0; c < 3; ++c)
+        for (int a = 0; a < 3; ++a) g[c][a] = (m[3 * nb[2 * a + 1] + c] - m[3 * nb[2 * a] + c]) * inv[a];
+}
+
+/* DMI and magnetoelastic field at active cell i added to h (demag_fp32.cu:319-376):
+ * interfacial 2D/(mu0 Ms) (dmz/dx, dmz/dy, -(dmx/dx + dmy/dy)), bulk 2D/(mu0 Ms) curl m,
+ * magnetoelastic -1/(mu0 Ms) (2 B1 m_i e_ii + B2 sum_{j != i} m_j e_ij). */
+static void dmi_mel_field_cell(const fo_problem *pr, const double *m, long i, double *h) {
+    const fo_params *p = &pr->p;
+    if (p->ms <= 0.0) return;
+    if (p->has_interfacial_dmi || p->has_bulk_dmi) {
+        double g[3][3];
+        central_gradient(pr, m, i, g);
+        const double pf = 2.0 / (FO_MU0 * p->ms);
+        if (p->has_interfacial_dmi) {
+            const double k = pf * p->dmi_d_interfacial;
+            h[0] += k * g[2][0];
+            h[1] += k * g[2][1];
+            h[2] -= k * (g[0][0] + g[1][1]);
+        }
+        if (p->has_bulk_dmi) {
+            const double k = pf * p->dmi_d_bulk;
+            h[0] += k * (g[2][1] - g[1][2]);
+            h[1] += k * (g[0][2] - g[2][0]);
+            h[2] += k * (g[1][0] - g[0][1]);
+        }
+    }
+    if (p->has_magnetoelastic) {
+        const double *mi = m + 3 * i;
+        const double a = -1.0 / (FO_MU0 * p->ms), b1 = p->mel_b1, b2 = p->mel_b2;
+        const double e11 = p->mel_strain[0], e22 = p->mel_strain[1], e33 = p->mel_strain[2];
+        const double e23 = 0.5 * p->mel_strain[3], e13 = 0.5 * p->mel_strain[4], e12 = 0.5 * p->mel_strain[5];
+        h[0] += a * (2.0 * b1 * mi[0] * e11 + b2 * (mi[1] * e12 + mi[2] * e13));
+        h[1] += a * (2.0 * b1 * mi[1] * e22 + b2 * (mi[0] * e12 + mi[2] * e23));
+        h[2] += a * (2.0 * b1 * mi[2] * e33 + b2 * (mi[0] * e13 + mi[1] * e23));
+    }
+}
+
+/* DMI energy density at active cell i (reductions_fp64.cu:647-710): interfacial
+ * D [mz (dmx/dx + dmy/dy) - mx dmz/dx - my dmz/dy], bulk D m.(curl m). */
+static double dmi_energy_cell(const fo_problem *pr, const double *m, long i) {
+    const fo_params *p = &pr->p;
+    if (!(p->has_interfacial_dmi || p->has_bulk_dmi)) return 0.0;
+    double g[3][3];
+    central_gradient(pr, m, i, g);
+    const double *mi = m + 3 * i;
+    double e = 0.0;
+    if (p->has_interfacial_dmi)
+        e += p->dmi_d_interfacial * (mi[2] * (g[0][0] + g[1][1]) - mi[0] * g[2][0] - mi[1] * g[2][1]);
+    if (p->has_bulk_dmi)
+        e += p->dmi_d_bulk * (mi[0] * (g[2][1] - g[1][2]) + mi[1] * (g[0][2] - g[2][0]) + mi[2] * (g[1][0] - g[0][1]));
+    return e;
+}
+
 static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h_d, double *h_eff,
                         double *rhs) {
     const fo_params *p = &pr->p;
@@ -680,6 +757,7 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
             if (pr->hmap)
                 for (int c = 0; c < 3; ++c) h[c] += pr->hmap[3 * i + c];
             anis_field_cell(pr, m + 3 * i, h);
+            dmi_mel_field_cell(pr, m, i, h);
         }
         for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
         if (rhs) rhs_cell(p, m + 3 * i, h, rhs + 3 * i);
@@ -723,11 +801,12 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
     const double V = p->dx * p->dy * p->dz;
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     const double ix2 = 1.0 / (p->dx * p->dx), iy2 = 1.0 / (p->dy * p->dy), iz2 = 1.0 / (p->dz * p->dz);
-    double epair = 0.0, exf = 0.0, ed = 0.0, eext = 0.0, euni = 0.0, ecub = 0.0, eacpu = 0.0;
-#pragma omp parallel for reduction(+ : epair, exf, ed, eext, euni, ecub, eacpu) schedule(static)
+    double epair = 0.0, exf = 0.0, ed = 0.0, eext = 0.0, euni = 0.0, ecub = 0.0, eacpu = 0.0, edmi = 0.0;
+#pragma omp parallel for reduction(+ : epair, exf, ed, eext, euni, ecub, eacpu, edmi) schedule(static)
     for (long i = 0; i < pr->n; ++i) {
         if (!active(pr, i)) continue;
         const double *mi = m + 3 * i;
+        edmi += V * dmi_energy_cell(pr, m, i);
         const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
         if (p->enable_exchange) {
             long nb[3] = {x + 1 < nx ? i + 1 : -1, y + 1 < ny ? i + nx : -1, z + 1 < nz ? i + (long)nx * ny : -1};
@@ -773,7 +852,8 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
     st->e_uniaxial = euni;
     st->e_cubic = ecub;
     st->e_anis_cpu = eacpu;
-    st->e_total = epair + ed + eext + euni + ecub;
+    st->e_dmi = edmi;
+    st->e_total = epair + ed + eext + euni + ecub + edmi;
     st->max_h_eff = vmax_norm(h_eff, pr->n);
     st->max_h_demag = p->enable_demag ? vmax_norm(h_d, pr->n) : 0.0;
     st->max_rhs = vmax_norm(rhs, pr->n);

@@ -62,6 +62,13 @@ typedef struct {
      * it), copied at create; native/backends/fdm/src/exchange_fp32.cu:48-104, api.cpp:405-420 */
     const uint32_t *region_mask;
     const double *exchange_lut;
+    /* DMI (J/m^2) and magnetoelastic coupling (B1, B2 in J/m^3, Voigt strain e11 e22 e33
+     * 2e23 2e13 2e12): native/backends/fdm/src/demag_fp32.cu:319-376,582-583 */
+    int32_t has_interfacial_dmi, has_bulk_dmi;
+    double dmi_d_interfacial, dmi_d_bulk;
+    int32_t has_magnetoelastic, pad1;
+    double mel_b1, mel_b2;
+    double mel_strain[6];
 } fo_params;
 
 #define FO_MAX_REGIONS 256
@@ -75,9 +82,10 @@ typedef struct {
     double e_uniaxial;           /* -V sum (Ku1 (m.u)^2 + Ku2 (m.u)^4)  (C ABI convention) */
     double e_cubic;              /* V sum (Kc1 s + Kc2 p + Kc3 s^2)    (C ABI convention) */
     double e_anis_cpu;           /* -1/2 mu0 Ms V sum m.H_anis          (CPU reference convention) */
-    double e_total;              /* e_exchange + e_demag + e_external + e_uniaxial + e_cubic */
+    double e_total;              /* e_exchange + e_demag + e_external + e_uniaxial + e_cubic + e_dmi */
     double max_h_eff, max_h_demag, max_rhs;
     double rejected_attempts;
+    double e_dmi;                /* V sum of the DMI energy densities (reductions_fp64.cu:647-720 forms) */
 } fo_stats;
 
 typedef struct fo_problem fo_problem;

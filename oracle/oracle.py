@@ -46,6 +46,10 @@ class Params(C.Structure):
         ("dp45_norm", C.c_int32), ("pad0", C.c_int32),
         ("active_mask", C.c_void_p),
         ("region_mask", C.c_void_p), ("exchange_lut", C.c_void_p),
+        ("has_interfacial_dmi", C.c_int32), ("has_bulk_dmi", C.c_int32),
+        ("dmi_d_interfacial", C.c_double), ("dmi_d_bulk", C.c_double),
+        ("has_magnetoelastic", C.c_int32), ("pad1", C.c_int32),
+        ("mel_b1", C.c_double), ("mel_b2", C.c_double), ("mel_strain", C.c_double * 6),
     ]
 
 
@@ -53,7 +57,7 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "step", "time", "dt_used", "suggested_next_dt",
         "e_exchange", "e_exchange_field", "e_demag", "e_external", "e_uniaxial", "e_cubic",
-        "e_anis_cpu", "e_total", "max_h_eff", "max_h_demag", "max_rhs", "rejected_attempts")]
+        "e_anis_cpu", "e_total", "max_h_eff", "max_h_demag", "max_rhs", "rejected_attempts", "e_dmi")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -147,7 +151,8 @@ class Problem:
                  kc1=None, kc2=0.0, kc3=0.0, c1=(1, 0, 0), c2=(0, 1, 0),
                  max_error=1e-5, dt_min=1e-18, dt_max=1e-10, headroom=0.8, rtol=0.0,
                  growth_limit=float("inf"), shrink_limit=0.0, dp45_norm=0,
-                 active_mask=None, m0=None, region_mask=None, exchange_lut=None):
+                 active_mask=None, m0=None, region_mask=None, exchange_lut=None,
+                 dmi_d_interfacial=None, dmi_d_bulk=None, mel_b1=None, mel_b2=0.0, mel_strain=(0.0,) * 6):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -166,6 +171,13 @@ class Problem:
         p.max_error, p.dt_min, p.dt_max, p.headroom = max_error, dt_min, dt_max, headroom
         p.rtol, p.growth_limit, p.shrink_limit = rtol, growth_limit, shrink_limit
         p.dp45_norm = dp45_norm
+        p.has_interfacial_dmi = int(dmi_d_interfacial is not None)
+        p.dmi_d_interfacial = dmi_d_interfacial or 0.0
+        p.has_bulk_dmi = int(dmi_d_bulk is not None)
+        p.dmi_d_bulk = dmi_d_bulk or 0.0
+        p.has_magnetoelastic = int(mel_b1 is not None)
+        p.mel_b1, p.mel_b2 = (mel_b1 or 0.0), mel_b2
+        p.mel_strain[:] = list(mel_strain)
         self._mask = None
         if active_mask is not None:
             self._mask = np.ascontiguousarray(active_mask, dtype=np.uint8)
