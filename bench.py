@@ -98,8 +98,8 @@ def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
 # the timed steps (profiles/launches_volume_256x256x64_rk4.md)
-NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 455.9e6, ("volume_256x256x64_rk4", "y_inverse"): 276.1e6,
-               ("volume_256x256x64_rk4", "y_forward"): 244.9e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6}
+NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 457.4e6, ("volume_256x256x64_rk4", "y_inverse"): 274.0e6,
+               ("volume_256x256x64_rk4", "y_forward"): 242.6e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6}
 
 
 WORKLOADS = {
