@@ -73,6 +73,10 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0),
               dmi_d_interfacial: Optional[float] = None, dmi_d_bulk: Optional[float] = None,
               mel_b1: Optional[float] = None, mel_b2: float = 0.0, mel_strain=(0.0,) * 6,
+              current_density=(0.0, 0.0, 0.0), stt_degree: float = 0.0, stt_beta: float = 0.0,
+              stt_p=(0.0, 0.0, 0.0), stt_lambda: float = 0.0, stt_epsilon_prime: float = 0.0,
+              sot_je: Optional[float] = None, sot_xi_dl: float = 0.0, sot_xi_fl: float = 0.0,
+              sot_sigma=(0.0, 0.0, 1.0), sot_thickness: float = 0.0,
               active_mask: Optional[np.ndarray] = None,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
@@ -114,6 +118,14 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
     p.has_magnetoelastic = int(mel_b1 is not None)
     p.mel_b1, p.mel_b2 = (mel_b1 or 0.0), mel_b2
     p.mel_strain[:] = list(mel_strain)
+    p.current_density_x, p.current_density_y, p.current_density_z = current_density
+    p.stt_degree, p.stt_beta = stt_degree, stt_beta
+    p.stt_p_x, p.stt_p_y, p.stt_p_z = stt_p
+    p.stt_lambda, p.stt_epsilon_prime = stt_lambda, stt_epsilon_prime
+    p.has_sot = int(sot_je is not None)
+    p.sot_je, p.sot_xi_dl, p.sot_xi_fl = (sot_je or 0.0), sot_xi_dl, sot_xi_fl
+    p.sot_sigma[:] = list(sot_sigma)
+    p.sot_thickness = sot_thickness
     p.sot_sigma[:] = [0.0, 0.0, 1.0]
     p.sot_thickness = 1e-9
     p.oersted_axis[:] = [0.0, 0.0, 1.0]

@@ -217,6 +217,8 @@ struct Engine {
     // DMI / magnetoelastic terms: their pass writes hextra (with the field map added), which
     // the right-hand-side row passes take as their field map; xpart holds its per-CTA sums
     bool has_extra = false;
+    bool has_torque = false;   // spin torques among the extra terms
+    bool torques_off = false;  // set while an observable pass runs
     ExtraField xf{};
     float *hextra = nullptr;
     double2 *xpart = nullptr;
@@ -463,6 +465,7 @@ struct Engine {
         q.hmap = hmap;
         q.out = hextra;
         q.partials = p.partials ? xpart : nullptr;
+        q.torques = torques_off ? 0 : 1;
         launches += 1;
         if (cuda_fail("extra field", launch_extra_field(q, stream))) return false;
         p.hmap = hextra;
@@ -624,6 +627,24 @@ struct Engine {
     // RHS at the committed state -> K[0], statistics, optionally observables.
     bool eval_state(bool write_fields) {
         if (!pass_forward(S[cur])) return false;
+        bool fields_written = false;
+        if (write_fields && has_torque) {
+            // the observables leave the spin torques out (they are not fields in the
+            // reference): one pass writes them without the torque terms, the next computes
+            // k1 and the statistics with them
+            RowPass q = row_base();
+            q.x_in = X;
+            q.m_in = S[cur];
+            q.h_ex_out = h_ex;
+            q.h_d_out = h_d;
+            q.h_eff_out = h_eff;
+            torques_off = true;
+            const bool ok = run_row(q);
+            torques_off = false;
+            if (!ok) return false;
+            write_fields = false;
+            fields_written = true;
+        }
         RowPass p = row_base();
         p.x_in = X;
         p.m_in = S[cur];
@@ -639,7 +660,7 @@ struct Engine {
         memcpy(stat_raw, hstats, sizeof(stat_raw));
         k1_valid = true;
         stats_valid = true;
-        if (write_fields) fields_valid = true;
+        if (write_fields || fields_written) fields_valid = true;
         fill_stats(stat_raw, cur_stats);
         cur_stats.step = step_count;
         cur_stats.time_seconds = time;
@@ -1635,9 +1656,6 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                                integrator != FULLMAG_FDM_INTEGRATOR_ABM3,
                     "integrators other than HEUN, RK4, DP45, RK23, ABM3") ||
         unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
-        unsupported(*this, plan->current_density_x != 0 || plan->current_density_y != 0 || plan->current_density_z != 0,
-                    "spin-transfer torque") ||
-        unsupported(*this, plan->has_sot != 0, "spin-orbit torque") ||
         unsupported(*this, plan->has_oersted_cylinder != 0, "Oersted field") ||
         unsupported(*this, plan->region_mask != nullptr, "region masks / exchange LUT") ||
         unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers") ||
@@ -1768,7 +1786,55 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     xf.e23 = (float)(0.5 * plan->mel_strain[3]);  // Voigt 2 e23 -> e23
     xf.e13 = (float)(0.5 * plan->mel_strain[4]);
     xf.e12 = (float)(0.5 * plan->mel_strain[5]);
-    has_extra = ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel);
+    // spin torques (prefactors as api.cpp:250-300 and context.hpp:321-339 compute them)
+    {
+        const double MU_B = 9.274009994e-24, E_CH = 1.60217662e-19, HBAR = 1.054571817e-34;
+        const double j[3] = {plan->current_density_x, plan->current_density_y, plan->current_density_z};
+        const bool has_j = j[0] != 0.0 || j[1] != 0.0 || j[2] != 0.0;
+        xf.has_zl = has_j && plan->stt_degree > 0.0 && ms > 0.0;
+        if (xf.has_zl) {
+            const double b = plan->stt_degree * MU_B / (E_CH * ms * (1.0 + plan->stt_beta * plan->stt_beta));
+            for (int c = 0; c < 3; ++c) xf.zl_u[c] = (float)(b * j[c]);
+            xf.zl_beta = (float)plan->stt_beta;
+        }
+        xf.inv_dx = (float)(1.0 / dx);
+        xf.inv_dy = (float)(1.0 / dy);
+        xf.inv_dz = (float)(1.0 / dz);
+        const double p2 = plan->stt_p_x * plan->stt_p_x + plan->stt_p_y * plan->stt_p_y + plan->stt_p_z * plan->stt_p_z;
+        xf.has_slon = p2 > 0.0 && plan->stt_lambda > 0.0 && has_j && ms > 0.0 && dz > 0.0;
+        if (xf.has_slon) {
+            const double js = sqrt(j[0] * j[0] + j[1] * j[1] + j[2] * j[2]);
+            xf.slon_pf = (float)(js * HBAR / (2.0 * E_CH * kMu0 * ms * dz));
+            xf.slon_P = (float)(plan->stt_degree > 0.0 ? plan->stt_degree : 1.0);
+            xf.slon_l2 = (float)(plan->stt_lambda * plan->stt_lambda);
+            xf.slon_eps = (float)plan->stt_epsilon_prime;
+            xf.slon_p[0] = (float)plan->stt_p_x;
+            xf.slon_p[1] = (float)plan->stt_p_y;
+            xf.slon_p[2] = (float)plan->stt_p_z;
+        }
+        xf.has_sot = plan->has_sot != 0 && ms > 0.0;
+        if (xf.has_sot) {
+            const double t = plan->sot_thickness > 0.0 ? plan->sot_thickness : 1.0e-9;
+            const double *sg = plan->sot_sigma;
+            const double len = sqrt(sg[0] * sg[0] + sg[1] * sg[1] + sg[2] * sg[2]);
+            const double inv = len > 1e-30 ? 1.0 / len : 0.0;
+            for (int c = 0; c < 3; ++c) xf.sot_s[c] = (float)(sg[c] * inv);
+            xf.sot_amp = (float)(std::fabs(plan->sot_je) * HBAR / (2.0 * E_CH * kMu0 * ms * t));
+            xf.sot_xi_dl = (float)plan->sot_xi_dl;
+            xf.sot_xi_fl = (float)plan->sot_xi_fl;
+        }
+        has_torque = xf.has_zl || xf.has_slon || xf.has_sot;
+        const double s = plan->disable_precession ? 0.0 : 1.0, gb = gamma / (1.0 + alpha * alpha);
+        if (has_torque && s + alpha * alpha <= 0.0) {
+            last_error = "spin torques need precession or damping (disable_precession with alpha = 0)";
+            return false;
+        }
+        if (has_torque) {
+            xf.tq_a = (float)(alpha / (gb * (s + alpha * alpha)));
+            xf.tq_b = (float)(s / (gb * (s + alpha * alpha)));
+        }
+    }
+    has_extra = ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque);
 
     // ---- device and stream ----
     if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;

@@ -170,6 +170,16 @@ struct ExtraField {
     double dinv2dx, dinv2dy, dinv2dz; // 1/(2 d) for the energy sums
     float mel_pref;            // -1 / (mu0 Ms)
     float b1, b2, e11, e22, e33, e23, e13, e12;  // B1, B2 (J/m^3), strain tensor (e_ij, i != j halved Voigt)
+    // spin torques T (added to dm/dt by the reference) enter as the field H = a T + b m x T,
+    // which the LLG right-hand side maps back to T for T perpendicular to m:
+    // a = alpha / (gbar (s + alpha^2)), b = s / (gbar (s + alpha^2)), s = 1 with precession
+    int torques;               // 0: leave the torque terms out (observable passes)
+    int has_zl, has_slon, has_sot;
+    float zl_u[3], zl_beta;    // Zhang-Li drift velocity (m/s) and non-adiabaticity
+    float inv_dx, inv_dy, inv_dz;
+    float slon_pf, slon_P, slon_l2, slon_eps, slon_p[3];  // Slonczewski
+    float sot_amp, sot_xi_dl, sot_xi_fl, sot_s[3];        // spin-orbit torque
+    float tq_a, tq_b;
 };
 int extra_field_blocks(const Grid &g);
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);

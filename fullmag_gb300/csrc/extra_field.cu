@@ -8,6 +8,11 @@
 //   magnetoelastic field (B1, B2, prescribed strain; shear strains halved from Voigt)
 //                                               native/backends/fdm/src/demag_fp32.cu:368-376,582-583
 //   DMI energy (FP64 sums of the FP32 state)    native/backends/fdm/src/reductions_fp64.cu:647-720
+//   Zhang-Li and Slonczewski spin-transfer torque, spin-orbit torque
+//                                               native/backends/fdm/src/llg_fp32.cu:65-195
+//                                               prefactors api.cpp:250-300, context.hpp:321-339
+// A torque T perpendicular to m is passed as the field H = a T + b (m x T), which the row
+// pass's LLG right-hand side maps back to exactly T; m.H = 0, so it adds no energy.
 // The reference reports the bulk DMI energy as +V D m.(curl m) while its field is
 // +2D/(mu0 Ms) curl m; both are kept as they are, so the energy is summed from its own
 // formula, not from m.H.  The row pass adds this pass's output as its field map, so its
@@ -93,6 +98,60 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                 ax += p.mel_pref * (2.f * p.b1 * mx * p.e11 + p.b2 * (my * p.e12 + mz * p.e13));
                 ay += p.mel_pref * (2.f * p.b1 * my * p.e22 + p.b2 * (mx * p.e12 + mz * p.e23));
                 az += p.mel_pref * (2.f * p.b1 * mz * p.e33 + p.b2 * (mx * p.e13 + my * p.e23));
+            }
+            if (p.torques && (p.has_zl || p.has_slon || p.has_sot)) {
+                float tx = 0.f, ty = 0.f, tz = 0.f;
+                if (p.has_zl) {
+                    // D = (u.grad) m by upwind differences: the upwind neighbour when it
+                    // exists, read without the mask (native/backends/fdm/src/llg_fp32.cu:65-140)
+                    const long long r = i / g.nx;
+                    const int pos[3] = {(int)(i % g.nx), (int)(r % g.ny), (int)(r / g.ny)};
+                    const int ext[3] = {g.nx, g.ny, g.nz};
+                    const long long st[3] = {1, g.nx, (long long)g.nx * g.ny};
+                    const float inv[3] = {p.inv_dx, p.inv_dy, p.inv_dz};
+                    float Dx = 0.f, Dy = 0.f, Dz = 0.f;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const float u = p.zl_u[a];
+                        if (u > 0.f && pos[a] > 0) {
+                            const long long q = i - st[a];
+                            Dx += u * (mx - m[q]) * inv[a];
+                            Dy += u * (my - m[n + q]) * inv[a];
+                            Dz += u * (mz - m[2 * n + q]) * inv[a];
+                        } else if (u < 0.f && pos[a] < ext[a] - 1) {
+                            const long long q = i + st[a];
+                            Dx += u * (m[q] - mx) * inv[a];
+                            Dy += u * (m[n + q] - my) * inv[a];
+                            Dz += u * (m[2 * n + q] - mz) * inv[a];
+                        }
+                    }
+                    const float c1x = my * Dz - mz * Dy, c1y = mz * Dx - mx * Dz, c1z = mx * Dy - my * Dx;
+                    const float c2x = my * c1z - mz * c1y, c2y = mz * c1x - mx * c1z, c2z = mx * c1y - my * c1x;
+                    tx += -c2x - p.zl_beta * c1x;
+                    ty += -c2y - p.zl_beta * c1y;
+                    tz += -c2z - p.zl_beta * c1z;
+                }
+                if (p.has_slon) {  // llg_fp32.cu:142-170
+                    const float px_ = p.slon_p[0], py_ = p.slon_p[1], pz_ = p.slon_p[2];
+                    const float mp = mx * px_ + my * py_ + mz * pz_;
+                    const float gs = p.slon_pf * (p.slon_P * p.slon_l2) / ((p.slon_l2 + 1.f) + (p.slon_l2 - 1.f) * mp);
+                    const float c1x = my * pz_ - mz * py_, c1y = mz * px_ - mx * pz_, c1z = mx * py_ - my * px_;
+                    const float c2x = my * c1z - mz * c1y, c2y = mz * c1x - mx * c1z, c2z = mx * c1y - my * c1x;
+                    tx += gs * (c2x + p.slon_eps * c1x);
+                    ty += gs * (c2y + p.slon_eps * c1y);
+                    tz += gs * (c2z + p.slon_eps * c1z);
+                }
+                if (p.has_sot) {  // llg_fp32.cu:172-195
+                    const float sx = p.sot_s[0], sy = p.sot_s[1], sz = p.sot_s[2];
+                    const float ms_ = mx * sx + my * sy + mz * sz;
+                    tx += p.sot_amp * (-p.sot_xi_dl * (ms_ * mx - sx) + p.sot_xi_fl * (my * sz - mz * sy));
+                    ty += p.sot_amp * (-p.sot_xi_dl * (ms_ * my - sy) + p.sot_xi_fl * (mz * sx - mx * sz));
+                    tz += p.sot_amp * (-p.sot_xi_dl * (ms_ * mz - sz) + p.sot_xi_fl * (mx * sy - my * sx));
+                }
+                // the field whose LLG right-hand side is T
+                ax += p.tq_a * tx + p.tq_b * (my * tz - mz * ty);
+                ay += p.tq_a * ty + p.tq_b * (mz * tx - mx * tz);
+                az += p.tq_a * tz + p.tq_b * (mx * ty - my * tx);
             }
             hx = ax;
             hy = ay;

@@ -422,6 +422,9 @@ struct fo_problem {
     double *abm_h[3];
     int abm_startup;
     double abm_last_dt;
+    /* torque prefactors (api.cpp:250-300, context.hpp:321-339) */
+    int has_zl, has_slon, has_sot;
+    double zl_u[3], slon_pf, slon_P, sot_amp, sot_s[3];
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
     uint32_t *region; /* optional region ids */
     double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
@@ -486,6 +489,32 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     for (int s = 0; s < 7; ++s) pr->k[s] = dalloc(n3);
     if (p->integrator == 3)
         for (int s = 0; s < 3; ++s) pr->abm_h[s] = dalloc(n3);
+    {
+        const double MU_B = 9.274009994e-24, E_CH = 1.60217662e-19, HBAR = 1.054571817e-34;
+        const double *j = p->current_density;
+        const int has_j = j[0] != 0.0 || j[1] != 0.0 || j[2] != 0.0;
+        pr->has_zl = has_j && p->stt_degree > 0.0 && p->ms > 0.0;
+        if (pr->has_zl) {
+            const double b = p->stt_degree * MU_B / (E_CH * p->ms * (1.0 + p->stt_beta * p->stt_beta));
+            for (int c = 0; c < 3; ++c) pr->zl_u[c] = b * j[c];
+        }
+        const double p2 = p->stt_p[0] * p->stt_p[0] + p->stt_p[1] * p->stt_p[1] + p->stt_p[2] * p->stt_p[2];
+        pr->has_slon = p2 > 0.0 && p->stt_lambda > 0.0 && has_j && p->ms > 0.0 && p->dz > 0.0;
+        if (pr->has_slon) {
+            const double js = sqrt(j[0] * j[0] + j[1] * j[1] + j[2] * j[2]);
+            pr->slon_pf = js * HBAR / (2.0 * E_CH * FO_MU0 * p->ms * p->dz);
+            pr->slon_P = p->stt_degree > 0.0 ? p->stt_degree : 1.0;
+        }
+        const double t = p->sot_thickness > 0.0 ? p->sot_thickness : 1.0e-9;
+        pr->has_sot = p->has_sot && p->ms > 0.0;
+        if (pr->has_sot) {
+            const double *sg = p->sot_sigma;
+            const double len = sqrt(sg[0] * sg[0] + sg[1] * sg[1] + sg[2] * sg[2]);
+            const double inv = len > 1e-30 ? 1.0 / len : 0.0;
+            for (int c = 0; c < 3; ++c) pr->sot_s[c] = sg[c] * inv;
+            pr->sot_amp = fabs(p->sot_je) * HBAR / (2.0 * E_CH * FO_MU0 * p->ms * t);
+        }
+    }
     norm3(p->u_axis, pr->u);
     norm3(p->c1, pr->c1);
     norm3(p->c2, pr->c2);
@@ -740,6 +769,62 @@ static double dmi_energy_cell(const fo_problem *pr, const double *m, long i) {
     return e;
 }
 
+static void cross3(const double *a, const double *b, double *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* Spin-transfer and spin-orbit torques added to dm/dt at active cell i
+ * (native/backends/fdm/src/llg_fp32.cu:65-195):
+ *   Zhang-Li   -m x (m x D) - beta m x D, D = (u.grad) m by upwind differences (the
+ *              upwind neighbour when it exists, taken without the mask as the reference
+ *              does, else no contribution along that axis)
+ *   Slonczewski beta_STT g [m x (m x p) + eps' m x p], g = P L^2 / ((L^2 + 1) + (L^2 - 1) m.p)
+ *   SOT        amp (-xi_DL ((m.s) m - s) + xi_FL m x s) */
+static void torque_add(const fo_problem *pr, const double *m, long i, double *k) {
+    const fo_params *p = &pr->p;
+    const double *mi = m + 3 * i;
+    if (pr->has_zl) {
+        const int nx = p->nx, ny = p->ny, nz = p->nz;
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+        const int pos[3] = {x, y, z}, ext[3] = {nx, ny, nz};
+        const long stride[3] = {1, nx, (long)nx * ny};
+        const double inv[3] = {1.0 / p->dx, 1.0 / p->dy, 1.0 / p->dz};
+        double D[3] = {0, 0, 0};
+        for (int a = 0; a < 3; ++a) {
+            const double u = pr->zl_u[a];
+            if (u > 0.0 && pos[a] > 0) {
+                const double *q = m + 3 * (i - stride[a]);
+                for (int c = 0; c < 3; ++c) D[c] += u * (mi[c] - q[c]) * inv[a];
+            } else if (u < 0.0 && pos[a] < ext[a] - 1) {
+                const double *q = m + 3 * (i + stride[a]);
+                for (int c = 0; c < 3; ++c) D[c] += u * (q[c] - mi[c]) * inv[a];
+            }
+        }
+        double c1[3], c2[3];
+        cross3(mi, D, c1);
+        cross3(mi, c1, c2);
+        for (int c = 0; c < 3; ++c) k[c] += -c2[c] - p->stt_beta * c1[c];
+    }
+    if (pr->has_slon) {
+        const double L2 = p->stt_lambda * p->stt_lambda;
+        const double mp = mi[0] * p->stt_p[0] + mi[1] * p->stt_p[1] + mi[2] * p->stt_p[2];
+        const double g = pr->slon_P * L2 / ((L2 + 1.0) + (L2 - 1.0) * mp);
+        double c1[3], c2[3];
+        cross3(mi, p->stt_p, c1);
+        cross3(mi, c1, c2);
+        for (int c = 0; c < 3; ++c) k[c] += pr->slon_pf * g * (c2[c] + p->stt_epsilon_prime * c1[c]);
+    }
+    if (pr->has_sot) {
+        const double *sv = pr->sot_s;
+        const double ms_ = mi[0] * sv[0] + mi[1] * sv[1] + mi[2] * sv[2];
+        double fl[3];
+        cross3(mi, sv, fl);
+        for (int c = 0; c < 3; ++c) k[c] += pr->sot_amp * (-p->sot_xi_dl * (ms_ * mi[c] - sv[c]) + p->sot_xi_fl * fl[c]);
+    }
+}
+
 static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h_d, double *h_eff,
                         double *rhs) {
     const fo_params *p = &pr->p;
@@ -760,7 +845,10 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
             dmi_mel_field_cell(pr, m, i, h);
         }
         for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
-        if (rhs) rhs_cell(p, m + 3 * i, h, rhs + 3 * i);
+        if (rhs) {
+            rhs_cell(p, m + 3 * i, h, rhs + 3 * i);
+            if (active(pr, i)) torque_add(pr, m, i, rhs + 3 * i);
+        }
     }
 }
 

@@ -69,6 +69,16 @@ typedef struct {
     int32_t has_magnetoelastic, pad1;
     double mel_b1, mel_b2;
     double mel_strain[6];
+    /* spin-transfer and spin-orbit torques (native/backends/fdm/src/llg_fp32.cu:65-195;
+     * prefactors api.cpp:250-300, context.hpp:321-339) */
+    double current_density[3];   /* A/m^2: Zhang-Li drift (with stt_degree > 0) and Slonczewski |j| */
+    double stt_degree, stt_beta;
+    double stt_p[3];             /* Slonczewski polarisation (not normalised, as the reference) */
+    double stt_lambda, stt_epsilon_prime;
+    int32_t has_sot, pad2;
+    double sot_je, sot_xi_dl, sot_xi_fl;
+    double sot_sigma[3];
+    double sot_thickness;
 } fo_params;
 
 #define FO_MAX_REGIONS 256

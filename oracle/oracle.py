@@ -50,6 +50,11 @@ class Params(C.Structure):
         ("dmi_d_interfacial", C.c_double), ("dmi_d_bulk", C.c_double),
         ("has_magnetoelastic", C.c_int32), ("pad1", C.c_int32),
         ("mel_b1", C.c_double), ("mel_b2", C.c_double), ("mel_strain", C.c_double * 6),
+        ("current_density", C.c_double * 3), ("stt_degree", C.c_double), ("stt_beta", C.c_double),
+        ("stt_p", C.c_double * 3), ("stt_lambda", C.c_double), ("stt_epsilon_prime", C.c_double),
+        ("has_sot", C.c_int32), ("pad2", C.c_int32),
+        ("sot_je", C.c_double), ("sot_xi_dl", C.c_double), ("sot_xi_fl", C.c_double),
+        ("sot_sigma", C.c_double * 3), ("sot_thickness", C.c_double),
     ]
 
 
@@ -152,7 +157,10 @@ class Problem:
                  max_error=1e-5, dt_min=1e-18, dt_max=1e-10, headroom=0.8, rtol=0.0,
                  growth_limit=float("inf"), shrink_limit=0.0, dp45_norm=0,
                  active_mask=None, m0=None, region_mask=None, exchange_lut=None,
-                 dmi_d_interfacial=None, dmi_d_bulk=None, mel_b1=None, mel_b2=0.0, mel_strain=(0.0,) * 6):
+                 dmi_d_interfacial=None, dmi_d_bulk=None, mel_b1=None, mel_b2=0.0, mel_strain=(0.0,) * 6,
+                 current_density=(0.0, 0.0, 0.0), stt_degree=0.0, stt_beta=0.0, stt_p=(0.0, 0.0, 0.0),
+                 stt_lambda=0.0, stt_epsilon_prime=0.0, sot_je=None, sot_xi_dl=0.0, sot_xi_fl=0.0,
+                 sot_sigma=(0.0, 0.0, 1.0), sot_thickness=0.0):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -178,6 +186,14 @@ class Problem:
         p.has_magnetoelastic = int(mel_b1 is not None)
         p.mel_b1, p.mel_b2 = (mel_b1 or 0.0), mel_b2
         p.mel_strain[:] = list(mel_strain)
+        p.current_density[:] = list(current_density)
+        p.stt_degree, p.stt_beta = stt_degree, stt_beta
+        p.stt_p[:] = list(stt_p)
+        p.stt_lambda, p.stt_epsilon_prime = stt_lambda, stt_epsilon_prime
+        p.has_sot = int(sot_je is not None)
+        p.sot_je, p.sot_xi_dl, p.sot_xi_fl = (sot_je or 0.0), sot_xi_dl, sot_xi_fl
+        p.sot_sigma[:] = list(sot_sigma)
+        p.sot_thickness = sot_thickness
         self._mask = None
         if active_mask is not None:
             self._mask = np.ascontiguousarray(active_mask, dtype=np.uint8)

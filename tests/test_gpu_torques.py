@@ -1,0 +1,63 @@
+"""Zhang-Li and Slonczewski spin-transfer torque and spin-orbit torque on the GPU against
+the FP64 oracle (native/backends/fdm/src/llg_fp32.cu:65-195).  The engine passes each
+torque T as the field a T + b m x T through its extra-field pass; the LLG right-hand side
+maps that back to T, so trajectories must follow the oracle, which adds T directly.  The
+H_eff observable leaves the torques out, as the reference's does."""
+import numpy as np
+import pytest
+
+from fullmag_gb300 import FdmBackend, FdmError, _abi
+from helpers import problem, rel_l2
+from test_gpu_parity import make_pair
+
+pytestmark = pytest.mark.gpu
+
+TORQUES = {
+    "zhang_li": dict(current_density=(6e11, -2e11, 0.0), stt_degree=0.6, stt_beta=0.05),
+    "slonczewski": dict(current_density=(0.0, 0.0, 2e11), stt_p=(0.0, 0.6, 0.8), stt_lambda=1.5,
+                        stt_epsilon_prime=0.1),
+    "sot": dict(sot_je=1.5e11, sot_xi_dl=0.25, sot_xi_fl=-0.1, sot_sigma=(0.0, 1.0, 0.0), sot_thickness=1e-9),
+}
+
+
+@pytest.mark.parametrize("name", list(TORQUES))
+@pytest.mark.parametrize("integrator", [_abi.INTEGRATOR_RK4, _abi.INTEGRATOR_HEUN])
+def test_torque_trajectory(gpu_lib, oracle, name, integrator):
+    kw = problem(24, 12, 2, seed=71, alpha=0.05, **TORQUES[name])
+    gpu, orc = make_pair(oracle, kw, integrator=integrator)
+    for _ in range(20):
+        sg = gpu.step(5e-14)
+        so = orc.step(5e-14)
+    assert np.abs(gpu.copy_field(_abi.OBSERVABLE_M) - orc.get_m()).max() < 2e-5
+    assert abs(sg["max_rhs_amplitude"] - so["max_rhs"]) <= 1e-4 * so["max_rhs"]
+    assert abs(sg["total_energy_joules"] - so["e_total"]) <= 1e-4 * abs(so["e_total"])
+
+
+def test_heff_observable_leaves_torques_out(gpu_lib, oracle):
+    kw = problem(16, 10, 2, seed=72, alpha=0.1, **TORQUES["zhang_li"], sot_je=2e11, sot_xi_dl=0.3,
+                 sot_sigma=(1.0, 0.0, 0.0))
+    gpu, orc = make_pair(oracle, kw)
+    gpu.step(5e-14)
+    orc.step(5e-14)
+    ref = orc.fields(orc.get_m())
+    assert rel_l2(gpu.copy_field(_abi.OBSERVABLE_H_EFF), ref["h_eff"]) < 1e-5
+    st = gpu.stats()
+    assert abs(st["max_rhs_amplitude"] - np.linalg.norm(ref["rhs"], axis=1).max()) <= 1e-4 * st["max_rhs_amplitude"]
+
+
+def test_masked_sot_leaves_inactive_cells(gpu_lib, oracle):
+    kw = problem(16, 8, 2, seed=73, alpha=0.1, **TORQUES["sot"])
+    mask = (np.random.default_rng(4).random(16 * 8 * 2) > 0.2).astype(np.uint8)
+    gpu, orc = make_pair(oracle, kw, mask=mask)
+    for _ in range(10):
+        gpu.step(5e-14)
+        orc.step(5e-14)
+    m = gpu.copy_field(_abi.OBSERVABLE_M)
+    assert np.abs(m[mask == 0]).max() == 0.0
+    assert np.abs(m - orc.get_m()).max() < 2e-5
+
+
+def test_torque_without_precession_or_damping_is_rejected(gpu_lib):
+    kw = problem(8, 4, 1, seed=74, alpha=0.0, disable_precession=True, **TORQUES["sot"])
+    with pytest.raises(FdmError):
+        FdmBackend(**kw)
