@@ -77,6 +77,9 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               stt_p=(0.0, 0.0, 0.0), stt_lambda: float = 0.0, stt_epsilon_prime: float = 0.0,
               sot_je: Optional[float] = None, sot_xi_dl: float = 0.0, sot_xi_fl: float = 0.0,
               sot_sigma=(0.0, 0.0, 1.0), sot_thickness: float = 0.0,
+              ku1_field: Optional[np.ndarray] = None, ku2_field: Optional[np.ndarray] = None,
+              kc1_field: Optional[np.ndarray] = None, kc2_field: Optional[np.ndarray] = None,
+              kc3_field: Optional[np.ndarray] = None,
               active_mask: Optional[np.ndarray] = None,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
@@ -126,6 +129,12 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
     p.sot_je, p.sot_xi_dl, p.sot_xi_fl = (sot_je or 0.0), sot_xi_dl, sot_xi_fl
     p.sot_sigma[:] = list(sot_sigma)
     p.sot_thickness = sot_thickness
+    for name, arr in (("ku1_field", ku1_field), ("ku2_field", ku2_field), ("kc1_field", kc1_field),
+                      ("kc2_field", kc2_field), ("kc3_field", kc3_field)):
+        if arr is not None:  # one value per cell, borrowed for the create call like every plan array
+            a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+            keep.append(a)
+            setattr(p, name, _dptr(a))
     p.sot_sigma[:] = [0.0, 0.0, 1.0]
     p.sot_thickness = 1e-9
     p.oersted_axis[:] = [0.0, 0.0, 1.0]

@@ -33,8 +33,9 @@ namespace fm {
 
 static constexpr double kMu0 = 4.0 * M_PI * 1e-7;
 // device statistics slots: the kNumStats row-pass statistics, the step size of graph
-// replays, and the extra field pass's Zeeman sum m.(H_ext + H_map) and DMI energy density
-static constexpr int kStatSlots = kNumStats + 3;
+// replays, and the extra field pass's four sums (ExtraSums: Zeeman m.(H_ext + H_map), DMI,
+// uniaxial and cubic energy densities)
+static constexpr int kStatSlots = kNumStats + 5;
 
 bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
                          std::string &err);
@@ -221,7 +222,8 @@ struct Engine {
     bool torques_off = false;  // set while an observable pass runs
     ExtraField xf{};
     float *hextra = nullptr;
-    double2 *xpart = nullptr;
+    ExtraSums *xpart = nullptr;
+    float *kmaps[5] = {};  // per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (device, FP32) or NULL
     float2 *X = nullptr, *Y = nullptr;
     float *kern = nullptr;
     uint8_t *mask = nullptr;
@@ -269,6 +271,10 @@ struct Engine {
         if (xpart) cudaFree(xpart);
         hextra = nullptr;
         xpart = nullptr;
+        for (float *&km : kmaps) {
+            if (km) cudaFree(km);
+            km = nullptr;
+        }
         if (arena) cudaFree(arena);
         arena = nullptr;
         if (staging) cudaFree(staging);
@@ -614,8 +620,9 @@ struct Engine {
         // sum m.(H_ext + H_map) then comes from the extra pass (slot kNumStats + 1)
         const double zeeman = has_extra ? d[kNumStats + 1] : d[2];
         st.external_energy_joules = (has_ext || hmap) ? -kMu0 * ms * V * zeeman : 0.0;
-        st.anisotropy_energy_joules = has_uni ? -V * d[3] : 0.0;
-        st.cubic_energy_joules = has_cub ? V * d[4] : 0.0;
+        // with per-cell anisotropy maps both terms are the extra pass's (slots kNumStats + 3, + 4)
+        st.anisotropy_energy_joules = has_uni ? -V * (xf.aniso ? d[kNumStats + 3] : d[3]) : 0.0;
+        st.cubic_energy_joules = has_cub ? V * (xf.aniso ? d[kNumStats + 4] : d[4]) : 0.0;
         st.dmi_energy_joules = has_extra ? V * d[kNumStats + 2] : 0.0;
         st.total_energy_joules = st.exchange_energy_joules + st.demag_energy_joules + st.external_energy_joules +
                                  st.anisotropy_energy_joules + st.cubic_energy_joules + st.dmi_energy_joules;
@@ -1658,9 +1665,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
         unsupported(*this, plan->has_oersted_cylinder != 0, "Oersted field") ||
         unsupported(*this, plan->region_mask != nullptr, "region masks / exchange LUT") ||
-        unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers") ||
-        unsupported(*this, plan->ku1_field || plan->ku2_field || plan->kc1_field || plan->kc2_field || plan->kc3_field,
-                    "per-cell anisotropy maps"))
+        unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers"))
         return false;
 
     if (plan->active_mask) {
@@ -1834,7 +1839,31 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
             xf.tq_b = (float)(s / (gb * (s + alpha * alpha)));
         }
     }
-    has_extra = ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque);
+    // per-cell anisotropy maps: the uniaxial and cubic terms move to the extra pass
+    {
+        const bool uni_map = has_uni && (plan->ku1_field || plan->ku2_field);
+        const bool cub_map = has_cub && (plan->kc1_field || plan->kc2_field || plan->kc3_field);
+        xf.aniso = (uni_map || cub_map) && ms > 0.0;
+        if (xf.aniso) {
+            xf.has_uni = has_uni;
+            xf.has_cub = has_cub;
+            xf.ku1 = mat.ku1f;
+            xf.ku2 = mat.ku2f;
+            xf.kc1 = mat.kc1f;
+            xf.kc2 = mat.kc2f;
+            xf.kc3 = mat.kc3f;
+            xf.inv_mu0ms = (float)(1.0 / mu0ms);
+            for (int c = 0; c < 3; ++c) {
+                xf.u[c] = mat.u[c];
+                xf.c1[c] = mat.c1[c];
+                xf.c2[c] = mat.c2[c];
+                xf.c3[c] = mat.c3[c];
+            }
+            mat.has_uni = 0;  // the row pass leaves them to the extra pass
+            mat.has_cub = 0;
+        }
+    }
+    has_extra = ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque || xf.aniso);
 
     // ---- device and stream ----
     if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;
@@ -1923,8 +1952,25 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     if (cuda_fail("cudaMallocHost(stats)", cudaMallocHost((void **)&hstats, sizeof(double) * kStatSlots))) return false;
     if (has_extra &&
         (cuda_fail("cudaMalloc(extra field)", cudaMalloc((void **)&hextra, sizeof(float) * 3 * (size_t)g.n)) ||
-         cuda_fail("cudaMalloc(extra sums)", cudaMalloc((void **)&xpart, sizeof(double2) * (size_t)extra_field_blocks(g)))))
+         cuda_fail("cudaMalloc(extra sums)", cudaMalloc((void **)&xpart, sizeof(ExtraSums) * (size_t)extra_field_blocks(g)))))
         return false;
+    if (xf.aniso) {  // per-cell anisotropy constants, FP32 on the device
+        const double *src[5] = {plan->ku1_field, plan->ku2_field, plan->kc1_field, plan->kc2_field, plan->kc3_field};
+        std::vector<float> tmp((size_t)g.n);
+        for (int k = 0; k < 5; ++k) {
+            if (!src[k]) continue;
+            for (long long i = 0; i < g.n; ++i) tmp[i] = (float)src[k][i];
+            if (cuda_fail("cudaMalloc(anisotropy map)", cudaMalloc((void **)&kmaps[k], sizeof(float) * (size_t)g.n)) ||
+                cuda_fail("anisotropy map upload",
+                          cudaMemcpy(kmaps[k], tmp.data(), sizeof(float) * (size_t)g.n, cudaMemcpyHostToDevice)))
+                return false;
+        }
+        xf.ku1m = kmaps[0];
+        xf.ku2m = kmaps[1];
+        xf.kc1m = kmaps[2];
+        xf.kc2m = kmaps[3];
+        xf.kc3m = kmaps[4];
+    }
     if (cuda_fail("cudaMallocHost(dt)", cudaMallocHost((void **)&dt_host, sizeof(double)))) return false;
     dt_dev = dstats + kNumStats;  // slot kNumStats holds dt (kStatSlots)
 

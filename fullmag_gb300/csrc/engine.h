@@ -154,13 +154,19 @@ size_t y_convolve_2d_smem(const Grid &g, int tx);
 // (extra_field.cu): interfacial and bulk DMI (central differences, Neumann clamp, mask)
 // and the magnetoelastic field of a prescribed strain, plus the applied field map.  The
 // row pass adds `out` as its field map; H = 0 at inactive cells.
+// per-CTA sums of the extra field pass (FP64): Zeeman m.(H_ext + H_map), DMI energy density,
+// and with per-cell anisotropy maps the uniaxial and cubic energy densities
+struct ExtraSums {
+    double zee, dmi, uni, cub;
+};
+
 struct ExtraField {
     Grid g;
     const uint8_t *mask;
     const float *m;            // stage input (SoA)
     const float *hmap;         // applied field map or NULL
     float *out;                // H_extra (SoA)
-    double2 *partials;         // NULL: no sums; else per CTA (Zeeman sum m.(H_ext + H_map), DMI energy density sum)
+    ExtraSums *partials;       // NULL: no sums; else one entry per CTA
     int has_ext;               // uniform applied field hext (A/m) in the Zeeman sum
     float hext[3];
     int has_int, has_bulk, has_mel;
@@ -180,11 +186,19 @@ struct ExtraField {
     float slon_pf, slon_P, slon_l2, slon_eps, slon_p[3];  // Slonczewski
     float sot_amp, sot_xi_dl, sot_xi_fl, sot_s[3];        // spin-orbit torque
     float tq_a, tq_b;
+    // per-cell anisotropy (any of the maps present): the whole uniaxial and cubic terms move
+    // here from the row pass, each constant taken from its map when there is one
+    int aniso;
+    int has_uni, has_cub;
+    const float *ku1m, *ku2m, *kc1m, *kc2m, *kc3m;  // maps (J/m^3) or NULL
+    float ku1, ku2, kc1, kc2, kc3;                  // uniform values (J/m^3)
+    float inv_mu0ms;                                // 1 / (mu0 Ms)
+    float u[3], c1[3], c2[3], c3[3];
 };
 int extra_field_blocks(const Grid &g);
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);
-// sums the per-CTA partials into out[0], out[1] (fixed order)
-cudaError_t launch_extra_finalize(const double2 *partials, int nblocks, double *out, cudaStream_t s);
+// sums the per-CTA partials into out[0..3] (fixed order)
+cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s);
 
 // Adjoint (reverse-mode RK4): the final-combination pass (adjoint.cu); all fields SoA.
 // The local VJP and the stage update are the row pass's adjoint modes.

@@ -34,12 +34,31 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// fixed-order block sum of the four partial sums; thread 0 returns the CTA's total
+__device__ __forceinline__ ExtraSums block_sum(ExtraSums v) {
+    __shared__ ExtraSums red[kThreads / 32];
+    v.zee = warp_sum(v.zee);
+    v.dmi = warp_sum(v.dmi);
+    v.uni = warp_sum(v.uni);
+    v.cub = warp_sum(v.cub);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    ExtraSums t{0.0, 0.0, 0.0, 0.0};
+    if (threadIdx.x == 0)
+        for (int w = 0; w < kThreads / 32; ++w) {
+            t.zee += red[w].zee;
+            t.dmi += red[w].dmi;
+            t.uni += red[w].uni;
+            t.cub += red[w].cub;
+        }
+    return t;
+}
+
 __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField p) {
-    __shared__ double2 red[kThreads / 32];
     const Grid &g = p.g;
     const long long n = g.n;
     const float *m = p.m;
-    double s_zee = 0.0, s_dmi = 0.0;
+    double s_zee = 0.0, s_dmi = 0.0, s_uni = 0.0, s_cub = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float hx = 0.f, hy = 0.f, hz = 0.f;
         if (p.mask == nullptr || p.mask[i] != 0) {
@@ -98,6 +117,43 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                 ax += p.mel_pref * (2.f * p.b1 * mx * p.e11 + p.b2 * (my * p.e12 + mz * p.e13));
                 ay += p.mel_pref * (2.f * p.b1 * my * p.e22 + p.b2 * (mx * p.e12 + mz * p.e23));
                 az += p.mel_pref * (2.f * p.b1 * mz * p.e33 + p.b2 * (mx * p.e13 + my * p.e23));
+            }
+            if (p.aniso) {
+                // per-cell anisotropy, the row pass's formulas with constants from the maps
+                // (native/backends/fdm/src/demag_fp32.cu:271-317)
+                if (p.has_uni) {
+                    const float k1 = p.ku1m ? p.ku1m[i] : p.ku1, k2 = p.ku2m ? p.ku2m[i] : p.ku2;
+                    const float mu = mx * p.u[0] + my * p.u[1] + mz * p.u[2];
+                    const float cf = 2.f * p.inv_mu0ms * (k1 * mu + 2.f * k2 * mu * mu * mu);
+                    ax += cf * p.u[0];
+                    ay += cf * p.u[1];
+                    az += cf * p.u[2];
+                    if (p.partials) {
+                        const double s2 = (double)mu * (double)mu;
+                        s_uni += (double)k1 * s2 + (double)k2 * s2 * s2;
+                    }
+                }
+                if (p.has_cub) {
+                    const float k1 = p.kc1m ? p.kc1m[i] : p.kc1, k2 = p.kc2m ? p.kc2m[i] : p.kc2;
+                    const float k3 = p.kc3m ? p.kc3m[i] : p.kc3;
+                    const float a1 = mx * p.c1[0] + my * p.c1[1] + mz * p.c1[2];
+                    const float a2 = mx * p.c2[0] + my * p.c2[1] + mz * p.c2[2];
+                    const float a3 = mx * p.c3[0] + my * p.c3[1] + mz * p.c3[2];
+                    const float s1 = a1 * a1, s2 = a2 * a2, s3 = a3 * a3;
+                    const float sig = s1 * s2 + s2 * s3 + s1 * s3;
+                    const float f1 = -2.f * k1 * p.inv_mu0ms, f2 = -2.f * k2 * p.inv_mu0ms, f3 = -4.f * k3 * p.inv_mu0ms;
+                    const float g1 = f1 * a1 * (s2 + s3) + f2 * a1 * s2 * s3 + f3 * sig * a1 * (s2 + s3);
+                    const float g2 = f1 * a2 * (s1 + s3) + f2 * a2 * s1 * s3 + f3 * sig * a2 * (s1 + s3);
+                    const float g3 = f1 * a3 * (s1 + s2) + f2 * a3 * s1 * s2 + f3 * sig * a3 * (s1 + s2);
+                    ax += g1 * p.c1[0] + g2 * p.c2[0] + g3 * p.c3[0];
+                    ay += g1 * p.c1[1] + g2 * p.c2[1] + g3 * p.c3[1];
+                    az += g1 * p.c1[2] + g2 * p.c2[2] + g3 * p.c3[2];
+                    if (p.partials) {
+                        const double d1 = (double)a1 * a1, d2 = (double)a2 * a2, d3 = (double)a3 * a3;
+                        const double ds = d1 * d2 + d2 * d3 + d1 * d3;
+                        s_cub += (double)k1 * ds + (double)k2 * d1 * d2 * d3 + (double)k3 * ds * ds;
+                    }
+                }
             }
             if (p.torques && (p.has_zl || p.has_slon || p.has_sot)) {
                 float tx = 0.f, ty = 0.f, tz = 0.f;
@@ -178,40 +234,26 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
         p.out[2 * n + i] = hz;
     }
     if (p.partials) {
-        const double a = warp_sum(s_zee), b = warp_sum(s_dmi);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(a, b);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 t = make_double2(0.0, 0.0);
-            for (int w = 0; w < kThreads / 32; ++w) {
-                t.x += red[w].x;
-                t.y += red[w].y;
-            }
-            p.partials[blockIdx.x] = t;
-        }
+        const ExtraSums t = block_sum(ExtraSums{s_zee, s_dmi, s_uni, s_cub});
+        if (threadIdx.x == 0) p.partials[blockIdx.x] = t;
     }
 }
 
-__global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const double2 *__restrict__ partials, int nblocks,
+__global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSums *__restrict__ partials, int nblocks,
                                                                   double *__restrict__ out) {
-    __shared__ double2 red[kThreads / 32];
-    double a = 0.0, b = 0.0;
+    ExtraSums v{0.0, 0.0, 0.0, 0.0};
     for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-        a += partials[k].x;
-        b += partials[k].y;
+        v.zee += partials[k].zee;
+        v.dmi += partials[k].dmi;
+        v.uni += partials[k].uni;
+        v.cub += partials[k].cub;
     }
-    a = warp_sum(a);
-    b = warp_sum(b);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(a, b);
-    __syncthreads();
+    const ExtraSums t = block_sum(v);
     if (threadIdx.x == 0) {
-        double2 t = make_double2(0.0, 0.0);
-        for (int w = 0; w < kThreads / 32; ++w) {
-            t.x += red[w].x;
-            t.y += red[w].y;
-        }
-        out[0] = t.x;
-        out[1] = t.y;
+        out[0] = t.zee;
+        out[1] = t.dmi;
+        out[2] = t.uni;
+        out[3] = t.cub;
     }
 }
 
@@ -224,7 +266,7 @@ cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_extra_finalize(const double2 *partials, int nblocks, double *out, cudaStream_t s) {
+cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s) {
     extra_finalize_kernel<<<1, kThreads, 0, s>>>(partials, nblocks, out);
     return cudaGetLastError();
 }

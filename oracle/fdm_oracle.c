@@ -425,6 +425,7 @@ struct fo_problem {
     /* torque prefactors (api.cpp:250-300, context.hpp:321-339) */
     int has_zl, has_slon, has_sot;
     double zl_u[3], slon_pf, slon_P, sot_amp, sot_s[3];
+    double *kmap[5]; /* per-cell Ku1 Ku2 Kc1 Kc2 Kc3 or NULL */
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
     uint32_t *region; /* optional region ids */
     double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
@@ -452,6 +453,7 @@ void fo_destroy(fo_problem *pr) {
     free(pr->region); free(pr->lut);
     for (int s = 0; s < 7; ++s) free(pr->k[s]);
     for (int s = 0; s < 3; ++s) free(pr->abm_h[s]);
+    for (int s = 0; s < 5; ++s) free(pr->kmap[s]);
     free(pr);
 }
 
@@ -470,6 +472,16 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     pr->p.active_mask = NULL;
     pr->p.region_mask = NULL;
     pr->p.exchange_lut = NULL;
+    {
+        const double *src[5] = {p->ku1_field, p->ku2_field, p->kc1_field, p->kc2_field, p->kc3_field};
+        const long nc = (long)p->nx * p->ny * p->nz;
+        for (int k = 0; k < 5; ++k)
+            if (src[k]) {
+                pr->kmap[k] = (double *)malloc(sizeof(double) * (size_t)nc);
+                memcpy(pr->kmap[k], src[k], sizeof(double) * (size_t)nc);
+            }
+        pr->p.ku1_field = pr->p.ku2_field = pr->p.kc1_field = pr->p.kc2_field = pr->p.kc3_field = NULL;
+    }
     pr->n = (long)p->nx * p->ny * p->nz;
     const long n3 = 3 * pr->n;
     if (p->active_mask) {
@@ -653,12 +665,18 @@ static void demag_add(fo_problem *pr, const double *m, double *h) {
 
 /* Uniaxial + cubic anisotropy field (fdm_fields.rs:648-705, 910-1047). The Kc3 term
  * follows the CUDA reference (native/backends/fdm/src/demag_fp32.cu:295-318). */
-static void anis_field_cell(const fo_problem *pr, const double *m, double *h) {
+/* Anisotropy constant k (0 Ku1, 1 Ku2, 2 Kc1, 3 Kc2, 4 Kc3) at cell i: the per-cell map when
+ * there is one, else the uniform value. */
+static inline double kval(const fo_problem *pr, int k, long i, double uniform) {
+    return pr->kmap[k] ? pr->kmap[k][i] : uniform;
+}
+
+static void anis_field_cell(const fo_problem *pr, const double *m, long i, double *h) {
     const fo_params *p = &pr->p;
     const double ms = p->ms > 1e-30 ? p->ms : 1e-30;
     if (p->has_uniaxial) {
         const double mu = m[0] * pr->u[0] + m[1] * pr->u[1] + m[2] * pr->u[2];
-        const double cf = 2.0 * p->ku1 / (FO_MU0 * ms) * mu + 4.0 * p->ku2 / (FO_MU0 * ms) * mu * mu * mu;
+        const double cf = 2.0 * kval(pr, 0, i, p->ku1) / (FO_MU0 * ms) * mu + 4.0 * kval(pr, 1, i, p->ku2) / (FO_MU0 * ms) * mu * mu * mu;
         for (int c = 0; c < 3; ++c) h[c] += pr->u[c] * cf;
     }
     if (p->has_cubic) {
@@ -668,10 +686,11 @@ static void anis_field_cell(const fo_problem *pr, const double *m, double *h) {
         const double pf = 2.0 / (FO_MU0 * ms);
         const double s1 = m1 * m1, s2 = m2 * m2, s3 = m3 * m3;
         const double sig = s1 * s2 + s2 * s3 + s1 * s3;
-        const double p3 = -4.0 * p->kc3 / (FO_MU0 * ms);
-        const double g1 = -pf * (p->kc1 * m1 * (s2 + s3) + p->kc2 * m1 * s2 * s3) + p3 * sig * m1 * (s2 + s3);
-        const double g2 = -pf * (p->kc1 * m2 * (s1 + s3) + p->kc2 * m2 * s1 * s3) + p3 * sig * m2 * (s1 + s3);
-        const double g3 = -pf * (p->kc1 * m3 * (s1 + s2) + p->kc2 * m3 * s1 * s2) + p3 * sig * m3 * (s1 + s2);
+        const double kc1 = kval(pr, 2, i, p->kc1), kc2 = kval(pr, 3, i, p->kc2), kc3 = kval(pr, 4, i, p->kc3);
+        const double p3 = -4.0 * kc3 / (FO_MU0 * ms);
+        const double g1 = -pf * (kc1 * m1 * (s2 + s3) + kc2 * m1 * s2 * s3) + p3 * sig * m1 * (s2 + s3);
+        const double g2 = -pf * (kc1 * m2 * (s1 + s3) + kc2 * m2 * s1 * s3) + p3 * sig * m2 * (s1 + s3);
+        const double g3 = -pf * (kc1 * m3 * (s1 + s2) + kc2 * m3 * s1 * s2) + p3 * sig * m3 * (s1 + s2);
         for (int c = 0; c < 3; ++c) h[c] += pr->c1[c] * g1 + pr->c2[c] * g2 + pr->c3[c] * g3;
     }
 }
@@ -841,7 +860,7 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
                 for (int c = 0; c < 3; ++c) h[c] += p->h_ext[c];
             if (pr->hmap)
                 for (int c = 0; c < 3; ++c) h[c] += pr->hmap[3 * i + c];
-            anis_field_cell(pr, m + 3 * i, h);
+            anis_field_cell(pr, m + 3 * i, i, h);
             dmi_mel_field_cell(pr, m, i, h);
         }
         for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
@@ -917,7 +936,7 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
         if (p->has_uniaxial) {
             const double mu = mi[0] * pr->u[0] + mi[1] * pr->u[1] + mi[2] * pr->u[2];
             const double s = mu * mu;
-            euni += -V * (p->ku1 * s + p->ku2 * s * s);
+            euni += -V * (kval(pr, 0, i, p->ku1) * s + kval(pr, 1, i, p->ku2) * s * s);
         }
         if (p->has_cubic) {
             const double m1 = mi[0] * pr->c1[0] + mi[1] * pr->c1[1] + mi[2] * pr->c1[2];
@@ -925,11 +944,11 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
             const double m3 = mi[0] * pr->c3[0] + mi[1] * pr->c3[1] + mi[2] * pr->c3[2];
             const double s1 = m1 * m1, s2 = m2 * m2, s3 = m3 * m3;
             const double sig = s1 * s2 + s2 * s3 + s1 * s3;
-            ecub += V * (p->kc1 * sig + p->kc2 * s1 * s2 * s3 + p->kc3 * sig * sig);
+            ecub += V * (kval(pr, 2, i, p->kc1) * sig + kval(pr, 3, i, p->kc2) * s1 * s2 * s3 + kval(pr, 4, i, p->kc3) * sig * sig);
         }
         if (p->has_uniaxial || p->has_cubic) {
             double ha[3] = {0, 0, 0};
-            anis_field_cell(pr, mi, ha);
+            anis_field_cell(pr, mi, i, ha);
             eacpu += -0.5 * FO_MU0 * p->ms * V * (mi[0] * ha[0] + mi[1] * ha[1] + mi[2] * ha[2]);
         }
     }
@@ -1202,7 +1221,7 @@ static void tangent_rhs(fo_problem *pr, const double *m, const double *dm, const
             if (p->has_uniaxial) {
                 const double mu = mi[0] * pr->u[0] + mi[1] * pr->u[1] + mi[2] * pr->u[2];
                 const double dmu = dmi[0] * pr->u[0] + dmi[1] * pr->u[1] + dmi[2] * pr->u[2];
-                const double cf = (2.0 * p->ku1 + 12.0 * p->ku2 * mu * mu) / (FO_MU0 * ms) * dmu;
+                const double cf = (2.0 * kval(pr, 0, i, p->ku1) + 12.0 * kval(pr, 1, i, p->ku2) * mu * mu) / (FO_MU0 * ms) * dmu;
                 for (int c = 0; c < 3; ++c) dH[c] += cf * pr->u[c];
             }
         }

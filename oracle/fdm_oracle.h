@@ -79,6 +79,9 @@ typedef struct {
     double sot_je, sot_xi_dl, sot_xi_fl;
     double sot_sigma[3];
     double sot_thickness;
+    /* optional per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (J/m^3, one per cell), copied at create
+     * (native/backends/fdm/src/demag_fp32.cu:275-292) */
+    const double *ku1_field, *ku2_field, *kc1_field, *kc2_field, *kc3_field;
 } fo_params;
 
 #define FO_MAX_REGIONS 256

@@ -55,6 +55,8 @@ class Params(C.Structure):
         ("has_sot", C.c_int32), ("pad2", C.c_int32),
         ("sot_je", C.c_double), ("sot_xi_dl", C.c_double), ("sot_xi_fl", C.c_double),
         ("sot_sigma", C.c_double * 3), ("sot_thickness", C.c_double),
+        ("ku1_field", C.c_void_p), ("ku2_field", C.c_void_p), ("kc1_field", C.c_void_p),
+        ("kc2_field", C.c_void_p), ("kc3_field", C.c_void_p),
     ]
 
 
@@ -160,7 +162,8 @@ class Problem:
                  dmi_d_interfacial=None, dmi_d_bulk=None, mel_b1=None, mel_b2=0.0, mel_strain=(0.0,) * 6,
                  current_density=(0.0, 0.0, 0.0), stt_degree=0.0, stt_beta=0.0, stt_p=(0.0, 0.0, 0.0),
                  stt_lambda=0.0, stt_epsilon_prime=0.0, sot_je=None, sot_xi_dl=0.0, sot_xi_fl=0.0,
-                 sot_sigma=(0.0, 0.0, 1.0), sot_thickness=0.0):
+                 sot_sigma=(0.0, 0.0, 1.0), sot_thickness=0.0,
+                 ku1_field=None, ku2_field=None, kc1_field=None, kc2_field=None, kc3_field=None):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -194,6 +197,15 @@ class Problem:
         p.sot_je, p.sot_xi_dl, p.sot_xi_fl = (sot_je or 0.0), sot_xi_dl, sot_xi_fl
         p.sot_sigma[:] = list(sot_sigma)
         p.sot_thickness = sot_thickness
+        self._kmaps = {}
+        for name, arr in (("ku1_field", ku1_field), ("ku2_field", ku2_field), ("kc1_field", kc1_field),
+                          ("kc2_field", kc2_field), ("kc3_field", kc3_field)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+                if a.size != nx * ny * nz:
+                    raise ValueError(f"{name} needs one value per cell")
+                self._kmaps[name] = a
+                setattr(p, name, a.ctypes.data)
         self._mask = None
         if active_mask is not None:
             self._mask = np.ascontiguousarray(active_mask, dtype=np.uint8)
