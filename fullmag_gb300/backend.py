@@ -80,6 +80,10 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               ku1_field: Optional[np.ndarray] = None, ku2_field: Optional[np.ndarray] = None,
               kc1_field: Optional[np.ndarray] = None, kc2_field: Optional[np.ndarray] = None,
               kc3_field: Optional[np.ndarray] = None,
+              oersted_current: Optional[float] = None, oersted_radius: float = 0.0,
+              oersted_center=(0.0, 0.0, 0.0), oersted_axis=(0.0, 0.0, 1.0), oersted_kind: int = 0,
+              oersted_freq: float = 0.0, oersted_phase: float = 0.0, oersted_offset: float = 0.0,
+              oersted_t_on: float = 0.0, oersted_t_off: float = 0.0,
               active_mask: Optional[np.ndarray] = None,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
@@ -135,6 +139,14 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
             a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
             keep.append(a)
             setattr(p, name, _dptr(a))
+    p.has_oersted_cylinder = int(oersted_current is not None)
+    p.oersted_current, p.oersted_radius = (oersted_current or 0.0), oersted_radius
+    p.oersted_center[:] = list(oersted_center)
+    p.oersted_axis[:] = list(oersted_axis)
+    p.oersted_time_dep_kind = oersted_kind
+    p.oersted_time_dep_freq, p.oersted_time_dep_phase = oersted_freq, oersted_phase
+    p.oersted_time_dep_offset = oersted_offset
+    p.oersted_time_dep_t_on, p.oersted_time_dep_t_off = oersted_t_on, oersted_t_off
     p.sot_sigma[:] = [0.0, 0.0, 1.0]
     p.sot_thickness = 1e-9
     p.oersted_axis[:] = [0.0, 0.0, 1.0]

@@ -224,6 +224,26 @@ struct Engine {
     float *hextra = nullptr;
     ExtraSums *xpart = nullptr;
     float *kmaps[5] = {};  // per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (device, FP32) or NULL
+    // Oersted field (context.cu:844-905, demag_fp32.cu:585-616): the field for 1 A and the
+    // device scales I(t): [0] for the stages of a step, [1] for its final evaluation
+    bool has_oersted = false;
+    float *h_oe = nullptr, *oe_dev = nullptr;
+    int oe_kind = 0;
+    double oe_current = 0.0, oe_freq = 0.0, oe_phase = 0.0, oe_offset = 0.0, oe_t_on = 0.0, oe_t_off = 0.0;
+
+    double oersted_current_at(double t) const {
+        double I = oe_current;
+        if (oe_kind == 1) I *= sin(2.0 * M_PI * oe_freq * t + oe_phase) + oe_offset;
+        else if (oe_kind == 2) I *= (t >= oe_t_on && t < oe_t_off) ? 1.0 : 0.0;
+        return I;
+    }
+    // I(t_stage) for the stages, I(t_final) for the final evaluation, enqueued on the stream
+    // ahead of the launches (or graph) that read them
+    bool set_oersted(double t_stage, double t_final) {
+        if (!has_oersted) return true;
+        const float v[2] = {(float)oersted_current_at(t_stage), (float)oersted_current_at(t_final)};
+        return !cuda_fail("Oersted current", cudaMemcpyAsync(oe_dev, v, sizeof(v), cudaMemcpyHostToDevice, stream));
+    }
     float2 *X = nullptr, *Y = nullptr;
     float *kern = nullptr;
     uint8_t *mask = nullptr;
@@ -275,6 +295,10 @@ struct Engine {
             if (km) cudaFree(km);
             km = nullptr;
         }
+        if (h_oe) cudaFree(h_oe);
+        if (oe_dev) cudaFree(oe_dev);
+        h_oe = nullptr;
+        oe_dev = nullptr;
         if (arena) cudaFree(arena);
         arena = nullptr;
         if (staging) cudaFree(staging);
@@ -472,6 +496,8 @@ struct Engine {
         q.out = hextra;
         q.partials = p.partials ? xpart : nullptr;
         q.torques = torques_off ? 0 : 1;
+        q.h_oe = h_oe;
+        q.oe_scale = oe_dev ? oe_dev + (p.partials ? 1 : 0) : nullptr;
         launches += 1;
         if (cuda_fail("extra field", launch_extra_field(q, stream))) return false;
         p.hmap = hextra;
@@ -633,6 +659,7 @@ struct Engine {
 
     // RHS at the committed state -> K[0], statistics, optionally observables.
     bool eval_state(bool write_fields) {
+        if (!set_oersted(time, time)) return false;
         if (!pass_forward(S[cur])) return false;
         bool fields_written = false;
         if (write_fields && has_torque) {
@@ -789,6 +816,8 @@ struct Engine {
     int step_fixed(double dt) {
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
+        // the stages see I(t); the final evaluation gives the next step's k1, at I(t + dt)
+        if (!set_oersted(time, time + dt)) return -1;
         if (poll == nullptr && use_graphs && !ktime) {
             if ((!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
                 // capture unavailable: clear the sticky state and fall back to eager launches
@@ -933,6 +962,8 @@ struct Engine {
     int begin_dp45_attempt(double dt) {
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
+        // every stage and the first-same-as-last derivative see I(t), as the reference's do
+        if (!set_oersted(time, time)) return -1;
         dp45_dt = dt;
         if (poll == nullptr && use_graphs && !ktime) {
             if (!dexec[cur] && !capture_dp45()) {
@@ -985,6 +1016,7 @@ struct Engine {
     double fixed_dt = 0.0;
     int begin_fixed_step(double dt) {
         if (!ensure_k1()) return -1;
+        if (!set_oersted(time, time + dt)) return -1;
         if (use_graphs && (!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
             cudaGetLastError();
             use_graphs = false;
@@ -1375,6 +1407,7 @@ struct Engine {
         if (abm_last_dt > 0.0 && std::fabs(dt - abm_last_dt) / abm_last_dt > 0.1) abm_startup = 0;
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
+        if (!set_oersted(time, time + dt)) return -1;
         const int nxt = 1 - cur;
         if (abm_startup < 3) {
             const int rc = enqueue_fixed_step(dt, true);  // the Heun sequence (ends with K[0] = f at S[nxt])
@@ -1663,7 +1696,6 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                                integrator != FULLMAG_FDM_INTEGRATOR_ABM3,
                     "integrators other than HEUN, RK4, DP45, RK23, ABM3") ||
         unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
-        unsupported(*this, plan->has_oersted_cylinder != 0, "Oersted field") ||
         unsupported(*this, plan->region_mask != nullptr, "region masks / exchange LUT") ||
         unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers"))
         return false;
@@ -1863,7 +1895,21 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
             mat.has_cub = 0;
         }
     }
-    has_extra = ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque || xf.aniso);
+    has_oersted = plan->has_oersted_cylinder != 0;
+    if (has_oersted) {
+        if (!(plan->oersted_radius > 0.0)) {
+            last_error = "oersted_radius must be positive";
+            return false;
+        }
+        oe_kind = (int)plan->oersted_time_dep_kind;
+        oe_current = plan->oersted_current;
+        oe_freq = plan->oersted_time_dep_freq;
+        oe_phase = plan->oersted_time_dep_phase;
+        oe_offset = plan->oersted_time_dep_offset;
+        oe_t_on = plan->oersted_time_dep_t_on;
+        oe_t_off = plan->oersted_time_dep_t_off;
+    }
+    has_extra = (ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque || xf.aniso)) || has_oersted;
 
     // ---- device and stream ----
     if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;
@@ -1970,6 +2016,25 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         xf.kc1m = kmaps[2];
         xf.kc2m = kmaps[3];
         xf.kc3m = kmaps[4];
+    }
+    if (has_oersted) {
+        // field of a z-directed cylinder through (cx, cy) for I = 1 A at the cell centres:
+        // H_phi = r / (2 pi R^2) inside, 1 / (2 pi r) outside, zero on the axis
+        const double R = plan->oersted_radius, cx = plan->oersted_center[0], cy = plan->oersted_center[1];
+        std::vector<float> f(3 * (size_t)g.n, 0.f);
+        for (long long i = 0; i < g.n; ++i) {
+            const long long ix = i % g.nx, iy = (i / g.nx) % g.ny;
+            const double ddx = (ix + 0.5) * dx - cx, ddy = (iy + 0.5) * dy - cy;
+            const double r = sqrt(ddx * ddx + ddy * ddy);
+            if (r < 1e-30) continue;
+            const double hphi = r < R ? r / (2.0 * M_PI * R * R) : 1.0 / (2.0 * M_PI * r);
+            f[i] = (float)(-hphi * ddy / r);
+            f[g.n + i] = (float)(hphi * ddx / r);
+        }
+        if (cuda_fail("cudaMalloc(Oersted field)", cudaMalloc((void **)&h_oe, sizeof(float) * f.size())) ||
+            cuda_fail("cudaMalloc(Oersted current)", cudaMalloc((void **)&oe_dev, 2 * sizeof(float))) ||
+            cuda_fail("Oersted field upload", cudaMemcpy(h_oe, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice)))
+            return false;
     }
     if (cuda_fail("cudaMallocHost(dt)", cudaMallocHost((void **)&dt_host, sizeof(double)))) return false;
     dt_dev = dstats + kNumStats;  // slot kNumStats holds dt (kStatSlots)

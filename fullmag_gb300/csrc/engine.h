@@ -194,6 +194,9 @@ struct ExtraField {
     float ku1, ku2, kc1, kc2, kc3;                  // uniform values (J/m^3)
     float inv_mu0ms;                                // 1 / (mu0 Ms)
     float u[3], c1[3], c2[3], c3[3];
+    // Oersted field: oe_scale[0] * h_oe (I(t) times the field for 1 A, SoA) or NULL
+    const float *h_oe;
+    const float *oe_scale;
 };
 int extra_field_blocks(const Grid &g);
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);

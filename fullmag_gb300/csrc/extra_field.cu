@@ -8,6 +8,9 @@
 //   magnetoelastic field (B1, B2, prescribed strain; shear strains halved from Voigt)
 //                                               native/backends/fdm/src/demag_fp32.cu:368-376,582-583
 //   DMI energy (FP64 sums of the FP32 state)    native/backends/fdm/src/reductions_fp64.cu:647-720
+//   Oersted field of a cylindrical conductor, scaled by I(t)
+//                                               native/backends/fdm/src/context.cu:844-905,
+//                                               demag_fp32.cu:585-616
 //   Zhang-Li and Slonczewski spin-transfer torque, spin-orbit torque
 //                                               native/backends/fdm/src/llg_fp32.cu:65-195
 //                                               prefactors api.cpp:250-300, context.hpp:321-339
@@ -208,6 +211,12 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                 ax += p.tq_a * tx + p.tq_b * (my * tz - mz * ty);
                 ay += p.tq_a * ty + p.tq_b * (mz * tx - mx * tz);
                 az += p.tq_a * tz + p.tq_b * (mx * ty - my * tx);
+            }
+            if (p.h_oe) {  // counted in no energy, as the reference's energies leave it out
+                const float I = *p.oe_scale;
+                ax += I * p.h_oe[i];
+                ay += I * p.h_oe[n + i];
+                az += I * p.h_oe[2 * n + i];
             }
             hx = ax;
             hy = ay;

@@ -426,6 +426,8 @@ struct fo_problem {
     int has_zl, has_slon, has_sot;
     double zl_u[3], slon_pf, slon_P, sot_amp, sot_s[3];
     double *kmap[5]; /* per-cell Ku1 Ku2 Kc1 Kc2 Kc3 or NULL */
+    double *h_oe;    /* Oersted field for I = 1 A (AoS) or NULL */
+    double oe_scale; /* current I(t) of the evaluations in progress */
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
     uint32_t *region; /* optional region ids */
     double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
@@ -454,6 +456,7 @@ void fo_destroy(fo_problem *pr) {
     for (int s = 0; s < 7; ++s) free(pr->k[s]);
     for (int s = 0; s < 3; ++s) free(pr->abm_h[s]);
     for (int s = 0; s < 5; ++s) free(pr->kmap[s]);
+    free(pr->h_oe);
     free(pr);
 }
 
@@ -481,6 +484,22 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
                 memcpy(pr->kmap[k], src[k], sizeof(double) * (size_t)nc);
             }
         pr->p.ku1_field = pr->p.ku2_field = pr->p.kc1_field = pr->p.kc2_field = pr->p.kc3_field = NULL;
+    }
+    if (p->has_oersted && p->oersted_radius > 0.0) {
+        /* field of a z-directed cylinder for I = 1 A at the cell centres: H_phi = r / (2 pi R^2)
+         * inside, 1 / (2 pi r) outside, zero on the axis (context.cu:844-905) */
+        const long nc = (long)p->nx * p->ny * p->nz;
+        const double R = p->oersted_radius, cx = p->oersted_center[0], cy = p->oersted_center[1];
+        pr->h_oe = dalloc(3 * nc);
+        for (long i = 0; i < nc; ++i) {
+            const long ix = i % p->nx, iy = (i / p->nx) % p->ny;
+            const double ddx = (ix + 0.5) * p->dx - cx, ddy = (iy + 0.5) * p->dy - cy;
+            const double r = sqrt(ddx * ddx + ddy * ddy);
+            if (r < 1e-30) continue;
+            const double hphi = r < R ? r / (2.0 * M_PI * R * R) : 1.0 / (2.0 * M_PI * r);
+            pr->h_oe[3 * i] = -hphi * ddy / r;
+            pr->h_oe[3 * i + 1] = hphi * ddx / r;
+        }
     }
     pr->n = (long)p->nx * p->ny * p->nz;
     const long n3 = 3 * pr->n;
@@ -788,6 +807,14 @@ static double dmi_energy_cell(const fo_problem *pr, const double *m, long i) {
     return e;
 }
 
+/* Current of the Oersted conductor at time t (demag_fp32.cu:586-606). */
+static double oersted_scale(const fo_params *p, double t) {
+    double I = p->oersted_current;
+    if (p->oersted_kind == 1) I *= sin(2.0 * M_PI * p->oersted_freq * t + p->oersted_phase) + p->oersted_offset;
+    else if (p->oersted_kind == 2) I *= (t >= p->oersted_t_on && t < p->oersted_t_off) ? 1.0 : 0.0;
+    return I;
+}
+
 static void cross3(const double *a, const double *b, double *o) {
     o[0] = a[1] * b[2] - a[2] * b[1];
     o[1] = a[2] * b[0] - a[0] * b[2];
@@ -862,6 +889,8 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
                 for (int c = 0; c < 3; ++c) h[c] += pr->hmap[3 * i + c];
             anis_field_cell(pr, m + 3 * i, i, h);
             dmi_mel_field_cell(pr, m, i, h);
+            if (pr->h_oe)
+                for (int c = 0; c < 3; ++c) h[c] += pr->oe_scale * pr->h_oe[3 * i + c];
         }
         for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
         if (rhs) {
@@ -874,6 +903,7 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
 int fo_fields(fo_problem *pr, const double *m_aos, double *h_ex, double *h_demag, double *h_ext,
               double *h_eff, double *rhs) {
     const long n3 = 3 * pr->n;
+    pr->oe_scale = oersted_scale(&pr->p, pr->t);
     double *m = dalloc(n3), *a = dalloc(n3), *b = dalloc(n3), *e = dalloc(n3), *r = dalloc(n3);
     for (long i = 0; i < pr->n; ++i)
         for (int c = 0; c < 3; ++c) m[3 * i + c] = active(pr, i) ? m_aos[3 * i + c] : 0.0;
@@ -968,6 +998,7 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
 
 int fo_observe(fo_problem *pr, fo_stats *st) {
     const long n3 = 3 * pr->n;
+    pr->oe_scale = oersted_scale(&pr->p, pr->t);
     double *a = dalloc(n3), *b = dalloc(n3), *r = dalloc(n3);
     eval_fields(pr, pr->m, a, b, pr->heff, r);
     memset(st, 0, sizeof(*st));
@@ -1068,6 +1099,9 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st) {
     const fo_params *p = &pr->p;
     const long n3 = 3 * pr->n;
     memcpy(pr->m0, pr->m, sizeof(double) * n3);
+    /* every stage of a step (and of its retries) sees the Oersted current at the step's
+     * start, as the GPU backend evaluates it from the time before the update */
+    pr->oe_scale = oersted_scale(p, pr->t);
     double rejected = 0.0, suggested = 0.0;
     if (p->integrator == 1) { /* Heun: fdm_integrators.rs:87-153 */
         heun_step(pr, dt);
@@ -1085,6 +1119,7 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st) {
             h[2] = h[1];
             h[1] = h[0];
             h[0] = t;
+            pr->oe_scale = oersted_scale(p, pr->t + dt);  /* evaluated after the time update */
             rhs_of(pr, pr->m, h[0]);
             pr->abm_startup += 1;
         } else {

@@ -82,6 +82,12 @@ typedef struct {
     /* optional per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (J/m^3, one per cell), copied at create
      * (native/backends/fdm/src/demag_fp32.cu:275-292) */
     const double *ku1_field, *ku2_field, *kc1_field, *kc2_field, *kc3_field;
+    /* Oersted field of a cylindrical conductor along z through (cx, cy), radius R, current
+     * I(t): kind 0 constant, 1 I (sin(2 pi f t + phase) + offset), 2 I on [t_on, t_off)
+     * (native/backends/fdm/src/context.cu:826-905, demag_fp32.cu:585-616) */
+    int32_t has_oersted, oersted_kind;
+    double oersted_current, oersted_radius, oersted_center[3];
+    double oersted_freq, oersted_phase, oersted_offset, oersted_t_on, oersted_t_off;
 } fo_params;
 
 #define FO_MAX_REGIONS 256

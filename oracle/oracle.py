@@ -57,6 +57,10 @@ class Params(C.Structure):
         ("sot_sigma", C.c_double * 3), ("sot_thickness", C.c_double),
         ("ku1_field", C.c_void_p), ("ku2_field", C.c_void_p), ("kc1_field", C.c_void_p),
         ("kc2_field", C.c_void_p), ("kc3_field", C.c_void_p),
+        ("has_oersted", C.c_int32), ("oersted_kind", C.c_int32),
+        ("oersted_current", C.c_double), ("oersted_radius", C.c_double), ("oersted_center", C.c_double * 3),
+        ("oersted_freq", C.c_double), ("oersted_phase", C.c_double), ("oersted_offset", C.c_double),
+        ("oersted_t_on", C.c_double), ("oersted_t_off", C.c_double),
     ]
 
 
@@ -163,7 +167,9 @@ class Problem:
                  current_density=(0.0, 0.0, 0.0), stt_degree=0.0, stt_beta=0.0, stt_p=(0.0, 0.0, 0.0),
                  stt_lambda=0.0, stt_epsilon_prime=0.0, sot_je=None, sot_xi_dl=0.0, sot_xi_fl=0.0,
                  sot_sigma=(0.0, 0.0, 1.0), sot_thickness=0.0,
-                 ku1_field=None, ku2_field=None, kc1_field=None, kc2_field=None, kc3_field=None):
+                 ku1_field=None, ku2_field=None, kc1_field=None, kc2_field=None, kc3_field=None,
+                 oersted_current=None, oersted_radius=0.0, oersted_center=(0.0, 0.0, 0.0), oersted_kind=0,
+                 oersted_freq=0.0, oersted_phase=0.0, oersted_offset=0.0, oersted_t_on=0.0, oersted_t_off=0.0):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -197,6 +203,13 @@ class Problem:
         p.sot_je, p.sot_xi_dl, p.sot_xi_fl = (sot_je or 0.0), sot_xi_dl, sot_xi_fl
         p.sot_sigma[:] = list(sot_sigma)
         p.sot_thickness = sot_thickness
+        if oersted_current is not None and not oersted_radius > 0.0:
+            raise ValueError("oersted_radius must be positive")
+        p.has_oersted = int(oersted_current is not None)
+        p.oersted_current, p.oersted_radius = (oersted_current or 0.0), oersted_radius
+        p.oersted_center[:] = list(oersted_center)
+        p.oersted_kind, p.oersted_freq, p.oersted_phase = oersted_kind, oersted_freq, oersted_phase
+        p.oersted_offset, p.oersted_t_on, p.oersted_t_off = oersted_offset, oersted_t_on, oersted_t_off
         self._kmaps = {}
         for name, arr in (("ku1_field", ku1_field), ("ku2_field", ku2_field), ("kc1_field", kc1_field),
                           ("kc2_field", kc2_field), ("kc3_field", kc3_field)):
