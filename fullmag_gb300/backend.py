@@ -85,6 +85,7 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               oersted_freq: float = 0.0, oersted_phase: float = 0.0, oersted_offset: float = 0.0,
               oersted_t_on: float = 0.0, oersted_t_off: float = 0.0,
               active_mask: Optional[np.ndarray] = None,
+              region_mask: Optional[np.ndarray] = None, exchange_lut: Optional[np.ndarray] = None,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
               adaptive_dt_max: float = 0.0, adaptive_headroom: float = 0.0,
@@ -147,9 +148,6 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
     p.oersted_time_dep_freq, p.oersted_time_dep_phase = oersted_freq, oersted_phase
     p.oersted_time_dep_offset = oersted_offset
     p.oersted_time_dep_t_on, p.oersted_time_dep_t_off = oersted_t_on, oersted_t_off
-    p.sot_sigma[:] = [0.0, 0.0, 1.0]
-    p.sot_thickness = 1e-9
-    p.oersted_axis[:] = [0.0, 0.0, 1.0]
     if spectra is not None and enable_demag:
         sp = np.ascontiguousarray(spectra, dtype=np.float64)
         keep.append(sp)
@@ -162,6 +160,16 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
         keep.append(mk)
         p.active_mask = mk.ctypes.data_as(C.POINTER(C.c_uint8))
         p.active_mask_len = mk.size
+    if region_mask is not None:  # region ids per cell and the optional 256 x 256 A_ij table
+        rg = np.ascontiguousarray(region_mask, dtype=np.uint32).reshape(-1)
+        keep.append(rg)
+        p.region_mask = rg.ctypes.data_as(C.POINTER(C.c_uint32))
+        p.region_mask_len = rg.size
+        if exchange_lut is not None:
+            lt = np.ascontiguousarray(exchange_lut, dtype=np.float64).reshape(-1)
+            keep.append(lt)
+            p.exchange_lut = _dptr(lt)
+            p.exchange_lut_len = lt.size
     m = np.ascontiguousarray(m0, dtype=np.float64).reshape(-1)
     keep.append(m)
     p.initial_magnetization_xyz = _dptr(m)

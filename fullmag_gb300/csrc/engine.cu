@@ -33,9 +33,9 @@ namespace fm {
 
 static constexpr double kMu0 = 4.0 * M_PI * 1e-7;
 // device statistics slots: the kNumStats row-pass statistics, the step size of graph
-// replays, and the extra field pass's four sums (ExtraSums: Zeeman m.(H_ext + H_map), DMI,
-// uniaxial and cubic energy densities)
-static constexpr int kStatSlots = kNumStats + 5;
+// replays, and the extra field pass's five sums (ExtraSums: Zeeman m.(H_ext + H_map), DMI,
+// uniaxial and cubic energy densities, region exchange pair sum)
+static constexpr int kStatSlots = kNumStats + 6;
 
 bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
                          std::string &err);
@@ -224,6 +224,10 @@ struct Engine {
     float *hextra = nullptr;
     ExtraSums *xpart = nullptr;
     float *kmaps[5] = {};  // per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (device, FP32) or NULL
+    // exchange with region ids (api.cpp:405-420): ids and the FP64 stiffness table on the
+    // device; the whole exchange term then runs in the extra pass
+    uint32_t *regions = nullptr;
+    double *lut = nullptr;
     // Oersted field (context.cu:844-905, demag_fp32.cu:585-616): the field for 1 A and the
     // device scales I(t): [0] for the stages of a step, [1] for its final evaluation
     bool has_oersted = false;
@@ -295,6 +299,10 @@ struct Engine {
             if (km) cudaFree(km);
             km = nullptr;
         }
+        if (regions) cudaFree(regions);
+        if (lut) cudaFree(lut);
+        regions = nullptr;
+        lut = nullptr;
         if (h_oe) cudaFree(h_oe);
         if (oe_dev) cudaFree(oe_dev);
         h_oe = nullptr;
@@ -498,6 +506,10 @@ struct Engine {
         q.torques = torques_off ? 0 : 1;
         q.h_oe = h_oe;
         q.oe_scale = oe_dev ? oe_dev + (p.partials ? 1 : 0) : nullptr;
+        if (xf.region) {  // the row pass's exchange is off: this pass writes H_EX
+            q.h_ex_out = p.h_ex_out;
+            p.h_ex_out = nullptr;
+        }
         launches += 1;
         if (cuda_fail("extra field", launch_extra_field(q, stream))) return false;
         p.hmap = hextra;
@@ -640,7 +652,8 @@ struct Engine {
 
     void fill_stats(const double *d, fullmag_fdm_step_stats &st) const {
         const double V = dx * dy * dz;
-        st.exchange_energy_joules = exchange ? a_ex * V * d[0] : 0.0;
+        // with region ids the exchange pair sum is the extra pass's (slot kNumStats + 5, A inside)
+        st.exchange_energy_joules = exchange ? (xf.region ? V * d[kNumStats + 5] : a_ex * V * d[0]) : 0.0;
         st.demag_energy_joules = demag ? -0.5 * kMu0 * ms * V * d[1] : 0.0;
         // with an extra pass, the row pass's field-map sum includes its terms; the Zeeman
         // sum m.(H_ext + H_map) then comes from the extra pass (slot kNumStats + 1)
@@ -1677,6 +1690,18 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                      std::to_string(plan->initial_magnetization_len);
         return false;
     }
+    if (plan->region_mask && plan->region_mask_len != (uint64_t)g.n) {
+        last_error = "region_mask_len mismatch: expected " + std::to_string(g.n) + ", got " +
+                     std::to_string(plan->region_mask_len);
+        return false;
+    }
+    if (plan->region_mask) {  // ids index a 256-row table; larger ids have no row
+        for (long long i = 0; i < g.n; ++i)
+            if (plan->region_mask[i] >= FULLMAG_FDM_MAX_EXCHANGE_REGIONS) {
+                last_error = "region_mask ids must be below " + std::to_string(FULLMAG_FDM_MAX_EXCHANGE_REGIONS);
+                return false;
+            }
+    }
     if (plan->active_mask && plan->active_mask_len != (uint64_t)g.n) {
         last_error = "active_mask_len mismatch: expected " + std::to_string(g.n) + ", got " +
                      std::to_string(plan->active_mask_len);
@@ -1696,7 +1721,6 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                                integrator != FULLMAG_FDM_INTEGRATOR_ABM3,
                     "integrators other than HEUN, RK4, DP45, RK23, ABM3") ||
         unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
-        unsupported(*this, plan->region_mask != nullptr, "region masks / exchange LUT") ||
         unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers"))
         return false;
 
@@ -1909,7 +1933,20 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         oe_t_on = plan->oersted_time_dep_t_on;
         oe_t_off = plan->oersted_time_dep_t_off;
     }
-    has_extra = (ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque || xf.aniso)) || has_oersted;
+    // exchange with region ids (exchange_fp32.cu:48-104) moves whole to the extra pass
+    const bool region_exchange = plan->region_mask && exchange && ms > 0.0;
+    if (region_exchange) {
+        xf.ex_s = (float)(2.0 / mu0ms);
+        xf.idx2 = mat.idx2;
+        xf.idy2 = mat.idy2;
+        xf.idz2 = mat.idz2;
+        xf.didx2 = 1.0 / (dx * dx);
+        xf.didy2 = 1.0 / (dy * dy);
+        xf.didz2 = 1.0 / (dz * dz);
+        mat.ex_pref = 0.f;
+    }
+    has_extra = (ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque || xf.aniso)) || has_oersted ||
+                region_exchange;
 
     // ---- device and stream ----
     if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;
@@ -2016,6 +2053,24 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         xf.kc1m = kmaps[2];
         xf.kc2m = kmaps[3];
         xf.kc3m = kmaps[4];
+    }
+    if (region_exchange) {
+        // the caller's table when it has 256 x 256 entries, else A on the diagonal
+        // (api.cpp:405-420)
+        constexpr size_t R = FULLMAG_FDM_MAX_EXCHANGE_REGIONS;
+        std::vector<double> table(R * R, 0.0);
+        if (plan->exchange_lut && plan->exchange_lut_len == R * R)
+            std::copy(plan->exchange_lut, plan->exchange_lut + R * R, table.begin());
+        else
+            for (size_t r = 0; r < R; ++r) table[r * R + r] = a_ex;
+        if (cuda_fail("cudaMalloc(region ids)", cudaMalloc((void **)&regions, sizeof(uint32_t) * (size_t)g.n)) ||
+            cuda_fail("cudaMalloc(exchange table)", cudaMalloc((void **)&lut, sizeof(double) * R * R)) ||
+            cuda_fail("region ids upload",
+                      cudaMemcpy(regions, plan->region_mask, sizeof(uint32_t) * (size_t)g.n, cudaMemcpyHostToDevice)) ||
+            cuda_fail("exchange table upload", cudaMemcpy(lut, table.data(), sizeof(double) * R * R, cudaMemcpyHostToDevice)))
+            return false;
+        xf.region = regions;
+        xf.lut = lut;
     }
     if (has_oersted) {
         // field of a z-directed cylinder through (cx, cy) for I = 1 A at the cell centres:

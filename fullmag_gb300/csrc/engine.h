@@ -155,9 +155,10 @@ size_t y_convolve_2d_smem(const Grid &g, int tx);
 // and the magnetoelastic field of a prescribed strain, plus the applied field map.  The
 // row pass adds `out` as its field map; H = 0 at inactive cells.
 // per-CTA sums of the extra field pass (FP64): Zeeman m.(H_ext + H_map), DMI energy density,
-// and with per-cell anisotropy maps the uniaxial and cubic energy densities
+// with per-cell anisotropy maps the uniaxial and cubic energy densities, and with region ids
+// the exchange pair sum sum A_ij |m_j - m_i|^2 / d^2
 struct ExtraSums {
-    double zee, dmi, uni, cub;
+    double zee, dmi, uni, cub, exch;
 };
 
 struct ExtraField {
@@ -197,10 +198,19 @@ struct ExtraField {
     // Oersted field: oe_scale[0] * h_oe (I(t) times the field for 1 A, SoA) or NULL
     const float *h_oe;
     const float *oe_scale;
+    // exchange with region ids (exchange_fp32.cu:48-104): 2/(mu0 Ms) sum_q A[r_i][r_q] (m_q - m_i)/d_q^2
+    // with A from the 256 x 256 FP64 table, read as FP32 for the field; the row pass's
+    // exchange is off, and this pass writes the H_EX observable (h_ex_out) when asked
+    const uint32_t *region;    // region id per cell (< 256) or NULL
+    const double *lut;         // exchange stiffness table, row-major [r_i][r_j] (J/m)
+    float ex_s;                // 2 / (mu0 Ms)
+    float idx2, idy2, idz2;    // 1 / d^2
+    double didx2, didy2, didz2;
+    float *h_ex_out;
 };
 int extra_field_blocks(const Grid &g);
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);
-// sums the per-CTA partials into out[0..3] (fixed order)
+// sums the per-CTA partials into out[0..4] (fixed order)
 cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s);
 
 // Adjoint (reverse-mode RK4): the final-combination pass (adjoint.cu); all fields SoA.

@@ -14,6 +14,9 @@
 //   Zhang-Li and Slonczewski spin-transfer torque, spin-orbit torque
 //                                               native/backends/fdm/src/llg_fp32.cu:65-195
 //                                               prefactors api.cpp:250-300, context.hpp:321-339
+//   exchange with region ids and a 256 x 256 stiffness table
+//                                               native/backends/fdm/src/exchange_fp32.cu:48-104,
+//                                               api.cpp:405-420, reductions_fp64.cu:123-215
 // A torque T perpendicular to m is passed as the field H = a T + b (m x T), which the row
 // pass's LLG right-hand side maps back to exactly T; m.H = 0, so it adds no energy.
 // The reference reports the bulk DMI energy as +V D m.(curl m) while its field is
@@ -37,22 +40,24 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// fixed-order block sum of the four partial sums; thread 0 returns the CTA's total
+// fixed-order block sum of the five partial sums; thread 0 returns the CTA's total
 __device__ __forceinline__ ExtraSums block_sum(ExtraSums v) {
     __shared__ ExtraSums red[kThreads / 32];
     v.zee = warp_sum(v.zee);
     v.dmi = warp_sum(v.dmi);
     v.uni = warp_sum(v.uni);
     v.cub = warp_sum(v.cub);
+    v.exch = warp_sum(v.exch);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    ExtraSums t{0.0, 0.0, 0.0, 0.0};
+    ExtraSums t{0.0, 0.0, 0.0, 0.0, 0.0};
     if (threadIdx.x == 0)
         for (int w = 0; w < kThreads / 32; ++w) {
             t.zee += red[w].zee;
             t.dmi += red[w].dmi;
             t.uni += red[w].uni;
             t.cub += red[w].cub;
+            t.exch += red[w].exch;
         }
     return t;
 }
@@ -61,13 +66,15 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
     const Grid &g = p.g;
     const long long n = g.n;
     const float *m = p.m;
-    double s_zee = 0.0, s_dmi = 0.0, s_uni = 0.0, s_cub = 0.0;
+    double s_zee = 0.0, s_dmi = 0.0, s_uni = 0.0, s_cub = 0.0, s_exch = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float hx = 0.f, hy = 0.f, hz = 0.f;
+        float rx = 0.f, ry = 0.f, rz = 0.f;  // region exchange (the H_EX observable)
         if (p.mask == nullptr || p.mask[i] != 0) {
             const float mx = m[i], my = m[n + i], mz = m[2 * n + i];
             float ax = 0.f, ay = 0.f, az = 0.f;  // DMI + magnetoelastic
-            if (p.has_int || p.has_bulk) {
+            if (p.has_int || p.has_bulk || p.region) {
+                // neighbours with the Neumann clamp: a missing or inactive neighbour is the cell itself
                 const int x = (int)(i % g.nx);
                 const long long r = i / g.nx;
                 const int y = (int)(r % g.ny), z = (int)(r / g.ny);
@@ -83,36 +90,71 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                     if (!p.mask[zm]) zm = i;
                     if (!p.mask[zp]) zp = i;
                 }
+                if (p.region) {
+                    // sum_q A[r_i][r_q] (m_q - m_i) / d_q^2 in the order x+, x-, y+, y-, z+, z-
+                    const double *row = p.lut + (size_t)p.region[i] * 256;
+                    const long long nb[6] = {xp, xm, yp, ym, zp, zm};
+                    const float w[6] = {p.idx2, p.idx2, p.idy2, p.idy2, p.idz2, p.idz2};
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        const long long j = nb[q];
+                        const float a = (float)row[p.region[j]] * w[q];
+                        rx += a * (m[j] - mx);
+                        ry += a * (m[n + j] - my);
+                        rz += a * (m[2 * n + j] - mz);
+                    }
+                    rx *= p.ex_s;
+                    ry *= p.ex_s;
+                    rz *= p.ex_s;
+                    ax += rx;
+                    ay += ry;
+                    az += rz;
+                    if (p.partials) {
+                        // forward pairs (x+1, y+1, z+1) with an active neighbour, each pair once,
+                        // the table read in FP64 as the reference's energy reduction does
+                        const double dw[3] = {p.didx2, p.didy2, p.didz2};
+                        const long long fw[3] = {xp, yp, zp};
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            const long long j = fw[a];
+                            if (j == i) continue;
+                            const double d0 = (double)m[j] - mx, d1 = (double)m[n + j] - my, d2 = (double)m[2 * n + j] - mz;
+                            s_exch += row[p.region[j]] * (d0 * d0 + d1 * d1 + d2 * d2) * dw[a];
+                        }
+                    }
+                }
                 // differences of neighbour values: component c of cell j at m[c n + j]
                 auto dif = [&](int c, long long a, long long b) { return m[c * n + a] - m[c * n + b]; };
-                const float dmx_dx = dif(0, xp, xm) * p.inv2dx, dmy_dx = dif(1, xp, xm) * p.inv2dx;
-                const float dmz_dx = dif(2, xp, xm) * p.inv2dx;
-                const float dmx_dy = dif(0, yp, ym) * p.inv2dy, dmy_dy = dif(1, yp, ym) * p.inv2dy;
-                const float dmz_dy = dif(2, yp, ym) * p.inv2dy;
-                const float dmx_dz = dif(0, zp, zm) * p.inv2dz, dmy_dz = dif(1, zp, zm) * p.inv2dz;
-                if (p.has_int) {
-                    ax += p.dmi_int * dmz_dx;
-                    ay += p.dmi_int * dmz_dy;
-                    az -= p.dmi_int * (dmx_dx + dmy_dy);
-                }
-                if (p.has_bulk) {
-                    ax += p.dmi_bulk * (dmz_dy - dmy_dz);
-                    ay += p.dmi_bulk * (dmx_dz - dmz_dx);
-                    az += p.dmi_bulk * (dmy_dx - dmx_dy);
-                }
-                if (p.partials) {
-                    // the energy sums take the differences in FP64 of the FP32 state
-                    auto ddif = [&](int c, long long a, long long b) { return (double)m[c * n + a] - (double)m[c * n + b]; };
-                    const double i2x = p.dinv2dx, i2y = p.dinv2dy, i2z = p.dinv2dz;
-                    const double Mx = mx, My = my, Mz = mz;
-                    if (p.has_int)
-                        s_dmi += p.d_int * (Mz * (ddif(0, xp, xm) * i2x + ddif(1, yp, ym) * i2y) - Mx * ddif(2, xp, xm) * i2x -
-                                            My * ddif(2, yp, ym) * i2y);
+                if (p.has_int || p.has_bulk) {
+                    const float dmx_dx = dif(0, xp, xm) * p.inv2dx, dmy_dx = dif(1, xp, xm) * p.inv2dx;
+                    const float dmz_dx = dif(2, xp, xm) * p.inv2dx;
+                    const float dmx_dy = dif(0, yp, ym) * p.inv2dy, dmy_dy = dif(1, yp, ym) * p.inv2dy;
+                    const float dmz_dy = dif(2, yp, ym) * p.inv2dy;
+                    const float dmx_dz = dif(0, zp, zm) * p.inv2dz, dmy_dz = dif(1, zp, zm) * p.inv2dz;
+                    if (p.has_int) {
+                        ax += p.dmi_int * dmz_dx;
+                        ay += p.dmi_int * dmz_dy;
+                        az -= p.dmi_int * (dmx_dx + dmy_dy);
+                    }
                     if (p.has_bulk) {
-                        const double cx = ddif(2, yp, ym) * i2y - ddif(1, zp, zm) * i2z;
-                        const double cy = ddif(0, zp, zm) * i2z - ddif(2, xp, xm) * i2x;
-                        const double cz = ddif(1, xp, xm) * i2x - ddif(0, yp, ym) * i2y;
-                        s_dmi += p.d_bulk * (Mx * cx + My * cy + Mz * cz);
+                        ax += p.dmi_bulk * (dmz_dy - dmy_dz);
+                        ay += p.dmi_bulk * (dmx_dz - dmz_dx);
+                        az += p.dmi_bulk * (dmy_dx - dmx_dy);
+                    }
+                    if (p.partials) {
+                        // the energy sums take the differences in FP64 of the FP32 state
+                        auto ddif = [&](int c, long long a, long long b) { return (double)m[c * n + a] - (double)m[c * n + b]; };
+                        const double i2x = p.dinv2dx, i2y = p.dinv2dy, i2z = p.dinv2dz;
+                        const double Mx = mx, My = my, Mz = mz;
+                        if (p.has_int)
+                            s_dmi += p.d_int * (Mz * (ddif(0, xp, xm) * i2x + ddif(1, yp, ym) * i2y) - Mx * ddif(2, xp, xm) * i2x -
+                                                My * ddif(2, yp, ym) * i2y);
+                        if (p.has_bulk) {
+                            const double cx = ddif(2, yp, ym) * i2y - ddif(1, zp, zm) * i2z;
+                            const double cy = ddif(0, zp, zm) * i2z - ddif(2, xp, xm) * i2x;
+                            const double cz = ddif(1, xp, xm) * i2x - ddif(0, yp, ym) * i2y;
+                            s_dmi += p.d_bulk * (Mx * cx + My * cy + Mz * cz);
+                        }
                     }
                 }
             }
@@ -241,21 +283,27 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
         p.out[i] = hx;
         p.out[n + i] = hy;
         p.out[2 * n + i] = hz;
+        if (p.h_ex_out) {
+            p.h_ex_out[i] = rx;
+            p.h_ex_out[n + i] = ry;
+            p.h_ex_out[2 * n + i] = rz;
+        }
     }
     if (p.partials) {
-        const ExtraSums t = block_sum(ExtraSums{s_zee, s_dmi, s_uni, s_cub});
+        const ExtraSums t = block_sum(ExtraSums{s_zee, s_dmi, s_uni, s_cub, s_exch});
         if (threadIdx.x == 0) p.partials[blockIdx.x] = t;
     }
 }
 
 __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSums *__restrict__ partials, int nblocks,
                                                                   double *__restrict__ out) {
-    ExtraSums v{0.0, 0.0, 0.0, 0.0};
+    ExtraSums v{0.0, 0.0, 0.0, 0.0, 0.0};
     for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
         v.zee += partials[k].zee;
         v.dmi += partials[k].dmi;
         v.uni += partials[k].uni;
         v.cub += partials[k].cub;
+        v.exch += partials[k].exch;
     }
     const ExtraSums t = block_sum(v);
     if (threadIdx.x == 0) {
@@ -263,6 +311,7 @@ __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSum
         out[1] = t.dmi;
         out[2] = t.uni;
         out[3] = t.cub;
+        out[4] = t.exch;
     }
 }
 

@@ -82,3 +82,21 @@ def test_null_safety_without_gpu():
     assert lib.fullmag_fdm_backend_last_error(None) == b"null handle"
     st = _abi.StepStats()
     assert lib.fullmag_fdm_backend_step(None, 1e-13, C.byref(st)) == _abi.ERR_INVALID
+
+
+def test_plan_builder_keeps_every_caller_value():
+    """make_plan fills each plan field from its argument (native_fdm.rs:132-499): the SOT
+    polarisation and thickness, the Oersted axis, region ids and the stiffness table reach
+    the plan unchanged."""
+    import numpy as np
+    from fullmag_gb300.backend import make_plan
+    reg = np.array([0, 1, 1, 2], dtype=np.uint32)
+    lut = np.arange(256 * 256, dtype=np.float64) * 1e-15
+    p, keep = make_plan(nx=4, ny=1, nz=1, dx=1e-9, dy=1e-9, dz=1e-9, ms=8e5, a_ex=1e-11, alpha=0.1,
+                        m0=np.tile([1.0, 0.0, 0.0], 4), sot_je=1.0, sot_sigma=(0.0, 1.0, 0.0),
+                        sot_thickness=2e-9, oersted_current=1.0, oersted_radius=1e-9,
+                        oersted_axis=(1.0, 0.0, 0.0), region_mask=reg, exchange_lut=lut)
+    assert list(p.sot_sigma) == [0.0, 1.0, 0.0] and p.sot_thickness == 2e-9
+    assert list(p.oersted_axis) == [1.0, 0.0, 0.0]
+    assert p.region_mask_len == 4 and [p.region_mask[i] for i in range(4)] == [0, 1, 1, 2]
+    assert p.exchange_lut_len == 256 * 256 and p.exchange_lut[257] == lut[257]

@@ -12,11 +12,15 @@ from test_gpu_parity import make_pair
 
 pytestmark = pytest.mark.gpu
 
+# The reference adds the Slonczewski and SOT torques to dm/dt with prefactors of order
+# hbar J / (2 e mu0 Ms t) per second, so the current densities below are chosen large enough
+# that each torque moves m by about 1e-3 over the 1 ps trajectories (at 1e11 A/m^2 they move
+# it by 2e-8, below the tolerance, and a wrong polarisation or thickness would pass).
 TORQUES = {
     "zhang_li": dict(current_density=(6e11, -2e11, 0.0), stt_degree=0.6, stt_beta=0.05),
-    "slonczewski": dict(current_density=(0.0, 0.0, 2e11), stt_p=(0.0, 0.6, 0.8), stt_lambda=1.5,
+    "slonczewski": dict(current_density=(0.0, 0.0, 2e16), stt_p=(0.0, 0.6, 0.8), stt_lambda=1.5,
                         stt_epsilon_prime=0.1),
-    "sot": dict(sot_je=1.5e11, sot_xi_dl=0.25, sot_xi_fl=-0.1, sot_sigma=(0.0, 1.0, 0.0), sot_thickness=1e-9),
+    "sot": dict(sot_je=1.5e16, sot_xi_dl=0.25, sot_xi_fl=-0.1, sot_sigma=(0.0, 1.0, 0.0), sot_thickness=2e-9),
 }
 
 
@@ -34,7 +38,7 @@ def test_torque_trajectory(gpu_lib, oracle, name, integrator):
 
 
 def test_heff_observable_leaves_torques_out(gpu_lib, oracle):
-    kw = problem(16, 10, 2, seed=72, alpha=0.1, **TORQUES["zhang_li"], sot_je=2e11, sot_xi_dl=0.3,
+    kw = problem(16, 10, 2, seed=72, alpha=0.1, **TORQUES["zhang_li"], sot_je=2e16, sot_xi_dl=0.3,
                  sot_sigma=(1.0, 0.0, 0.0))
     gpu, orc = make_pair(oracle, kw)
     gpu.step(5e-14)
