@@ -86,6 +86,7 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               oersted_t_on: float = 0.0, oersted_t_off: float = 0.0,
               active_mask: Optional[np.ndarray] = None,
               region_mask: Optional[np.ndarray] = None, exchange_lut: Optional[np.ndarray] = None,
+              temperature: float = 0.0,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
               adaptive_dt_max: float = 0.0, adaptive_headroom: float = 0.0,
@@ -107,6 +108,7 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
     p.precision = precision
     p.integrator = integrator
     p.disable_precession = int(disable_precession)
+    p.temperature = temperature
     p.enable_exchange = int(enable_exchange)
     p.enable_demag = int(enable_demag)
     p.has_external_field = int(h_ext is not None)

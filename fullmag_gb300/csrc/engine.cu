@@ -228,6 +228,14 @@ struct Engine {
     // device; the whole exchange term then runs in the extra pass
     uint32_t *regions = nullptr;
     double *lut = nullptr;
+    // Brown thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896): sigma^2 =
+    // th_pref / dt with the step's dt (1e-13 s for adaptive integrators); a step counter that
+    // advances once per completed step; th_dev[0] for the evaluations inside a step,
+    // th_dev[1] for its final evaluation (the next step's k1)
+    bool has_thermal = false;
+    double th_pref = 0.0, th_dt = 1e-13;
+    unsigned long long th_seed = 42, th_step = 0;
+    ThermalSlot *th_dev = nullptr;
     // Oersted field (context.cu:844-905, demag_fp32.cu:585-616): the field for 1 A and the
     // device scales I(t): [0] for the stages of a step, [1] for its final evaluation
     bool has_oersted = false;
@@ -243,6 +251,26 @@ struct Engine {
     }
     // I(t_stage) for the stages, I(t_final) for the final evaluation, enqueued on the stream
     // ahead of the launches (or graph) that read them
+    // the thermal keys and amplitude of a step's evaluations (counter c_stage) and of its
+    // final evaluation (c_final), written in stream order before the step's launches
+    bool set_thermal(unsigned long long c_stage, unsigned long long c_final) {
+        if (!has_thermal) return true;
+        const float sg = (float)sqrt(th_pref / th_dt);
+        const ThermalSlot v[2] = {{th_seed + c_stage * 0x9E3779B97F4A7C15ull, sg, 0.f},
+                                  {th_seed + c_final * 0x9E3779B97F4A7C15ull, sg, 0.f}};
+        return !cuda_fail("thermal keys", cudaMemcpyAsync(th_dev, v, sizeof(v), cudaMemcpyHostToDevice, stream));
+    }
+    // the amplitude's dt for a step of size dt; a change makes the stored k1 stale
+    void thermal_dt_for(double dt) {
+        if (!has_thermal) return;
+        const double d = adaptive() ? 1e-13 : dt;
+        if (d != th_dt) {
+            th_dt = d;
+            k1_valid = false;
+            stats_valid = false;
+            fields_valid = false;
+        }
+    }
     bool set_oersted(double t_stage, double t_final) {
         if (!has_oersted) return true;
         const float v[2] = {(float)oersted_current_at(t_stage), (float)oersted_current_at(t_final)};
@@ -303,6 +331,8 @@ struct Engine {
         if (lut) cudaFree(lut);
         regions = nullptr;
         lut = nullptr;
+        if (th_dev) cudaFree(th_dev);
+        th_dev = nullptr;
         if (h_oe) cudaFree(h_oe);
         if (oe_dev) cudaFree(oe_dev);
         h_oe = nullptr;
@@ -506,6 +536,7 @@ struct Engine {
         q.torques = torques_off ? 0 : 1;
         q.h_oe = h_oe;
         q.oe_scale = oe_dev ? oe_dev + (p.partials ? 1 : 0) : nullptr;
+        q.th = th_dev ? th_dev + (p.partials ? 1 : 0) : nullptr;
         if (xf.region) {  // the row pass's exchange is off: this pass writes H_EX
             q.h_ex_out = p.h_ex_out;
             p.h_ex_out = nullptr;
@@ -672,7 +703,7 @@ struct Engine {
 
     // RHS at the committed state -> K[0], statistics, optionally observables.
     bool eval_state(bool write_fields) {
-        if (!set_oersted(time, time)) return false;
+        if (!set_oersted(time, time) || !set_thermal(th_step, th_step)) return false;
         if (!pass_forward(S[cur])) return false;
         bool fields_written = false;
         if (write_fields && has_torque) {
@@ -695,7 +726,9 @@ struct Engine {
         RowPass p = row_base();
         p.x_in = X;
         p.m_in = S[cur];
-        p.k_out = K[0];
+        // a valid k1 stays: after DP45 / RK23 it is the first-same-as-last derivative, taken
+        // inside the step (with that step's Oersted current and thermal counter)
+        p.k_out = k1_valid ? nullptr : K[0];
         p.partials = partials;
         if (write_fields) {
             p.h_ex_out = h_ex;
@@ -827,10 +860,12 @@ struct Engine {
     }
 
     int step_fixed(double dt) {
+        thermal_dt_for(dt);
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
-        // the stages see I(t); the final evaluation gives the next step's k1, at I(t + dt)
-        if (!set_oersted(time, time + dt)) return -1;
+        // the stages see I(t) and the step's thermal counter; the final evaluation gives the
+        // next step's k1, at I(t + dt) and the next counter
+        if (!set_oersted(time, time + dt) || !set_thermal(th_step, th_step + 1)) return -1;
         if (poll == nullptr && use_graphs && !ktime) {
             if ((!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
                 // capture unavailable: clear the sticky state and fall back to eager launches
@@ -859,6 +894,7 @@ struct Engine {
         cur = 1 - cur;
         memcpy(stat_raw, raw, sizeof(stat_raw));
         step_count += 1;
+        th_step += 1;
         time += dt;
         k1_valid = true;
         stats_valid = true;
@@ -975,8 +1011,9 @@ struct Engine {
     int begin_dp45_attempt(double dt) {
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
-        // every stage and the first-same-as-last derivative see I(t), as the reference's do
-        if (!set_oersted(time, time)) return -1;
+        // every stage and the first-same-as-last derivative see I(t), as the reference's do,
+        // and the step's thermal counter
+        if (!set_oersted(time, time) || !set_thermal(th_step, th_step)) return -1;
         dp45_dt = dt;
         if (poll == nullptr && use_graphs && !ktime) {
             if (!dexec[cur] && !capture_dp45()) {
@@ -1021,6 +1058,9 @@ struct Engine {
             return 1;
         }
         next_dt = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
+        // a retry starts from k1 at the step's own thermal counter and Oersted current: the
+        // first-same-as-last derivative came from the previous step's evaluations
+        if (has_thermal || (has_oersted && oe_kind != 0)) k1_valid = false;
         return 0;
     }
 
@@ -1028,8 +1068,9 @@ struct Engine {
     bool fixed_pending = false;
     double fixed_dt = 0.0;
     int begin_fixed_step(double dt) {
+        thermal_dt_for(dt);
         if (!ensure_k1()) return -1;
-        if (!set_oersted(time, time + dt)) return -1;
+        if (!set_oersted(time, time + dt) || !set_thermal(th_step, th_step + 1)) return -1;
         if (use_graphs && (!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
             cudaGetLastError();
             use_graphs = false;
@@ -1418,9 +1459,10 @@ struct Engine {
 
     int step_abm3(double dt) {
         if (abm_last_dt > 0.0 && std::fabs(dt - abm_last_dt) / abm_last_dt > 0.1) abm_startup = 0;
+        thermal_dt_for(dt);
         if (!ensure_k1()) return -1;
         if (poll_hit()) return 1;
-        if (!set_oersted(time, time + dt)) return -1;
+        if (!set_oersted(time, time + dt) || !set_thermal(th_step, th_step + 1)) return -1;
         const int nxt = 1 - cur;
         if (abm_startup < 3) {
             const int rc = enqueue_fixed_step(dt, true);  // the Heun sequence (ends with K[0] = f at S[nxt])
@@ -1720,7 +1762,6 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
                                integrator != FULLMAG_FDM_INTEGRATOR_DP45 && integrator != FULLMAG_FDM_INTEGRATOR_RK23 &&
                                integrator != FULLMAG_FDM_INTEGRATOR_ABM3,
                     "integrators other than HEUN, RK4, DP45, RK23, ABM3") ||
-        unsupported(*this, plan->temperature > 0.0, "thermal noise") ||
         unsupported(*this, plan->boundary_correction != FULLMAG_FDM_BOUNDARY_NONE, "boundary correction tiers"))
         return false;
 
@@ -1945,8 +1986,14 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         xf.didz2 = 1.0 / (dz * dz);
         mat.ex_pref = 0.f;
     }
+    // thermal field: sigma^2 = 2 alpha kB T / (gamma (1 + alpha^2) mu0 Ms V dt)
+    // (crates/fullmag-engine/src/fdm_fields.rs:836-842; no noise without damping)
+    has_thermal = plan->temperature > 0.0 && ms > 0.0 && alpha > 0.0;
+    if (has_thermal)
+        th_pref = 2.0 * alpha * 1.380649e-23 * plan->temperature /
+                  (gamma * (1.0 + alpha * alpha) * 1.2566370614359173e-6 * ms * dx * dy * dz);
     has_extra = (ms > 0.0 && (xf.has_int || xf.has_bulk || xf.has_mel || has_torque || xf.aniso)) || has_oersted ||
-                region_exchange;
+                region_exchange || has_thermal;
 
     // ---- device and stream ----
     if (cuda_fail("cudaGetDevice", cudaGetDevice(&device))) return false;
@@ -2054,6 +2101,8 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         xf.kc2m = kmaps[3];
         xf.kc3m = kmaps[4];
     }
+    if (has_thermal && cuda_fail("cudaMalloc(thermal keys)", cudaMalloc((void **)&th_dev, 2 * sizeof(ThermalSlot))))
+        return false;
     if (region_exchange) {
         // the caller's table when it has 256 x 256 entries, else A on the diagonal
         // (api.cpp:405-420)

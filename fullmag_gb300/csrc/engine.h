@@ -160,6 +160,13 @@ size_t y_convolve_2d_smem(const Grid &g, int tx);
 struct ExtraSums {
     double zee, dmi, uni, cub, exch;
 };
+// Brown thermal field of one evaluation: key = seed + step counter * 0x9E3779B97F4A7C15
+// (wrapping) and the amplitude sigma (A/m); sigma 0 adds nothing
+struct ThermalSlot {
+    unsigned long long key;
+    float sigma;
+    float pad;
+};
 
 struct ExtraField {
     Grid g;
@@ -207,6 +214,8 @@ struct ExtraField {
     float idx2, idy2, idz2;    // 1 / d^2
     double didx2, didy2, didz2;
     float *h_ex_out;
+    // thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896) or NULL
+    const ThermalSlot *th;
 };
 int extra_field_blocks(const Grid &g);
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);

@@ -14,6 +14,8 @@
 //   Zhang-Li and Slonczewski spin-transfer torque, spin-orbit torque
 //                                               native/backends/fdm/src/llg_fp32.cu:65-195
 //                                               prefactors api.cpp:250-300, context.hpp:321-339
+//   Brown thermal field: SplitMix64 counter keyed by (seed, step, cell, stream), Box-Muller
+//                                               crates/fullmag-engine/src/fdm_fields.rs:818-896
 //   exchange with region ids and a 256 x 256 stiffness table
 //                                               native/backends/fdm/src/exchange_fp32.cu:48-104,
 //                                               api.cpp:405-420, reductions_fp64.cu:123-215
@@ -33,6 +35,24 @@ namespace fm {
 namespace {
 
 constexpr int kThreads = 256;
+
+// SplitMix64 output function (Vigna's published finaliser)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// u = ((bits >> 11) + 1) / (2^53 + 1) in (0, 1], as FP32
+__device__ __forceinline__ float unit_of(unsigned long long bits) { return (float)((bits >> 11) + 1ull) * 0x1p-53f; }
+
+// -2 ln u: logf of u itself up to u = 1/2, log1pf(-(1 - u)) above, with 1 - u formed from
+// the exact integer so that u near 1 keeps its relative accuracy
+__device__ __forceinline__ float neg2log_of(unsigned long long bits) {
+    const unsigned long long b = (bits >> 11) + 1ull;  // 1 .. 2^53
+    if (b <= (1ull << 52)) return -2.f * logf((float)b * 0x1p-53f);
+    return -2.f * log1pf(-(float)((1ull << 53) + 1ull - b) * 0x1p-53f);
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -259,6 +279,21 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                 ax += I * p.h_oe[i];
                 ay += I * p.h_oe[n + i];
                 az += I * p.h_oe[2 * n + i];
+            }
+            if (p.th) {  // in no energy sum, as in the reference
+                const float sg = p.th->sigma;
+                if (sg > 0.f) {
+                    constexpr unsigned long long kCell = 0x517CC1B727220A95ull, kStream = 0x6C62272E07BB0142ull;
+                    const unsigned long long key = p.th->key + (unsigned long long)i * kCell;
+                    const float r1 = sqrtf(neg2log_of(mix64(key)));
+                    const float r2 = sqrtf(neg2log_of(mix64(key + 2ull * kStream)));
+                    float s1, c1, s2, c2;
+                    sincospif(2.f * unit_of(mix64(key + kStream)), &s1, &c1);
+                    sincospif(2.f * unit_of(mix64(key + 3ull * kStream)), &s2, &c2);
+                    ax += sg * r1 * c1;
+                    ay += sg * r1 * s1;
+                    az += sg * r2 * c2;
+                }
             }
             hx = ax;
             hy = ay;

@@ -428,6 +428,10 @@ struct fo_problem {
     double *kmap[5]; /* per-cell Ku1 Ku2 Kc1 Kc2 Kc3 or NULL */
     double *h_oe;    /* Oersted field for I = 1 A (AoS) or NULL */
     double oe_scale; /* current I(t) of the evaluations in progress */
+    /* thermal field: step counter (advanced once per completed step), the counter and
+     * amplitude of the evaluations in progress, and the dt the amplitude is taken at */
+    uint64_t th_step, th_eval;
+    double th_sigma, th_dt;
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
     uint32_t *region; /* optional region ids */
     double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
@@ -472,6 +476,7 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     fo_problem *pr = (fo_problem *)calloc(1, sizeof(fo_problem));
     if (!pr) return NULL;
     pr->p = *p;
+    pr->th_dt = 1e-13;
     pr->p.active_mask = NULL;
     pr->p.region_mask = NULL;
     pr->p.exchange_lut = NULL;
@@ -807,6 +812,42 @@ static double dmi_energy_cell(const fo_problem *pr, const double *m, long i) {
     return e;
 }
 
+/* Thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896).  sigma at step size dt
+ * (the fixed step; 1e-13 s, the reference's default thermal_dt, for adaptive integrators). */
+static double thermal_sigma(const fo_params *p, double dt) {
+    if (!(p->temperature > 0.0) || !(p->ms > 0.0) || !(dt > 0.0)) return 0.0;
+    const double kb = 1.380649e-23, mu0 = 1.2566370614359173e-6;
+    const double gamma0 = p->gamma * (1.0 + p->alpha * p->alpha);
+    return sqrt(2.0 * p->alpha * kb * p->temperature / (gamma0 * mu0 * p->ms * p->dx * p->dy * p->dz * dt));
+}
+
+/* SplitMix64 output function (Vigna's published finaliser). */
+static uint64_t splitmix64_mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* Uniform in (0, 1] from the key seed + step C1 + cell C2 + stream C3 (wrapping). */
+static double counter_uniform(uint64_t seed, uint64_t step, uint64_t cell, uint64_t stream) {
+    const uint64_t key = seed + step * 0x9E3779B97F4A7C15ull + cell * 0x517CC1B727220A95ull + stream * 0x6C62272E07BB0142ull;
+    return ((double)(splitmix64_mix(key) >> 11) + 1.0) / (9007199254740992.0 + 1.0);
+}
+
+/* Adds sigma (r1 cos t1, r1 sin t1, r2 cos t2) at cell i, Box-Muller on four uniforms. */
+static void thermal_add(const fo_problem *pr, long i, double *h) {
+    const uint64_t seed = pr->p.thermal_seed, st = pr->th_eval, ci = (uint64_t)i;
+    double u1 = counter_uniform(seed, st, ci, 0), u3 = counter_uniform(seed, st, ci, 2);
+    if (u1 < 1e-300) u1 = 1e-300;
+    if (u3 < 1e-300) u3 = 1e-300;
+    const double u2 = counter_uniform(seed, st, ci, 1), u4 = counter_uniform(seed, st, ci, 3);
+    const double r1 = sqrt(-2.0 * log(u1)), r2 = sqrt(-2.0 * log(u3));
+    const double t1 = 2.0 * M_PI * u2, t2 = 2.0 * M_PI * u4;
+    h[0] += pr->th_sigma * r1 * cos(t1);
+    h[1] += pr->th_sigma * r1 * sin(t1);
+    h[2] += pr->th_sigma * r2 * cos(t2);
+}
+
 /* Current of the Oersted conductor at time t (demag_fp32.cu:586-606). */
 static double oersted_scale(const fo_params *p, double t) {
     double I = p->oersted_current;
@@ -891,6 +932,7 @@ static void eval_fields(fo_problem *pr, const double *m, double *h_ex, double *h
             dmi_mel_field_cell(pr, m, i, h);
             if (pr->h_oe)
                 for (int c = 0; c < 3; ++c) h[c] += pr->oe_scale * pr->h_oe[3 * i + c];
+            if (pr->th_sigma > 0.0) thermal_add(pr, i, h);
         }
         for (int c = 0; c < 3; ++c) h_eff[3 * i + c] = h[c];
         if (rhs) {
@@ -904,6 +946,8 @@ int fo_fields(fo_problem *pr, const double *m_aos, double *h_ex, double *h_demag
               double *h_eff, double *rhs) {
     const long n3 = 3 * pr->n;
     pr->oe_scale = oersted_scale(&pr->p, pr->t);
+    pr->th_eval = pr->th_step;
+    pr->th_sigma = thermal_sigma(&pr->p, pr->th_dt);
     double *m = dalloc(n3), *a = dalloc(n3), *b = dalloc(n3), *e = dalloc(n3), *r = dalloc(n3);
     for (long i = 0; i < pr->n; ++i)
         for (int c = 0; c < 3; ++c) m[3 * i + c] = active(pr, i) ? m_aos[3 * i + c] : 0.0;
@@ -996,9 +1040,13 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
     st->max_rhs = vmax_norm(rhs, pr->n);
 }
 
-int fo_observe(fo_problem *pr, fo_stats *st) {
+/* Statistics at the current state with the Oersted current at t_oe and the thermal field of
+ * step counter th (the evaluation of the state itself, or the last evaluation of a step). */
+static int observe_at(fo_problem *pr, fo_stats *st, double t_oe, uint64_t th) {
     const long n3 = 3 * pr->n;
-    pr->oe_scale = oersted_scale(&pr->p, pr->t);
+    pr->oe_scale = oersted_scale(&pr->p, t_oe);
+    pr->th_eval = th;
+    pr->th_sigma = thermal_sigma(&pr->p, pr->th_dt);
     double *a = dalloc(n3), *b = dalloc(n3), *r = dalloc(n3);
     eval_fields(pr, pr->m, a, b, pr->heff, r);
     memset(st, 0, sizeof(*st));
@@ -1008,6 +1056,8 @@ int fo_observe(fo_problem *pr, fo_stats *st) {
     free(a); free(b); free(r);
     return 0;
 }
+
+int fo_observe(fo_problem *pr, fo_stats *st) { return observe_at(pr, st, pr->t, pr->th_step); }
 
 static void rhs_of(fo_problem *pr, const double *m, double *k) {
     const long n3 = 3 * pr->n;
@@ -1100,8 +1150,17 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st) {
     const long n3 = 3 * pr->n;
     memcpy(pr->m0, pr->m, sizeof(double) * n3);
     /* every stage of a step (and of its retries) sees the Oersted current at the step's
-     * start, as the GPU backend evaluates it from the time before the update */
+     * start, as the GPU backend evaluates it from the time before the update, and the
+     * thermal field of the step counter, which advances once per completed step
+     * (fdm_problem.rs:244-245); its amplitude takes the fixed step, or 1e-13 s for the
+     * adaptive integrators (the reference's thermal_dt when no fixed step is set,
+     * fdm_problem.rs:92, cpu_reference.rs:287-290) */
+    const double t_start = pr->t;
+    const int adaptive = p->integrator == 2 || p->integrator == 5;
+    pr->th_dt = adaptive ? 1e-13 : dt;
     pr->oe_scale = oersted_scale(p, pr->t);
+    pr->th_eval = pr->th_step;
+    pr->th_sigma = thermal_sigma(p, pr->th_dt);
     double rejected = 0.0, suggested = 0.0;
     if (p->integrator == 1) { /* Heun: fdm_integrators.rs:87-153 */
         heun_step(pr, dt);
@@ -1120,6 +1179,7 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st) {
             h[1] = h[0];
             h[0] = t;
             pr->oe_scale = oersted_scale(p, pr->t + dt);  /* evaluated after the time update */
+            pr->th_eval = pr->th_step + 1;
             rhs_of(pr, pr->m, h[0]);
             pr->abm_startup += 1;
         } else {
@@ -1220,7 +1280,12 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st) {
     }
     pr->t += dt;
     pr->step += 1.0;
-    fo_observe(pr, st);
+    pr->th_step += 1;
+    /* the statistics of a step come from its last evaluation: at the new state after the
+     * time and counter update for the fixed-step integrators, the first-same-as-last
+     * derivative (inside the step) for DP45 and RK23 */
+    if (adaptive) observe_at(pr, st, t_start, pr->th_step - 1);
+    else fo_observe(pr, st);
     st->dt_used = dt;
     st->suggested_next_dt = suggested;
     st->rejected_attempts = rejected;

@@ -88,6 +88,11 @@ typedef struct {
     int32_t has_oersted, oersted_kind;
     double oersted_current, oersted_radius, oersted_center[3];
     double oersted_freq, oersted_phase, oersted_offset, oersted_t_on, oersted_t_off;
+    /* Brown thermal field at temperature T (K, 0 = none): counter-based Gaussian noise keyed
+     * by (seed, step counter, cell) with sigma^2 = 2 alpha kB T / (gamma (1 + alpha^2) mu0 Ms V dt)
+     * (crates/fullmag-engine/src/fdm_fields.rs:818-896, fdm_problem.rs:24-35,244-273) */
+    double temperature;
+    uint64_t thermal_seed;
 } fo_params;
 
 #define FO_MAX_REGIONS 256

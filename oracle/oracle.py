@@ -61,6 +61,7 @@ class Params(C.Structure):
         ("oersted_current", C.c_double), ("oersted_radius", C.c_double), ("oersted_center", C.c_double * 3),
         ("oersted_freq", C.c_double), ("oersted_phase", C.c_double), ("oersted_offset", C.c_double),
         ("oersted_t_on", C.c_double), ("oersted_t_off", C.c_double),
+        ("temperature", C.c_double), ("thermal_seed", C.c_uint64),
     ]
 
 
@@ -169,7 +170,8 @@ class Problem:
                  sot_sigma=(0.0, 0.0, 1.0), sot_thickness=0.0,
                  ku1_field=None, ku2_field=None, kc1_field=None, kc2_field=None, kc3_field=None,
                  oersted_current=None, oersted_radius=0.0, oersted_center=(0.0, 0.0, 0.0), oersted_kind=0,
-                 oersted_freq=0.0, oersted_phase=0.0, oersted_offset=0.0, oersted_t_on=0.0, oersted_t_off=0.0):
+                 oersted_freq=0.0, oersted_phase=0.0, oersted_offset=0.0, oersted_t_on=0.0, oersted_t_off=0.0,
+                 temperature=0.0, thermal_seed=42):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -210,6 +212,7 @@ class Problem:
         p.oersted_center[:] = list(oersted_center)
         p.oersted_kind, p.oersted_freq, p.oersted_phase = oersted_kind, oersted_freq, oersted_phase
         p.oersted_offset, p.oersted_t_on, p.oersted_t_off = oersted_offset, oersted_t_on, oersted_t_off
+        p.temperature, p.thermal_seed = temperature, thermal_seed
         self._kmaps = {}
         for name, arr in (("ku1_field", ku1_field), ("ku2_field", ku2_field), ("kc1_field", kc1_field),
                           ("kc2_field", kc2_field), ("kc3_field", kc3_field)):
