@@ -107,6 +107,11 @@ WORKLOADS = {
                                   kc1=-4.8e4, dt=2e-14, integrator="rk4", seed=3),
     "box_64x32x4_heun": dict(nx=64, ny=32, nz=4, d=4e-9, ms=8e5, a_ex=1.3e-11, alpha=0.5,
                              b_mt=(10.0, 5.0, 0.0), dt=5e-14, integrator="heun", seed=0),
+    # the volume with every term of the extra-field pass: interfacial DMI, magnetoelastic
+    # field, spin-orbit torque, a constant Oersted current, exchange with two regions and a
+    # table, a per-cell Ku1 map and the thermal field at 300 K
+    "volume_256x256x64_rk4_allterms": dict(nx=256, ny=256, nz=64, d=2e-9, ms=1.4e6, a_ex=2.1e-11, alpha=0.01,
+                                           kc1=-4.8e4, ku1=4e3, dt=2e-14, integrator="rk4", seed=3, terms="all"),
     "film_256x64x1_rk4": dict(nx=256, ny=64, nz=1, d=4e-9, ms=8e5, a_ex=1.3e-11, alpha=0.05,
                               b_mt=(5.0, 0.0, 0.0), dt=5e-14, integrator="rk4", seed=2),
     # thin film, adaptive Dormand-Prince (max error 1e-5), Ku = 5e3 J/m^3 along x, driven at
@@ -403,8 +408,34 @@ def plan_kwargs(w):
         kw.update(kc1=w["kc1"], c1=(1.0, 0.0, 0.0), c2=(0.0, 1.0, 0.0))
     if "ku1" in w:
         kw.update(ku1=w["ku1"], u_axis=(1.0, 0.0, 0.0))
+    if w.get("terms") == "all":
+        kw.update(extra_terms(w["nx"], w["ny"], w["nz"], d, w["seed"]))
     integ = {"rk4": _abi.INTEGRATOR_RK4, "heun": _abi.INTEGRATOR_HEUN, "dp45": _abi.INTEGRATOR_DP45}[w["integrator"]]
     return kw, integ
+
+
+def extra_terms(nx, ny, nz, d, seed):
+    """Plan keywords of every extra-field term, sized for an (nx, ny, nz) grid of cells d."""
+    n = nx * ny * nz
+    rng = np.random.default_rng(seed + 100)
+    x = np.tile(np.arange(nx, dtype=np.int64), ny * nz)
+    reg = np.where(x < nx // 2, 1, 2).astype(np.uint32)
+    lut = np.zeros((256, 256))
+    lut[1, 1], lut[2, 2], lut[1, 2], lut[2, 1] = 2.1e-11, 1.5e-11, 0.5e-11, 0.5e-11
+    return dict(dmi_d_interfacial=1.5e-3, mel_b1=-3e6, mel_b2=2e6, mel_strain=(1e-3, -5e-4, 2e-4, 1e-4, 0.0, 3e-4),
+                sot_je=1e11, sot_xi_dl=0.2, sot_xi_fl=0.05, sot_sigma=(0.0, 1.0, 0.0), sot_thickness=2e-9,
+                oersted_current=1e-3, oersted_radius=0.25 * nx * d[0],
+                oersted_center=(0.5 * nx * d[0], 0.5 * ny * d[1], 0.0),
+                region_mask=reg, exchange_lut=lut, ku1_field=rng.uniform(2e3, 6e3, n), temperature=300.0)
+
+
+def extra_bytes_per_cell(w):
+    """Algorithmic bytes per cell of one extra-field launch: m read and H_extra written
+    (12 + 12), plus the region id (4), the Ku1 map (4) and the Oersted field (12) when
+    present; the neighbour reads of DMI and exchange come from the same m rows."""
+    if w.get("terms") != "all":
+        return None
+    return 12 + 12 + 4 + 4 + 12
 
 
 def gpu_plan(w):
@@ -518,6 +549,19 @@ def cpu_baseline(w, threads):
     return {"value": sx * sy * sz * steps / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
             "sample": f"{steps} {w['integrator'].upper()} step(s) of {sx}x{sy}x{sz} (same physics, FP64, "
                       f"after 1 warm-up step), wall clock"}
+
+
+def extra_roofline(w, n, ktimes, peak):
+    """HBM roofline of the extra-field pass (None when the workload has no extra terms)."""
+    bpc = extra_bytes_per_cell(w)
+    ms, cnt = ktimes.get("extra_field", (0.0, 0))
+    if bpc is None or not cnt:
+        return None
+    avg_s = ms / cnt * 1e-3
+    ach = bpc * n / avg_s / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if peak else None,
+            "traffic": None, "kernel": "extra_field", "bytes_per_launch": bpc * n, "avg_launch_ms": avg_s * 1e3,
+            "launches_timed": cnt, "note": f"{bpc} B/cell algorithmic; CUDA events per launch"}
 
 
 def run_reference(args, w, name, rank, world):
@@ -722,6 +766,7 @@ def main():
                           "frac": achieved / peak if peak else None,
                           "note": f"whole step, compulsory-traffic model v1 {bpc:.1f} B/cell-step"},
         "kernel_times_ms_per_launch": {k: (v[0] / v[1] if v[1] else None) for k, v in ktimes.items()},
+        "roofline_extra": extra_roofline(w, n, ktimes, peak),
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
@@ -729,7 +774,8 @@ def main():
         "m_norm_max_dev": float(np.abs(np.linalg.norm(m_out, axis=1) - 1).max()),
     }
     be.close()
-    if not args.no_plain and w["integrator"] != "dp45":  # the plain path has Heun and RK4 only
+    # the plain path has Heun and RK4 and none of the extra-field terms
+    if not args.no_plain and w["integrator"] != "dp45" and w.get("terms") is None:
         # the cuFFT + unfused path (reference per-step kernel structure), same workload;
         # each of its steps ends in blocking copies, so wall clock is its device time
         from fullmag_gb300.plain import PlainBaseline

@@ -338,7 +338,7 @@ class FdmBackend:
         return c.value
 
     KERNEL_KINDS = ("row_pass", "y_forward", "z_convolve", "y_inverse", "yz_convolve", "y_convolve_2d",
-                    "finalize_stats")
+                    "finalize_stats", "extra_field")
 
     def set_kernel_timing(self, enable: bool):
         """Per-launch CUDA-event timing of every kernel (fixed steps then run without graphs)."""

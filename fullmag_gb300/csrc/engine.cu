@@ -224,10 +224,10 @@ struct Engine {
     float *hextra = nullptr;
     ExtraSums *xpart = nullptr;
     float *kmaps[5] = {};  // per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (device, FP32) or NULL
-    // exchange with region ids (api.cpp:405-420): ids and the FP64 stiffness table on the
+    // exchange with region ids (api.cpp:405-420): ids and the stiffness table (FP32) on the
     // device; the whole exchange term then runs in the extra pass
     uint32_t *regions = nullptr;
-    double *lut = nullptr;
+    float *lut = nullptr;
     // Brown thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896): sigma^2 =
     // th_pref / dt with the step's dt (1e-13 s for adaptive integrators); a step counter that
     // advances once per completed step; th_dev[0] for the evaluations inside a step,
@@ -451,7 +451,7 @@ struct Engine {
     // With timing on, fixed steps run eagerly (no graph) and every launch is bracketed
     // by a pair of events on the engine's stream; the elapsed times are summed per
     // kernel kind whenever the stream has been synchronised.
-    enum { KT_ROW, KT_YF, KT_Z, KT_YI, KT_YZ, KT_Y2D, KT_FIN, KT_N };
+    enum { KT_ROW, KT_YF, KT_Z, KT_YI, KT_YZ, KT_Y2D, KT_FIN, KT_EXTRA, KT_N };
     bool ktime = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_ev;
     std::vector<int> kt_kind;
@@ -542,7 +542,10 @@ struct Engine {
             p.h_ex_out = nullptr;
         }
         launches += 1;
-        if (cuda_fail("extra field", launch_extra_field(q, stream))) return false;
+        kt_begin(KT_EXTRA);
+        const cudaError_t rc = launch_extra_field(q, stream);
+        kt_end();
+        if (cuda_fail("extra field", rc)) return false;
         p.hmap = hextra;
         return true;
     }
@@ -1873,12 +1876,9 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     xf.d_bulk = plan->dmi_D_bulk;
     xf.dmi_int = (float)(2.0 * plan->dmi_D_interfacial / mu0ms);
     xf.dmi_bulk = (float)(2.0 * plan->dmi_D_bulk / mu0ms);
-    xf.dinv2dx = 0.5 / dx;
-    xf.dinv2dy = 0.5 / dy;
-    xf.dinv2dz = 0.5 / dz;
-    xf.inv2dx = (float)xf.dinv2dx;
-    xf.inv2dy = (float)xf.dinv2dy;
-    xf.inv2dz = (float)xf.dinv2dz;
+    xf.inv2dx = (float)(0.5 / dx);
+    xf.inv2dy = (float)(0.5 / dy);
+    xf.inv2dz = (float)(0.5 / dz);
     xf.mel_pref = (float)(-1.0 / mu0ms);
     xf.b1 = (float)plan->mel_b1;
     xf.b2 = (float)plan->mel_b2;
@@ -1981,9 +1981,6 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         xf.idx2 = mat.idx2;
         xf.idy2 = mat.idy2;
         xf.idz2 = mat.idz2;
-        xf.didx2 = 1.0 / (dx * dx);
-        xf.didy2 = 1.0 / (dy * dy);
-        xf.didz2 = 1.0 / (dz * dz);
         mat.ex_pref = 0.f;
     }
     // thermal field: sigma^2 = 2 alpha kB T / (gamma (1 + alpha^2) mu0 Ms V dt)
@@ -2106,17 +2103,18 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     if (region_exchange) {
         // the caller's table when it has 256 x 256 entries, else A on the diagonal
         // (api.cpp:405-420)
+        // (api.cpp:405-420), held as FP32 as the reference's field kernel reads it
         constexpr size_t R = FULLMAG_FDM_MAX_EXCHANGE_REGIONS;
-        std::vector<double> table(R * R, 0.0);
+        std::vector<float> table(R * R, 0.f);
         if (plan->exchange_lut && plan->exchange_lut_len == R * R)
-            std::copy(plan->exchange_lut, plan->exchange_lut + R * R, table.begin());
+            for (size_t k = 0; k < R * R; ++k) table[k] = (float)plan->exchange_lut[k];
         else
-            for (size_t r = 0; r < R; ++r) table[r * R + r] = a_ex;
+            for (size_t r = 0; r < R; ++r) table[r * R + r] = (float)a_ex;
         if (cuda_fail("cudaMalloc(region ids)", cudaMalloc((void **)&regions, sizeof(uint32_t) * (size_t)g.n)) ||
-            cuda_fail("cudaMalloc(exchange table)", cudaMalloc((void **)&lut, sizeof(double) * R * R)) ||
+            cuda_fail("cudaMalloc(exchange table)", cudaMalloc((void **)&lut, sizeof(float) * R * R)) ||
             cuda_fail("region ids upload",
                       cudaMemcpy(regions, plan->region_mask, sizeof(uint32_t) * (size_t)g.n, cudaMemcpyHostToDevice)) ||
-            cuda_fail("exchange table upload", cudaMemcpy(lut, table.data(), sizeof(double) * R * R, cudaMemcpyHostToDevice)))
+            cuda_fail("exchange table upload", cudaMemcpy(lut, table.data(), sizeof(float) * R * R, cudaMemcpyHostToDevice)))
             return false;
         xf.region = regions;
         xf.lut = lut;

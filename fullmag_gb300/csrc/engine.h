@@ -154,7 +154,8 @@ size_t y_convolve_2d_smem(const Grid &g, int tx);
 // (extra_field.cu): interfacial and bulk DMI (central differences, Neumann clamp, mask)
 // and the magnetoelastic field of a prescribed strain, plus the applied field map.  The
 // row pass adds `out` as its field map; H = 0 at inactive cells.
-// per-CTA sums of the extra field pass (FP64): Zeeman m.(H_ext + H_map), DMI energy density,
+// per-CTA sums of the extra field pass (each thread accumulates float-float pairs, the CTA
+// adds them in FP64): Zeeman m.(H_ext + H_map), DMI energy density,
 // with per-cell anisotropy maps the uniaxial and cubic energy densities, and with region ids
 // the exchange pair sum sum A_ij |m_j - m_i|^2 / d^2
 struct ExtraSums {
@@ -179,9 +180,8 @@ struct ExtraField {
     float hext[3];
     int has_int, has_bulk, has_mel;
     float dmi_int, dmi_bulk;   // 2 D / (mu0 Ms), A/m per unit gradient
-    double d_int, d_bulk;      // D (J/m^2) for the energy sums
-    float inv2dx, inv2dy, inv2dz;     // 1/(2 d) for the field
-    double dinv2dx, dinv2dy, dinv2dz; // 1/(2 d) for the energy sums
+    float d_int, d_bulk;       // D (J/m^2) for the energy sums
+    float inv2dx, inv2dy, inv2dz;     // 1/(2 d)
     float mel_pref;            // -1 / (mu0 Ms)
     float b1, b2, e11, e22, e33, e23, e13, e12;  // B1, B2 (J/m^3), strain tensor (e_ij, i != j halved Voigt)
     // spin torques T (added to dm/dt by the reference) enter as the field H = a T + b m x T,
@@ -209,10 +209,9 @@ struct ExtraField {
     // with A from the 256 x 256 FP64 table, read as FP32 for the field; the row pass's
     // exchange is off, and this pass writes the H_EX observable (h_ex_out) when asked
     const uint32_t *region;    // region id per cell (< 256) or NULL
-    const double *lut;         // exchange stiffness table, row-major [r_i][r_j] (J/m)
+    const float *lut;          // exchange stiffness table as FP32, row-major [r_i][r_j] (J/m)
     float ex_s;                // 2 / (mu0 Ms)
     float idx2, idy2, idz2;    // 1 / d^2
-    double didx2, didy2, didz2;
     float *h_ex_out;
     // thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896) or NULL
     const ThermalSlot *th;

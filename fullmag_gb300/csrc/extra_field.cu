@@ -7,7 +7,7 @@
 //   active mask                                 native/backends/fdm/src/demag_fp32.cu:319-366
 //   magnetoelastic field (B1, B2, prescribed strain; shear strains halved from Voigt)
 //                                               native/backends/fdm/src/demag_fp32.cu:368-376,582-583
-//   DMI energy (FP64 sums of the FP32 state)    native/backends/fdm/src/reductions_fp64.cu:647-720
+//   DMI energy (sums of the FP32 state)         native/backends/fdm/src/reductions_fp64.cu:647-720
 //   Oersted field of a cylindrical conductor, scaled by I(t)
 //                                               native/backends/fdm/src/context.cu:844-905,
 //                                               demag_fp32.cu:585-616
@@ -25,8 +25,11 @@
 // +2D/(mu0 Ms) curl m; both are kept as they are, so the energy is summed from its own
 // formula, not from m.H.  The row pass adds this pass's output as its field map, so its
 // own Zeeman sum would include these terms: the Zeeman sum m.(H_ext + H_map) is taken
-// here instead, in FP64.
+// here instead.  Every energy term is formed in FP32 and summed in float-float pairs
+// (TwoSum); only the per-CTA reduction runs in FP64, whose throughput is a small fraction
+// of FP32 on this part.
 #include "engine.h"
+#include "fft_smem.cuh"
 
 #include <algorithm>
 
@@ -43,15 +46,21 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     return z ^ (z >> 31);
 }
 
+// b < 2^54 as FP32 from its two 32-bit halves (32-bit conversions and one FMA, which keep
+// the 64-bit conversion off the slow pipe)
+__device__ __forceinline__ float u54_to_float(unsigned long long b) {
+    return fmaf((float)(unsigned)(b >> 32), 4294967296.0f, (float)(unsigned)b);
+}
+
 // u = ((bits >> 11) + 1) / (2^53 + 1) in (0, 1], as FP32
-__device__ __forceinline__ float unit_of(unsigned long long bits) { return (float)((bits >> 11) + 1ull) * 0x1p-53f; }
+__device__ __forceinline__ float unit_of(unsigned long long bits) { return u54_to_float((bits >> 11) + 1ull) * 0x1p-53f; }
 
 // -2 ln u: logf of u itself up to u = 1/2, log1pf(-(1 - u)) above, with 1 - u formed from
 // the exact integer so that u near 1 keeps its relative accuracy
 __device__ __forceinline__ float neg2log_of(unsigned long long bits) {
     const unsigned long long b = (bits >> 11) + 1ull;  // 1 .. 2^53
-    if (b <= (1ull << 52)) return -2.f * logf((float)b * 0x1p-53f);
-    return -2.f * log1pf(-(float)((1ull << 53) + 1ull - b) * 0x1p-53f);
+    if (b <= (1ull << 52)) return -2.f * logf(u54_to_float(b) * 0x1p-53f);
+    return -2.f * log1pf(-u54_to_float((1ull << 53) + 1ull - b) * 0x1p-53f);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -82,11 +91,15 @@ __device__ __forceinline__ ExtraSums block_sum(ExtraSums v) {
     return t;
 }
 
-__global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField p) {
+// three CTAs per SM (80 registers, no spills)
+__global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraField p) {
     const Grid &g = p.g;
     const long long n = g.n;
     const float *m = p.m;
-    double s_zee = 0.0, s_dmi = 0.0, s_uni = 0.0, s_cub = 0.0, s_exch = 0.0;
+    // energy sums: FP32 terms in float-float pairs (TwoSum); FP64 only in the CTA reduction,
+    // since FP64 throughput is a small fraction of FP32 on this part
+    enum { kZee, kDmi, kUni, kCub, kExch };
+    float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float hx = 0.f, hy = 0.f, hz = 0.f;
         float rx = 0.f, ry = 0.f, rz = 0.f;  // region exchange (the H_EX observable)
@@ -112,13 +125,13 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                 }
                 if (p.region) {
                     // sum_q A[r_i][r_q] (m_q - m_i) / d_q^2 in the order x+, x-, y+, y-, z+, z-
-                    const double *row = p.lut + (size_t)p.region[i] * 256;
+                    const float *row = p.lut + (size_t)p.region[i] * 256;
                     const long long nb[6] = {xp, xm, yp, ym, zp, zm};
                     const float w[6] = {p.idx2, p.idx2, p.idy2, p.idy2, p.idz2, p.idz2};
 #pragma unroll
                     for (int q = 0; q < 6; ++q) {
                         const long long j = nb[q];
-                        const float a = (float)row[p.region[j]] * w[q];
+                        const float a = row[p.region[j]] * w[q];
                         rx += a * (m[j] - mx);
                         ry += a * (m[n + j] - my);
                         rz += a * (m[2 * n + j] - mz);
@@ -130,16 +143,15 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                     ay += ry;
                     az += rz;
                     if (p.partials) {
-                        // forward pairs (x+1, y+1, z+1) with an active neighbour, each pair once,
-                        // the table read in FP64 as the reference's energy reduction does
-                        const double dw[3] = {p.didx2, p.didy2, p.didz2};
+                        // forward pairs (x+1, y+1, z+1) with an active neighbour, each pair once
+                        const float fwv[3] = {p.idx2, p.idy2, p.idz2};
                         const long long fw[3] = {xp, yp, zp};
 #pragma unroll
                         for (int a = 0; a < 3; ++a) {
                             const long long j = fw[a];
                             if (j == i) continue;
-                            const double d0 = (double)m[j] - mx, d1 = (double)m[n + j] - my, d2 = (double)m[2 * n + j] - mz;
-                            s_exch += row[p.region[j]] * (d0 * d0 + d1 * d1 + d2 * d2) * dw[a];
+                            const float d0 = m[j] - mx, d1 = m[n + j] - my, d2 = m[2 * n + j] - mz;
+                            ff_add(sh[kExch], sl[kExch], row[p.region[j]] * (d0 * d0 + d1 * d1 + d2 * d2) * fwv[a]);
                         }
                     }
                 }
@@ -161,20 +173,12 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                         ay += p.dmi_bulk * (dmx_dz - dmz_dx);
                         az += p.dmi_bulk * (dmy_dx - dmx_dy);
                     }
-                    if (p.partials) {
-                        // the energy sums take the differences in FP64 of the FP32 state
-                        auto ddif = [&](int c, long long a, long long b) { return (double)m[c * n + a] - (double)m[c * n + b]; };
-                        const double i2x = p.dinv2dx, i2y = p.dinv2dy, i2z = p.dinv2dz;
-                        const double Mx = mx, My = my, Mz = mz;
+                    if (p.partials) {  // energy densities from the same central differences
                         if (p.has_int)
-                            s_dmi += p.d_int * (Mz * (ddif(0, xp, xm) * i2x + ddif(1, yp, ym) * i2y) - Mx * ddif(2, xp, xm) * i2x -
-                                                My * ddif(2, yp, ym) * i2y);
-                        if (p.has_bulk) {
-                            const double cx = ddif(2, yp, ym) * i2y - ddif(1, zp, zm) * i2z;
-                            const double cy = ddif(0, zp, zm) * i2z - ddif(2, xp, xm) * i2x;
-                            const double cz = ddif(1, xp, xm) * i2x - ddif(0, yp, ym) * i2y;
-                            s_dmi += p.d_bulk * (Mx * cx + My * cy + Mz * cz);
-                        }
+                            ff_add(sh[kDmi], sl[kDmi], p.d_int * (mz * (dmx_dx + dmy_dy) - mx * dmz_dx - my * dmz_dy));
+                        if (p.has_bulk)
+                            ff_add(sh[kDmi], sl[kDmi], p.d_bulk * (mx * (dmz_dy - dmy_dz) + my * (dmx_dz - dmz_dx) +
+                                                                   mz * (dmy_dx - dmx_dy)));
                     }
                 }
             }
@@ -194,8 +198,8 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                     ay += cf * p.u[1];
                     az += cf * p.u[2];
                     if (p.partials) {
-                        const double s2 = (double)mu * (double)mu;
-                        s_uni += (double)k1 * s2 + (double)k2 * s2 * s2;
+                        const float s2 = mu * mu;
+                        ff_add(sh[kUni], sl[kUni], k1 * s2 + k2 * s2 * s2);
                     }
                 }
                 if (p.has_cub) {
@@ -213,11 +217,7 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                     ax += g1 * p.c1[0] + g2 * p.c2[0] + g3 * p.c3[0];
                     ay += g1 * p.c1[1] + g2 * p.c2[1] + g3 * p.c3[1];
                     az += g1 * p.c1[2] + g2 * p.c2[2] + g3 * p.c3[2];
-                    if (p.partials) {
-                        const double d1 = (double)a1 * a1, d2 = (double)a2 * a2, d3 = (double)a3 * a3;
-                        const double ds = d1 * d2 + d2 * d3 + d1 * d3;
-                        s_cub += (double)k1 * ds + (double)k2 * d1 * d2 * d3 + (double)k3 * ds * ds;
-                    }
+                    if (p.partials) ff_add(sh[kCub], sl[kCub], k1 * sig + k2 * s1 * s2 * s3 + k3 * sig * sig);
                 }
             }
             if (p.torques && (p.has_zl || p.has_slon || p.has_sot)) {
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
             hx = ax;
             hy = ay;
             hz = az;
-            double zx = 0.0, zy = 0.0, zz = 0.0;  // applied field of the Zeeman sum
+            float zx = 0.f, zy = 0.f, zz = 0.f;  // applied field of the Zeeman sum
             if (p.has_ext) {
                 zx = p.hext[0];
                 zy = p.hext[1];
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
                 zy += uy;
                 zz += uz;
             }
-            if (p.partials) s_zee += (double)mx * zx + (double)my * zy + (double)mz * zz;
+            if (p.partials) ff_add(sh[kZee], sl[kZee], mx * zx + my * zy + mz * zz);
         }
         p.out[i] = hx;
         p.out[n + i] = hy;
@@ -325,7 +325,9 @@ __global__ void __launch_bounds__(kThreads) extra_field_kernel(const ExtraField 
         }
     }
     if (p.partials) {
-        const ExtraSums t = block_sum(ExtraSums{s_zee, s_dmi, s_uni, s_cub, s_exch});
+        const ExtraSums t = block_sum(ExtraSums{(double)sh[kZee] + (double)sl[kZee], (double)sh[kDmi] + (double)sl[kDmi],
+                                                (double)sh[kUni] + (double)sl[kUni], (double)sh[kCub] + (double)sl[kCub],
+                                                (double)sh[kExch] + (double)sl[kExch]});
         if (threadIdx.x == 0) p.partials[blockIdx.x] = t;
     }
 }
@@ -352,7 +354,8 @@ __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSum
 
 }  // namespace
 
-int extra_field_blocks(const Grid &g) { return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, 152 * 8); }
+// four full waves of three CTAs on each of the 152 SMs, threads striding over the cells
+int extra_field_blocks(const Grid &g) { return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, 152 * 3 * 4); }
 
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {
     extra_field_kernel<<<extra_field_blocks(p.g), kThreads, 0, s>>>(p);

@@ -381,7 +381,8 @@ int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px,
  * kernel launch is bracketed by CUDA events on the handle's stream.  Enabling or
  * disabling resets the totals.  kernel_times fills n_kinds entries in the order
  * row pass, y forward, z convolve, y inverse, fused y+z, thin-film y, statistics
- * finalize: total milliseconds and launch counts since timing was enabled. */
+ * finalize, extra-field pass: total milliseconds and launch counts since timing was
+ * enabled. */
 int fullmag_fdm_backend_set_kernel_timing(fullmag_fdm_backend *handle, int enable);
 int fullmag_fdm_backend_kernel_times(fullmag_fdm_backend *handle, double *total_ms, uint64_t *counts, uint32_t n_kinds);
 
