@@ -99,7 +99,9 @@ def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
 # the timed steps (profiles/launches_volume_256x256x64_rk4.md)
 NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 457.4e6, ("volume_256x256x64_rk4", "y_inverse"): 274.0e6,
-               ("volume_256x256x64_rk4", "y_forward"): 242.6e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6}
+               ("volume_256x256x64_rk4", "y_forward"): 242.6e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6,
+               # profiles/ncu_extra_field_volume_256x256x64_rk4_allterms.md (stage launch)
+               ("volume_256x256x64_rk4_allterms", "extra_field"): 189.1e6}
 
 
 WORKLOADS = {
@@ -551,7 +553,7 @@ def cpu_baseline(w, threads):
                       f"after 1 warm-up step), wall clock"}
 
 
-def extra_roofline(w, n, ktimes, peak):
+def extra_roofline(w, n, ktimes, peak, workload):
     """HBM roofline of the extra-field pass (None when the workload has no extra terms)."""
     bpc = extra_bytes_per_cell(w)
     ms, cnt = ktimes.get("extra_field", (0.0, 0))
@@ -560,7 +562,8 @@ def extra_roofline(w, n, ktimes, peak):
     avg_s = ms / cnt * 1e-3
     ach = bpc * n / avg_s / 1e9
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if peak else None,
-            "traffic": None, "kernel": "extra_field", "bytes_per_launch": bpc * n, "avg_launch_ms": avg_s * 1e3,
+            "traffic": NCU_TRAFFIC.get((workload, "extra_field")), "kernel": "extra_field",
+            "bytes_per_launch": bpc * n, "avg_launch_ms": avg_s * 1e3,
             "launches_timed": cnt, "note": f"{bpc} B/cell algorithmic; CUDA events per launch"}
 
 
@@ -766,7 +769,7 @@ def main():
                           "frac": achieved / peak if peak else None,
                           "note": f"whole step, compulsory-traffic model v1 {bpc:.1f} B/cell-step"},
         "kernel_times_ms_per_launch": {k: (v[0] / v[1] if v[1] else None) for k, v in ktimes.items()},
-        "roofline_extra": extra_roofline(w, n, ktimes, peak),
+        "roofline_extra": extra_roofline(w, n, ktimes, peak, args.workload),
         "e2e": {"value": e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
