@@ -54,3 +54,28 @@ def test_trajectory(gpu_lib, oracle, integrator):
     assert np.abs(gpu.copy_field(_abi.OBSERVABLE_M) - orc.get_m()).max() < 3e-5
     assert abs(sg["max_rhs_amplitude"] - so["max_rhs"]) <= 1e-4 * so["max_rhs"]
     assert abs(sg["total_energy_joules"] - so["e_total"]) <= 1e-4 * abs(so["e_total"])
+
+
+@pytest.mark.parametrize("shape", [(7, 5, 3), (9, 1, 1), (1, 1, 1), (1, 7, 1), (5, 1, 4), (3, 4, 2)])
+def test_edge_shapes(gpu_lib, oracle, shape):
+    # extents of 1 clamp every neighbour of DMI and region exchange to the cell itself
+    nx, ny, nz = shape
+    n = nx * ny * nz
+    terms = _all_terms(nx, ny, nz, 7)
+    terms["region_mask"] = (np.arange(n) % 3).astype(np.uint32)
+    lut = terms["exchange_lut"]
+    lut[0, 0], lut[0, 1], lut[1, 0], lut[0, 2], lut[2, 0] = 1.1e-11, 0.2e-11, 0.2e-11, 0.6e-11, 0.6e-11
+    kw = problem(nx, ny, nz, seed=123, alpha=0.1, d=(3e-9, 2e-9, 2.5e-9), **terms)
+    mask = np.ones(n, dtype=np.uint8)
+    if n > 2:
+        mask[n // 2] = 0
+    gpu, orc = make_pair(oracle, kw, mask=mask)
+    ref = orc.fields(kw["m0"] * mask[:, None])
+    assert rel_l2(gpu.copy_field(_abi.OBSERVABLE_H_EFF), ref["h_eff"]) < 1e-5
+    h_ex = gpu.copy_field(_abi.OBSERVABLE_H_EX)
+    assert np.abs(h_ex - ref["h_ex"]).max() <= 1e-5 * max(np.abs(ref["h_ex"]).max(), 1.0)
+    for _ in range(5):
+        sg = gpu.step(4e-14)
+        so = orc.step(4e-14)
+    assert np.abs(gpu.copy_field(_abi.OBSERVABLE_M) - orc.get_m()).max() < 2e-5
+    assert abs(sg["total_energy_joules"] - so["e_total"]) <= 1e-4 * abs(so["e_total"]) + 1e-30
