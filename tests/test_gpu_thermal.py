@@ -82,3 +82,30 @@ def test_step_many_advances_the_counter(gpu_lib, oracle):
     for _ in range(6):
         orc.step(5e-14)
     assert np.abs(gpu.copy_field(_abi.OBSERVABLE_M) - orc.get_m()).max() < 2e-5
+
+
+def test_batch_matches_single_runs(gpu_lib):
+    # problems with extra-field terms take the batch driver's per-problem path; the thermal
+    # counter, the amplitude's dt (the last step is cut to t_end) and the DP45 retries must
+    # come out as in single-problem stepping
+    from fullmag_gb300 import FdmBatch
+    reg = (np.arange(20 * 10 * 2) % 2).astype(np.uint32)
+    ps = [problem(20, 10, 2, seed=116, alpha=0.1, temperature=30.0, region_mask=reg),
+          problem(16, 8, 1, seed=117, alpha=0.1, temperature=10.0, adaptive_max_error=1e-4)]
+    ps[0]["integrator"] = _abi.INTEGRATOR_RK4
+    ps[1]["integrator"] = _abi.INTEGRATOR_DP45
+    t_end, dt0 = 6.3e-13, 5e-14
+    batch = FdmBatch(ps)
+    steps, _ = batch.step_until(t_end, dt0)
+    for i, kw in enumerate(ps):
+        be = FdmBackend(**kw)
+        t, dt, n = 0.0, dt0, 0
+        while t < t_end * (1 - 1e-12):
+            st = be.step(min(dt, t_end - t))
+            t, n = st["time_seconds"], n + 1
+            if kw["integrator"] == _abi.INTEGRATOR_DP45:
+                dt = st["suggested_next_dt"]
+        assert steps[i] == n
+        assert np.abs(batch.copy_field(i) - be.copy_field(_abi.OBSERVABLE_M)).max() < 1e-6
+        be.close()
+    batch.close()
