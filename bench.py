@@ -102,6 +102,10 @@ NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 457.4e6, ("volume_256x25
                ("volume_256x256x64_rk4", "y_forward"): 242.6e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6,
                # profiles/ncu_extra_field_volume_256x256x64_rk4_allterms.md (stage launch)
                ("volume_256x256x64_rk4_allterms", "extra_field"): 189.1e6}
+# the column passes of the all-terms volume are the same launches on the same grid as the
+# plain volume's (the extra terms enter only through the row pass's field map)
+for _k in ("z_convolve", "y_forward", "y_inverse"):
+    NCU_TRAFFIC[("volume_256x256x64_rk4_allterms", _k)] = NCU_TRAFFIC[("volume_256x256x64_rk4", _k)]
 
 
 WORKLOADS = {
