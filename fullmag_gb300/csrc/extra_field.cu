@@ -92,6 +92,9 @@ __device__ __forceinline__ ExtraSums block_sum(ExtraSums v) {
 }
 
 // three CTAs per SM (80 registers, no spills)
+// kNb: neighbour stencils (DMI, region exchange, Zhang-Li) compiled in; kTh: thermal field.
+// The instances without them keep fewer registers for problems that only have local terms.
+template <bool kNb, bool kTh>
 __global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraField p) {
     const Grid &g = p.g;
     const long long n = g.n;
@@ -106,7 +109,7 @@ __global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraFie
         if (p.mask == nullptr || p.mask[i] != 0) {
             const float mx = m[i], my = m[n + i], mz = m[2 * n + i];
             float ax = 0.f, ay = 0.f, az = 0.f;  // DMI + magnetoelastic
-            if (p.has_int || p.has_bulk || p.region) {
+            if (kNb && (p.has_int || p.has_bulk || p.region)) {
                 // neighbours with the Neumann clamp: a missing or inactive neighbour is the cell itself
                 const int x = (int)(i % g.nx);
                 const long long r = i / g.nx;
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraFie
             }
             if (p.torques && (p.has_zl || p.has_slon || p.has_sot)) {
                 float tx = 0.f, ty = 0.f, tz = 0.f;
-                if (p.has_zl) {
+                if (kNb && p.has_zl) {
                     // D = (u.grad) m by upwind differences: the upwind neighbour when it
                     // exists, read without the mask (native/backends/fdm/src/llg_fp32.cu:65-140)
                     const long long r = i / g.nx;
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraFie
                 ay += I * p.h_oe[n + i];
                 az += I * p.h_oe[2 * n + i];
             }
-            if (p.th) {  // in no energy sum, as in the reference
+            if (kTh && p.th) {  // in no energy sum, as in the reference
                 const float sg = p.th->sigma;
                 if (sg > 0.f) {
                     constexpr unsigned long long kCell = 0x517CC1B727220A95ull, kStream = 0x6C62272E07BB0142ull;
@@ -358,7 +361,12 @@ __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSum
 int extra_field_blocks(const Grid &g) { return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, 152 * 3 * 4); }
 
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {
-    extra_field_kernel<<<extra_field_blocks(p.g), kThreads, 0, s>>>(p);
+    const bool nb = p.has_int || p.has_bulk || p.region || (p.torques && p.has_zl), th = p.th != nullptr;
+    const dim3 grid(extra_field_blocks(p.g));
+    if (nb && th) extra_field_kernel<true, true><<<grid, kThreads, 0, s>>>(p);
+    else if (nb) extra_field_kernel<true, false><<<grid, kThreads, 0, s>>>(p);
+    else if (th) extra_field_kernel<false, true><<<grid, kThreads, 0, s>>>(p);
+    else extra_field_kernel<false, false><<<grid, kThreads, 0, s>>>(p);
     return cudaGetLastError();
 }
 
