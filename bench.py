@@ -437,11 +437,12 @@ def extra_terms(nx, ny, nz, d, seed):
 
 def extra_bytes_per_cell(w):
     """Algorithmic bytes per cell of one extra-field launch: m read and H_extra written
-    (12 + 12), plus the region id (4), the Ku1 map (4) and the Oersted field (12) when
-    present; the neighbour reads of DMI and exchange come from the same m rows."""
+    (12 + 12), plus the region id (1, one byte per cell on the device), the Ku1 map (4)
+    and the Oersted field (12) when present; the neighbour reads of DMI and exchange come
+    from the same m rows."""
     if w.get("terms") != "all":
         return None
-    return 12 + 12 + 4 + 4 + 12
+    return 12 + 12 + 1 + 4 + 12
 
 
 def gpu_plan(w):

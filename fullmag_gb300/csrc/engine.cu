@@ -226,7 +226,7 @@ struct Engine {
     float *kmaps[5] = {};  // per-cell Ku1 Ku2 Kc1 Kc2 Kc3 (device, FP32) or NULL
     // exchange with region ids (api.cpp:405-420): ids and the stiffness table (FP32) on the
     // device; the whole exchange term then runs in the extra pass
-    uint32_t *regions = nullptr;
+    uint8_t *regions = nullptr;  // ids below 256, one byte per cell
     float *lut = nullptr;
     // Brown thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896): sigma^2 =
     // th_pref / dt with the step's dt (1e-13 s for adaptive integrators); a step counter that
@@ -2110,10 +2110,12 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
             for (size_t k = 0; k < R * R; ++k) table[k] = (float)plan->exchange_lut[k];
         else
             for (size_t r = 0; r < R; ++r) table[r * R + r] = (float)a_ex;
-        if (cuda_fail("cudaMalloc(region ids)", cudaMalloc((void **)&regions, sizeof(uint32_t) * (size_t)g.n)) ||
+        std::vector<uint8_t> ids((size_t)g.n);  // validated below 256 at the top of setup
+        for (long long i = 0; i < g.n; ++i) ids[i] = (uint8_t)plan->region_mask[i];
+        if (cuda_fail("cudaMalloc(region ids)", cudaMalloc((void **)&regions, (size_t)g.n)) ||
             cuda_fail("cudaMalloc(exchange table)", cudaMalloc((void **)&lut, sizeof(float) * R * R)) ||
             cuda_fail("region ids upload",
-                      cudaMemcpy(regions, plan->region_mask, sizeof(uint32_t) * (size_t)g.n, cudaMemcpyHostToDevice)) ||
+                      cudaMemcpy(regions, ids.data(), (size_t)g.n, cudaMemcpyHostToDevice)) ||
             cuda_fail("exchange table upload", cudaMemcpy(lut, table.data(), sizeof(float) * R * R, cudaMemcpyHostToDevice)))
             return false;
         xf.region = regions;

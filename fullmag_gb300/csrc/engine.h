@@ -208,7 +208,7 @@ struct ExtraField {
     // exchange with region ids (exchange_fp32.cu:48-104): 2/(mu0 Ms) sum_q A[r_i][r_q] (m_q - m_i)/d_q^2
     // with A from the 256 x 256 FP64 table, read as FP32 for the field; the row pass's
     // exchange is off, and this pass writes the H_EX observable (h_ex_out) when asked
-    const uint32_t *region;    // region id per cell (< 256) or NULL
+    const uint8_t *region;     // region id per cell (validated < 256, one byte each) or NULL
     const float *lut;          // exchange stiffness table as FP32, row-major [r_i][r_j] (J/m)
     float ex_s;                // 2 / (mu0 Ms)
     float idx2, idy2, idz2;    // 1 / d^2
