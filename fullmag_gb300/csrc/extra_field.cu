@@ -92,10 +92,10 @@ __device__ __forceinline__ ExtraSums block_sum(ExtraSums v) {
 }
 
 // three CTAs per SM (80 registers, no spills)
-// kNb: neighbour stencils (DMI, region exchange, Zhang-Li) compiled in; kTh: thermal field.
-// The instances without them keep fewer registers for problems that only have local terms.
-template <bool kNb, bool kTh>
-__global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraField p) {
+// kNb: neighbour stencils (DMI, Zhang-Li) compiled in; kRg: exchange with region ids;
+// kTh: thermal field.  The instances without them keep fewer registers.
+template <bool kNb, bool kRg, bool kTh>
+__global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(const ExtraField p) {
     const Grid &g = p.g;
     const long long n = g.n;
     const float *m = p.m;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraFie
         if (p.mask == nullptr || p.mask[i] != 0) {
             const float mx = m[i], my = m[n + i], mz = m[2 * n + i];
             float ax = 0.f, ay = 0.f, az = 0.f;  // DMI + magnetoelastic
-            if (kNb && (p.has_int || p.has_bulk || p.region)) {
+            if ((kNb || kRg) && (p.has_int || p.has_bulk || (kRg && p.region))) {
                 // neighbours with the Neumann clamp: a missing or inactive neighbour is the cell itself
                 const int x = (int)(i % g.nx);
                 const long long r = i / g.nx;
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kThreads, 3) extra_field_kernel(const ExtraFie
                     if (!p.mask[zm]) zm = i;
                     if (!p.mask[zp]) zp = i;
                 }
-                if (p.region) {
+                if (kRg && p.region) {
                     // sum_q A[r_i][r_q] (m_q - m_i) / d_q^2 in the order x+, x-, y+, y-, z+, z-
                     const float *row = p.lut + (size_t)p.region[i] * 256;
                     const long long nb[6] = {xp, xm, yp, ym, zp, zm};
@@ -361,12 +361,19 @@ __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSum
 int extra_field_blocks(const Grid &g) { return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, 152 * 3 * 4); }
 
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {
-    const bool nb = p.has_int || p.has_bulk || p.region || (p.torques && p.has_zl), th = p.th != nullptr;
+    const bool rg = p.region != nullptr, th = p.th != nullptr;
+    const bool nb = p.has_int || p.has_bulk || (p.torques && p.has_zl);
     const dim3 grid(extra_field_blocks(p.g));
-    if (nb && th) extra_field_kernel<true, true><<<grid, kThreads, 0, s>>>(p);
-    else if (nb) extra_field_kernel<true, false><<<grid, kThreads, 0, s>>>(p);
-    else if (th) extra_field_kernel<false, true><<<grid, kThreads, 0, s>>>(p);
-    else extra_field_kernel<false, false><<<grid, kThreads, 0, s>>>(p);
+    if (rg) {  // region exchange: the full instance (neighbours, with or without thermal)
+        if (th) extra_field_kernel<true, true, true><<<grid, kThreads, 0, s>>>(p);
+        else extra_field_kernel<true, true, false><<<grid, kThreads, 0, s>>>(p);
+    } else if (nb) {
+        if (th) extra_field_kernel<true, false, true><<<grid, kThreads, 0, s>>>(p);
+        else extra_field_kernel<true, false, false><<<grid, kThreads, 0, s>>>(p);
+    } else {
+        if (th) extra_field_kernel<false, false, true><<<grid, kThreads, 0, s>>>(p);
+        else extra_field_kernel<false, false, false><<<grid, kThreads, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
