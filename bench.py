@@ -97,10 +97,10 @@ def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
-# the timed steps (profiles/launches_volume_256x256x64_rk4.md)
+# the timed steps of each workload
 NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 457.4e6, ("volume_256x256x64_rk4", "y_inverse"): 274.0e6,
                ("volume_256x256x64_rk4", "y_forward"): 242.6e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6,
-               # profiles/ncu_extra_field_volume_256x256x64_rk4_allterms.md (stage launch)
+               # the extra-field pass's stage launch
                ("volume_256x256x64_rk4_allterms", "extra_field"): 189.1e6}
 # the column passes of the all-terms volume are the same launches on the same grid as the
 # plain volume's (the extra terms enter only through the row pass's field map)
@@ -227,7 +227,7 @@ def run_sweep(args, rank=0, world=1, dist=None):
     print(json.dumps(out), flush=True)
 
 
-def run_sweep_reference(args):
+def run_sweep_reference(args, world=1):
     """The reference's way to run a sweep: one problem after another on the CPU engine
     (the FP64 oracle, all host threads), each to t_end with its own DP45 controller
     (dt0 = 1e-13 s, max error 1e-5).  Bounded: evenly strided problems until about 150 s
@@ -262,7 +262,7 @@ def run_sweep_reference(args):
             break
     v = solved / spent if spent > 0 else 0.0
     print(json.dumps({"metric": "problems/s (batched sweep, DP45 to %.2g s)" % t_end, "value": v,
-                      "unit": "problems/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+                      "unit": "problems/s", "n_gpus": world, "higher_is_better": True, "dtype": "f64",
                       "data": "synthetic (seeded)", "impl": "reference",
                       "config": {"workload": SWEEP_WORKLOAD, "problems_solved": solved, "stride": stride,
                                  "threads": threads},
@@ -530,20 +530,49 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(w, threads):
-    """FP64 oracle (C restatement of the reference CPU engine) on a bounded sample:
-    one step of the same physics on a grid with 1/8 of the cells (halved per axis
-    for 3-D), after one warm-up step."""
+def oracle_sample_grid(O, w, steps, budget):
+    """Largest sample of the workload's grid whose probe step says that `steps` steps
+    fit `budget` seconds of CPU time: the full grid first, then halved per axis (cell-
+    steps/s is per cell, so the sample size sets only the run time).  Returns the
+    oracle problem (one probe step taken) and its grid."""
+    sx, sy, sz = w["nx"], w["ny"], w["nz"]
+    while True:
+        pr = oracle_problem(O, w, sx, sy, sz)
+        t0 = time.perf_counter()
+        pr.step(w["dt"])  # probe step, not counted
+        t_probe = time.perf_counter() - t0
+        if steps * t_probe <= budget or sx * sy * sz <= 4096:
+            return pr, (sx, sy, sz)
+        pr.close()
+        sx, sy, sz = max(sx // 2, 8), max(sy // 2, 8), max(sz // 2, 1)
+
+
+def cpu_baseline(w, threads, h_eff_gpu=None):
+    """FP64 oracle (C restatement of the reference CPU engine) on a bounded sample of
+    the workload: the full grid when 3 steps fit about 30 s of CPU time, else the grid
+    halved per axis until they do; up to 3 timed steps (10 s at most) after the probe
+    step.  With the GPU's H_eff of the initial state (h_eff_gpu) and a full-grid sample
+    it also returns the relative L2 error of that H_eff against the oracle's FP64 one;
+    that comparison runs before the timed steps and is not timed."""
     from oracle import oracle as O
     O.build()
     O.set_threads(threads)
-    nx, ny, nz = w["nx"], w["ny"], w["nz"]
-    if nz > 1:
-        sx, sy, sz = max(nx // 2, 1), max(ny // 2, 1), max(nz // 2, 1)
+    heff_err = None
+    full = (w["nx"], w["ny"], w["nz"])
+    if h_eff_gpu is not None:
+        pr = oracle_problem(O, w, *full)
+        h_ref = pr.fields()["h_eff"]
+        heff_err = float(np.linalg.norm(h_eff_gpu.reshape(-1) - h_ref) / np.linalg.norm(h_ref))
+        del h_ref
+        t0 = time.perf_counter()
+        pr.step(w["dt"])  # probe step
+        if 3 * (time.perf_counter() - t0) > 30.0:
+            pr.close()
+            pr, grid = oracle_sample_grid(O, w, 3, 30.0)
+        else:
+            grid = full
     else:
-        sx, sy, sz = nx, ny, nz
-    pr = oracle_problem(O, w, sx, sy, sz)
-    pr.step(w["dt"])
+        pr, grid = oracle_sample_grid(O, w, 3, 30.0)
     t0 = time.perf_counter()
     steps = 0
     while True:
@@ -553,9 +582,12 @@ def cpu_baseline(w, threads):
             break
     el = time.perf_counter() - t0
     pr.close()
-    return {"value": sx * sy * sz * steps / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} {w['integrator'].upper()} step(s) of {sx}x{sy}x{sz} (same physics, FP64, "
-                      f"after 1 warm-up step), wall clock"}
+    sx, sy, sz = grid
+    out = {"value": sx * sy * sz * steps / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+           "sample": f"{steps} {w['integrator'].upper()} step(s) of {sx}x{sy}x{sz} (same physics, FP64, "
+                     f"after 1 untimed step), wall clock",
+           "same_grid": tuple(grid) == full}
+    return out, heff_err
 
 
 def extra_roofline(w, n, ktimes, peak, workload):
@@ -579,20 +611,9 @@ def run_reference(args, w, name, rank, world):
     from oracle import oracle as O
     O.build()
     O.set_threads(threads)
-    nx, ny, nz = w["nx"], w["ny"], w["nz"]
-    sx, sy, sz = (max(nx // 2, 1), max(ny // 2, 1), max(nz // 2, 1)) if nz > 1 else (nx, ny, nz)
-    # bounded sample: halve the grid per axis until warm-up + timed steps fit ~150 s of
-    # CPU time (cell-steps/s is per cell, so the sample size only sets the run time)
-    budget = 150.0
-    while True:
-        pr = oracle_problem(O, w, sx, sy, sz)
-        t0 = time.perf_counter()
-        pr.step(w["dt"])  # probe step, not counted
-        t_probe = time.perf_counter() - t0
-        if (args.steps + args.warmup) * t_probe <= budget or sx * sy * sz <= 4096:
-            break
-        pr.close()
-        sx, sy, sz = max(sx // 2, 8), max(sy // 2, 8), max(sz // 2, 1)
+    # bounded sample: the full grid when warm-up + timed steps fit ~150 s of CPU time,
+    # else the grid halved per axis until they do
+    pr, (sx, sy, sz) = oracle_sample_grid(O, w, args.steps + args.warmup, 150.0)
     for _ in range(args.warmup):
         pr.step(w["dt"])
     t0 = time.perf_counter()
@@ -605,11 +626,25 @@ def run_reference(args, w, name, rank, world):
            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
            "impl": "reference",
-           "config": {"workload": name, "sample_grid": [sx, sy, sz], "threads": threads},
+           "config": {"workload": name, "grid": [w["nx"], w["ny"], w["nz"]], "sample_grid": [sx, sy, sz],
+                      "same_grid": (sx, sy, sz) == (w["nx"], w["ny"], w["nz"]), "threads": threads},
            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                             "sample": f"{args.steps} step(s) of {sx}x{sy}x{sz} per timed step set"},
            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def relaunch_ranks(n):
+    """`bench.py --gpus N` started as one process: run the same command as N ranks (one
+    per GPU, LOCAL_RANK selects the device) under torch.distributed.run on 127.0.0.1 and
+    return its exit status.  Every rank prints nothing but rank 0's single line."""
+    import socket
+    with socket.socket() as sock:
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.run(cmd).returncode
 
 
 def main():
@@ -632,13 +667,15 @@ def main():
         args.steps = 5 if args.workload == ADJOINT_WORKLOAD else 300
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_ranks(args.gpus))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload == SWEEP_WORKLOAD:
         if args.impl == "reference":
             if rank == 0:
-                run_sweep_reference(args)
+                run_sweep_reference(args, world)
             return
         dist = None
         if world > 1:
@@ -681,6 +718,10 @@ def main():
     dt = w["dt"]
 
     be = FdmBackend(**kw, integrator=integ)
+    # H_eff of the initial state (create ends with the observables refreshed), kept for the
+    # comparison with the FP64 oracle in the CPU-baseline leg, after the timed region
+    want_heff = rank == 0 and not args.no_cpu_baseline and world == 1 and not args.profile
+    h_eff0 = be.copy_field(_abi.OBSERVABLE_H_EFF) if want_heff else None
     stream = torch.cuda.ExternalStream(be.stream())
     # the sampler starts before the warm-up so that nvidia-smi's own start-up does not
     # overlap the timed steps; its samples cover the warm-up and the timed region
@@ -803,7 +844,9 @@ def main():
         out["fused_over_plain"] = value / out["plain"]["value"]
         del m_plain
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
+        out["cpu_baseline"], err = cpu_baseline(w, os.cpu_count() or 1, h_eff0)
+        out["heff_rel_l2_vs_fp64"] = {"value": err, "step": 0, "grid": [w["nx"], w["ny"], w["nz"]],
+                                      "bound": 1e-5, "oracle": "FP64 C restatement of the reference CPU engine"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:

@@ -357,7 +357,9 @@ __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSum
 
 }  // namespace
 
-// four full waves of three CTAs on each of the 152 SMs, threads striding over the cells
+// 1824 CTAs, threads striding over the cells: on the 152 SMs of a GB300 that is three full
+// waves of the four-CTA-per-SM instances (no region exchange) and four of the three-CTA
+// region instances
 int extra_field_blocks(const Grid &g) { return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, 152 * 3 * 4); }
 
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {

@@ -12,7 +12,11 @@
 //  * at most kNoAllocMaxCells cells (the scratch is 3 * kNoAllocMaxCells doubles,
 //    6 MiB); larger grids are rejected and must use the regular upload;
 //  * the scratch is resolved with cudaGetSymbolAddress once per device, on the first
-//    call for a handle on that device, with that device made current for the lookup;
+//    call for a handle on that device, with that device made current for the lookup.
+//    With lazy module loading (the CUDA 12+ default) that first call also loads this
+//    file's module and its 6 MiB array, which can synchronise the device once; later
+//    calls do not.  Make the first call before any stream capture and before the
+//    latency-critical part of a run;
 //  * nothing in the scratch has to start at zero: the kernel reads only the 3n doubles
 //    the same call copied in;
 //  * all handles on one device share the scratch, so calls that overlap in time (for
@@ -32,6 +36,9 @@ namespace {
 static __device__ __align__(256) double g_upload_scratch[3 * kNoAllocMaxCells];
 
 constexpr int kMaxDevices = 64;
+// Resolved addresses, one per device, kept for the life of the process.  They belong to
+// the device's primary context: a caller that destroys that context (cudaDeviceReset)
+// invalidates them, and must not use this upload afterwards in the same process.
 double *g_scratch_addr[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 

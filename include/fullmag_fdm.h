@@ -433,8 +433,11 @@ void fullmag_fdm_batch_destroy(fullmag_fdm_batch *batch);
  * other streams work (cudaMalloc/cudaFree can synchronise the whole device) or a
  * process whose device memory is reserved up front.  Limits: grids of at most
  * 262,144 cells (larger ones get FULLMAG_FDM_ERR_INVALID); the first call for a
- * device resolves the array's address with cudaGetSymbolAddress, so make one call
- * before any stream capture; all handles on a device share the array, so calls that
+ * device resolves the array's address with cudaGetSymbolAddress and, under lazy
+ * module loading, loads the array itself, which may synchronise the device once, so
+ * make one call before any stream capture and before the latency-critical part of a
+ * run; the address stays valid until the device's primary context is destroyed
+ * (cudaDeviceReset); all handles on a device share the array, so calls that
  * overlap in time (several host threads) race and must be serialised by the caller. */
 int fullmag_fdm_backend_upload_magnetization_f64_noalloc(fullmag_fdm_backend *handle, const double *m_xyz,
                                                          uint64_t len);

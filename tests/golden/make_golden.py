@@ -11,7 +11,9 @@ import re
 import sys
 from pathlib import Path
 
-root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py <path of a mzrptu/fullmag checkout>")
+root = Path(sys.argv[1])
 newell = (root / "crates/fullmag-fdm-demag/src/newell.rs").read_text()
 
 

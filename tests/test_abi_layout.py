@@ -100,3 +100,28 @@ def test_plan_builder_keeps_every_caller_value():
     assert list(p.oersted_axis) == [1.0, 0.0, 0.0]
     assert p.region_mask_len == 4 and [p.region_mask[i] for i in range(4)] == [0, 1, 1, 2]
     assert p.exchange_lut_len == 256 * 256 and p.exchange_lut[257] == lut[257]
+
+
+def test_header_matches_reference_layout(tmp_path):
+    """include/fullmag_fdm.h against the reference header's own layout, recorded by
+    tests/golden/make_abi_golden.py from native/include/fullmag_fdm.h: every struct of
+    the reference has the same size, the same fields in the same order at the same
+    offsets; every enum constant has the same value; every reference function is
+    declared."""
+    import json
+    import sys
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from make_abi_golden import parse_header, probe
+    gold = json.loads((ROOT / "tests" / "golden" / "abi_layout.json").read_text())
+    structs, constants, functions = parse_header(HEADER.read_text())
+    for s, fields in gold["field_order"].items():
+        assert s in structs, s
+        # the reference's fields, in its order, lead each struct (no field is inserted)
+        assert structs[s][:len(fields)] == fields, s
+    mine = probe(HEADER, gold["field_order"], list(gold["constants"]), tmp_path)
+    for s, d in gold["structs"].items():
+        assert mine["structs"][s]["size"] == d["size"], s
+        assert mine["structs"][s]["fields"] == d["fields"], s
+    assert mine["constants"] == gold["constants"]
+    assert set(gold["functions"]) <= set(functions)
+    assert len(gold["functions"]) == 22

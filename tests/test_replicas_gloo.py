@@ -91,3 +91,19 @@ def test_reference_arm_runs_on_rank0_only():
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_gpus_flag_launches_ranks_itself():
+    """`bench.py --gpus 2` started as one plain process launches two ranks itself
+    (torch.distributed.run on 127.0.0.1); with --impl reference rank 0 alone works and
+    prints one line for the whole job."""
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl", "reference",
+                        "--workload", "box_64x32x4_heun", "--steps", "1", "--warmup", "0"],
+                       capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.strip().splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2
+    assert line["config"]["same_grid"] is True

@@ -47,6 +47,39 @@ def test_noalloc_upload_matches_regular_upload(gpu_lib):
         assert np.array_equal(regular.magnetization(), noalloc.magnetization())
 
 
+def test_noalloc_upload_allocates_nothing(gpu_lib):
+    """A fresh handle that only ever receives allocation-free uploads and steps: the
+    device's free memory is the same before and after the uploads (the regular upload's
+    staging buffer would take 3 n doubles on its first call), and the stepped state
+    equals that of a handle fed by the regular upload."""
+    import torch
+
+    kw = problem(64, 64, 4, seed=23)
+    n = 64 * 64 * 4
+    warm = FdmBackend(**problem(8, 4, 1, seed=2))
+    assert _noalloc(gpu_lib, warm.handle, random_unit(8 * 4, 5)) == _abi.OK  # set-up of the device's array
+    warm.close()
+    be = FdmBackend(**kw)
+    be.step(1e-14)  # two steps: the step graphs of both state buffers exist before the measurement
+    be.step(1e-14)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for seed in (41, 42):
+        assert _noalloc(gpu_lib, be.handle, random_unit(n, seed)) == _abi.OK
+        be.step(1e-14)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, (free0, free1)
+    ref = FdmBackend(**kw)
+    ref.step(1e-14)
+    ref.step(1e-14)
+    ref.upload(random_unit(n, 42))
+    ref.step(1e-14)
+    assert np.array_equal(ref.magnetization(), be.magnetization())
+    be.close()
+    ref.close()
+
+
 def test_noalloc_upload_rejects_bad_input(gpu_lib):
     kw = problem(8, 4, 1, seed=2)
     be = FdmBackend(**kw)
