@@ -562,7 +562,7 @@ def cpu_baseline(w, threads, h_eff_gpu=None):
     if h_eff_gpu is not None:
         pr = oracle_problem(O, w, *full)
         h_ref = pr.fields()["h_eff"]
-        heff_err = float(np.linalg.norm(h_eff_gpu.reshape(-1) - h_ref) / np.linalg.norm(h_ref))
+        heff_err = float(np.linalg.norm(h_eff_gpu.reshape(-1) - h_ref.reshape(-1)) / np.linalg.norm(h_ref))
         del h_ref
         t0 = time.perf_counter()
         pr.step(w["dt"])  # probe step
