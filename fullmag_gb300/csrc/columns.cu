@@ -10,6 +10,7 @@
 // transforms of one CTA, and the y-frequencies ky and py-ky share one CTA so
 // every octant kernel value is read from HBM once per evaluation.
 #include "engine.h"
+#include "fft_pair.cuh"
 
 #include <algorithm>
 
@@ -360,6 +361,111 @@ __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve
         for (int z1 = 0; z1 < H1; ++z1) {
             const int z = N2 * z1 + z2;
             if (z < nz) dst[(size_t)z * zstride] = e[z1];
+        }
+    }
+}
+
+// The pruned two-level z convolution on y-frequency pairs in packed FP32x2 form: lane A
+// is ky, lane B is py - ky (the two share every twiddle and, up to the sign of the
+// odd-in-y components xy and yz, every kernel value).  Tiles of 8 kx columns; phase 1
+// item (c, z2, col), phase 2 item (k1, col) with all three components of both lanes,
+// phase 3 item (c, z2, col).  Shared memory holds pair elements (float4), so the
+// buffer is the size of the unpaired kernel's.  For ky = 0 and ky = py/2 (no partner)
+// lane B repeats lane A and is not stored.
+template <int N1, int N2>
+__global__ void __launch_bounds__(3 * N2 * 8, 2) z_convolve_pair_kernel(const ColPass p) {
+    constexpr int N = N1 * N2, H1 = N1 / 2, TX = 8;
+    constexpr int ls = skewed_len(N);
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4 *buf = reinterpret_cast<float4 *>(smem);  // line (c, col) at (c*TX + col)*ls
+    const Grid &g = p.g;
+    const int kx0 = blockIdx.x * TX, ncol = min(TX, g.nkx - kx0);
+    const int kya = blockIdx.y;
+    int kyb;
+    const int np = ky_pair(kya, g.py, kyb);
+    const int kyB = np == 2 ? kyb : kya;
+    const int nz = g.nz;
+    const size_t cstride = (size_t)nz * g.py * g.nkx;  // component stride of Y
+    const size_t zstride = (size_t)g.py * g.nkx;
+    const float2 *__restrict__ tw = p.plan.tw;        // e^{-2 pi i e / N}
+
+    // phase 1: item (c, z2, col), col fastest
+    for (int it = threadIdx.x; it < 3 * N2 * TX; it += blockDim.x) {
+        const int col = it & (TX - 1), cz = it >> 3;
+        if (col >= ncol) continue;
+        const int z2 = cz & (N2 - 1), c = cz / N2;
+        const float2 *srcA = p.in + c * cstride + (size_t)kya * g.nkx + kx0 + col;
+        const float2 *srcB = p.in + c * cstride + (size_t)kyB * g.nkx + kx0 + col;
+        cp2 e[H1];
+#pragma unroll
+        for (int z1 = 0; z1 < H1; ++z1) {
+            const int z = N2 * z1 + z2;
+            e[z1] = z < nz ? ppack(srcA[(size_t)z * zstride], srcB[(size_t)z * zstride]) : pzero();
+        }
+        phalf_dft_store<N1, N2>(e, z2, buf + (c * TX + col) * ls, tw);
+    }
+    __syncthreads();
+
+    // phase 2: item (k1, col); inner DFTs, the tensor multiply, inverse inner DFTs
+    const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
+    for (int it = threadIdx.x; it < N1 * TX; it += blockDim.x) {
+        const int col = it & (TX - 1), k1 = it >> 3;
+        if (col >= ncol) continue;
+        cp2 m[3][N2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float4 *line = buf + (c * TX + col) * ls;
+#pragma unroll
+            for (int z2 = 0; z2 < N2; ++z2) m[c][z2] = pload(line[sk(k1 * N2 + z2)]);
+            pdft<N2>(m[c], false);
+        }
+        const int kx = kx0 + col;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+            int kzm;
+            float sz;
+            kernel_mirror(k1 + N1 * k2, N, kzm, sz);
+            const float *K = p.kern + ((size_t)kzm * g.nky + kya) * g.nkx + kx;
+            const float kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc);
+            const float kxy = __ldg(K + 3 * kc), kxz = sz * __ldg(K + 4 * kc), kyz = sz * __ldg(K + 5 * kc);
+            // H = -N M; lane B (py - ky) flips the odd-in-y components xy and yz
+            const float2 Nxx = pb(-kxx), Nyy = pb(-kyy), Nzz = pb(-kzz), Nxz = pb(-kxz);
+            const float2 Nxy = make_float2(-kxy, kxy), Nyz = make_float2(-kyz, kyz);
+            const cp2 mx = m[0][k2], my = m[1][k2], mz = m[2][k2];
+            m[0][k2] = {__ffma2_rn(Nxz, mz.re, __ffma2_rn(Nxy, my.re, __fmul2_rn(Nxx, mx.re))),
+                        __ffma2_rn(Nxz, mz.im, __ffma2_rn(Nxy, my.im, __fmul2_rn(Nxx, mx.im)))};
+            m[1][k2] = {__ffma2_rn(Nyz, mz.re, __ffma2_rn(Nyy, my.re, __fmul2_rn(Nxy, mx.re))),
+                        __ffma2_rn(Nyz, mz.im, __ffma2_rn(Nyy, my.im, __fmul2_rn(Nxy, mx.im)))};
+            m[2][k2] = {__ffma2_rn(Nzz, mz.re, __ffma2_rn(Nyz, my.re, __fmul2_rn(Nxz, mx.re))),
+                        __ffma2_rn(Nzz, mz.im, __ffma2_rn(Nyz, my.im, __fmul2_rn(Nxz, mx.im)))};
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            pdft<N2>(m[c], true);
+            float4 *line = buf + (c * TX + col) * ls;
+#pragma unroll
+            for (int z2 = 0; z2 < N2; ++z2)
+                line[sk(k1 * N2 + z2)] = pstore((z2 && k1) ? pmulw(m[c][z2], __ldg(tw + z2 * k1), true) : m[c][z2]);
+        }
+    }
+    __syncthreads();
+
+    // phase 3: item (c, z2, col); outputs z1 < N1/2 with z < nz
+    for (int it = threadIdx.x; it < 3 * N2 * TX; it += blockDim.x) {
+        const int col = it & (TX - 1), cz = it >> 3;
+        if (col >= ncol) continue;
+        const int z2 = cz & (N2 - 1), c = cz / N2;
+        cp2 e[H1];
+        phalf_idft_load<N1, N2>(e, z2, buf + (c * TX + col) * ls, tw);
+        float2 *dstA = p.out + c * cstride + (size_t)kya * g.nkx + kx0 + col;
+        float2 *dstB = p.out + c * cstride + (size_t)kyb * g.nkx + kx0 + col;
+#pragma unroll
+        for (int z1 = 0; z1 < H1; ++z1) {
+            const int z = N2 * z1 + z2;
+            if (z < nz) {
+                dstA[(size_t)z * zstride] = plane_a(e[z1]);
+                if (np == 2) dstB[(size_t)z * zstride] = plane_b(e[z1]);
+            }
         }
     }
 }
@@ -950,7 +1056,29 @@ size_t z_convolve_smem(const Grid &g, int tx) {
     return z_fused_ok(g) ? one : 2 * one;
 }
 
+namespace {
+
+// the packed ky-pair z pass: tile 8, pz = N1 * N2 with an inner radix of 8
+bool z_pair_ok(const Grid &g, int tx) { return tx == 8 && z_fused_ok(g) && (g.pz == 64 || g.pz == 128); }
+
+template <int N1, int N2>
+cudaError_t launch_z_pair(const ColPass &p, cudaStream_t s) {
+    const void *fn = (const void *)z_convolve_pair_kernel<N1, N2>;
+    const size_t sm = sizeof(float4) * (size_t)3 * 8 * skewed_len(N1 * N2);
+    cudaError_t e = ensure_smem(fn, sm);
+    if (e != cudaSuccess) return e;
+    z_convolve_pair_kernel<N1, N2><<<dim3(tiles(p), p.g.nky), 3 * N2 * 8, sm, s>>>(p);
+    return cudaGetLastError();
+}
+}  // namespace
+
+bool z_convolve_pair_ok(const Grid &g, int tx) { return z_pair_ok(g, tx); }
+
 cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
+    if (p.pipe) {
+        if (!z_pair_ok(p.g, p.tx)) return cudaErrorInvalidValue;
+        return p.g.pz == 64 ? launch_z_pair<8, 8>(p, s) : launch_z_pair<16, 8>(p, s);
+    }
     if (z_fused_ok(p.g)) {
         switch (p.g.pz) {
             case 16: return launch_z_fused<4, 4>(p, s);

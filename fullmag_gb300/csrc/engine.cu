@@ -571,6 +571,7 @@ struct Engine {
     // tx_z doubles as the tile of the fused y+z pass when the (y, z) plane of a kx
     // column fits in shared memory (use_yz)
     int tx_yf = 1, tx_z = 1, tx_yi = 1, tx_2d = 1;
+    int z_pair = 0;  // 1: the z pass runs the packed ky-pair kernel (tile 8)
     bool use_yz = false;
     int row_blocks = 1;  // CTAs of the row pass at the current rows-per-CTA
 
@@ -618,7 +619,9 @@ struct Engine {
         kt_end();
         if (cuda_fail("y forward", rc)) return false;
         kt_begin(KT_Z);
-        rc = launch_z_convolve(col_pass(plan_z, tx_z, Y, Y), stream);
+        ColPass zp = col_pass(plan_z, tx_z, Y, Y);
+        zp.pipe = z_pair;
+        rc = launch_z_convolve(zp, stream);
         kt_end();
         if (cuda_fail("z convolve", rc)) return false;
         launches += 3;
@@ -2187,7 +2190,7 @@ struct TuneKey {
     }
 };
 struct TuneChoice {
-    int tx_yf, tx_z, tx_yi, tx_2d, rows;
+    int tx_yf, tx_z, tx_yi, tx_2d, rows, z_pair;
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneChoice> g_tune_cache;
@@ -2207,6 +2210,7 @@ bool Engine::autotune() {
             tx_z = it->second.tx_z;
             tx_yi = it->second.tx_yi;
             tx_2d = it->second.tx_2d;
+            z_pair = it->second.z_pair;
             if (!std::getenv("FULLMAG_FDM_ROWS_PER_CTA")) row_rows = it->second.rows;
             row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
             return true;
@@ -2256,6 +2260,23 @@ bool Engine::autotune() {
             tx_yf = tune(tx_yf, ysm, [&](int tx) { return launch_y_forward(col_pass(plan_y, tx, X, Y), stream) == cudaSuccess; });
             tx_z = tune(tx_z, [&](int tx) { return z_convolve_smem(g, tx); },
                         [&](int tx) { return launch_z_convolve(col_pass(plan_z, tx, Y, Y), stream) == cudaSuccess; });
+            // the packed ky-pair z pass (tile 8) against the best unpaired launch;
+            // FULLMAG_FDM_Z_PAIR=0 or 1 forces the choice
+            z_pair = 0;
+            const char *zp_env = std::getenv("FULLMAG_FDM_Z_PAIR");
+            if (z_convolve_pair_ok(g, 8) && zp_env && zp_env[0] == '1') {
+                tx_z = 8;
+                z_pair = 1;
+            } else if (z_convolve_pair_ok(g, 8) && !(zp_env && zp_env[0] == '0')) {
+                ColPass best = col_pass(plan_z, tx_z, Y, Y), paired = col_pass(plan_z, 8, Y, Y);
+                paired.pipe = 1;
+                const float t_best = time_ms([&] { return launch_z_convolve(best, stream) == cudaSuccess; });
+                const float t_pair = time_ms([&] { return launch_z_convolve(paired, stream) == cudaSuccess; });
+                if (t_pair < t_best) {
+                    tx_z = 8;
+                    z_pair = 1;
+                }
+            }
             tx_yi = tune(tx_yi, ysm, [&](int tx) { return launch_y_inverse(col_pass(plan_y, tx, Y, X), stream) == cudaSuccess; });
         }
     }
@@ -2292,7 +2313,7 @@ bool Engine::autotune() {
     // those is rewritten before it is read again
     if (cuda_fail("autotune sync", cudaStreamSynchronize(stream))) return false;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = TuneChoice{tx_yf, tx_z, tx_yi, tx_2d, row_rows};
+    g_tune_cache[key] = TuneChoice{tx_yf, tx_z, tx_yi, tx_2d, row_rows, z_pair};
     return true;
 }
 
@@ -2749,14 +2770,15 @@ int fullmag_fdm_backend_kernel_times(fullmag_fdm_backend *handle, double *total_
     return FULLMAG_FDM_OK;
 }
 
-int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out5) {
+int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out6) {
     Engine *e = eng(handle);
-    if (!e || !out5) return FULLMAG_FDM_ERR_INVALID;
-    out5[0] = (uint32_t)e->row_rows;
-    out5[1] = (uint32_t)e->tx_yf;
-    out5[2] = (uint32_t)e->tx_z;
-    out5[3] = (uint32_t)e->tx_yi;
-    out5[4] = (uint32_t)e->tx_2d;
+    if (!e || !out6) return FULLMAG_FDM_ERR_INVALID;
+    out6[0] = (uint32_t)e->row_rows;
+    out6[1] = (uint32_t)e->tx_yf;
+    out6[2] = (uint32_t)e->tx_z;
+    out6[3] = (uint32_t)e->tx_yi;
+    out6[4] = (uint32_t)e->tx_2d;
+    out6[5] = (uint32_t)e->z_pair;
     return FULLMAG_FDM_OK;
 }
 

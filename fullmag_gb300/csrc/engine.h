@@ -132,6 +132,7 @@ struct ColPass {
     const float *kern;       // demag kernel (multiply passes)
     int inverse;
     const double *skip_dt;   // batched rounds: the problem's step size; <= 0 skips its tiles
+    int pipe;                // z pass: 1 = the packed ky-pair kernel (tile 8)
 };
 
 // Launchers (kernels.cu)
@@ -147,6 +148,8 @@ size_t yz_convolve_smem(const Grid &g, int tx);
 // K[c][kz][ky][kx] -> K[c][kz][kx][ky] (the fused y+z path's layout), out of place
 cudaError_t launch_kern_ky_fast(const float *in, float *out, int ncomp, int nkz, int nky, int nkx, cudaStream_t s);
 size_t z_convolve_smem(const Grid &g, int tx);
+// the packed ky-pair z pass exists for this grid at tile tx
+bool z_convolve_pair_ok(const Grid &g, int tx);
 size_t y_pass_smem(const Grid &g, int tx);
 size_t y_convolve_2d_smem(const Grid &g, int tx);
 
