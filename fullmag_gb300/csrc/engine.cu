@@ -551,6 +551,7 @@ struct Engine {
     }
 
     bool run_row(RowPass &p) {
+        if (p.x_out) prep_ready = false;  // X no longer holds a prepared first stage
         if (!run_extra(p)) return false;
         if (!demag) {
             p.x_in = nullptr;
@@ -808,15 +809,58 @@ struct Engine {
         }
     }
 
-    // Enqueues a Heun or RK4 step from S[cur] into S[1-cur]; `poll_between`
-    // checks the interrupt callback between passes (eager mode only).
-    int enqueue_fixed_step(double dt, bool poll_between) {
+    // The final evaluation of a fixed step can also form the next step's first stage input
+    // A[0] = N(m' + c dt k1') for the same dt (c = 1/2 for RK4, 1 for Heun), transform it
+    // along x and run the column passes on it: that is all the next step's first pass does,
+    // and k1' is at hand in that evaluation's registers.  The next step at the same dt then
+    // starts with its second pass (RK4: four row passes per step instead of five; Heun: two
+    // instead of three).  prep_ready says that X and A[0] hold that stage for state
+    // parity prep_cur and step prep_dt; any other pass that writes X clears it (run_row).
+    bool prep_ready = false;
+    int prep_cur = -1;
+    double prep_dt = 0.0;
+
+    double first_coef() const { return integrator == FULLMAG_FDM_INTEGRATOR_RK4 ? 0.5 : 1.0; }
+    bool first_ready(double dt) const { return prep_ready && prep_cur == cur && prep_dt == dt; }
+    void mark_next(double dt) {
+        prep_ready = true;
+        prep_cur = cur;
+        prep_dt = dt;
+    }
+
+    // first pass of a fixed step: A[0] = N(m0 + c dt k1), forward x-transform, column passes
+    bool first_stage(double dt) {
+        const int k0[1] = {0};
+        const double c[1] = {first_coef()};
+        return stage(nullptr, nullptr, 1, k0, c, dt, A[0]);
+    }
+
+    // Final evaluation at m (k1' -> K[0], statistics) fused with the next step's first stage.
+    bool final_prepare(float *m, double dt, bool sync) {
+        RowPass p = row_base();
+        p.x_in = X;
+        p.m_in = m;
+        p.k_out = K[0];
+        p.partials = partials;
+        p.m0 = m;
+        p.m_next = A[0];
+        p.n_comb = 1;
+        p.comb_k[0] = nullptr;
+        p.comb_c[0] = (float)first_coef();
+        p.dt = (float)dt;
+        p.x_out = X;
+        return run_row(p) && run_columns() && (sync ? read_stats() : enqueue_stats());
+    }
+
+    // Enqueues a Heun or RK4 step from S[cur] into S[1-cur]; `poll_between` checks the
+    // interrupt callback between passes (eager mode only).  with_first: run the first
+    // pass (else X and A[0] already hold it); prepare: end with final_prepare.
+    int enqueue_fixed_step(double dt, bool poll_between, bool with_first = true, bool prepare = false) {
         const int nxt = 1 - cur;
         if (integrator == FULLMAG_FDM_INTEGRATOR_RK4) {
             const int self[1] = {-1};
             const double h[1] = {0.5}, one[1] = {1.0};
-            const int k0[1] = {0};
-            if (!stage(nullptr, nullptr, 1, k0, h, dt, A[0])) return -1;
+            if (with_first && !first_stage(dt)) return -1;
             if (poll_between && poll_hit()) return 1;
             if (!stage(A[0], K[1], 1, self, h, dt, A[1])) return -1;
             if (poll_between && poll_hit()) return 1;
@@ -826,14 +870,13 @@ struct Engine {
             const double c[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
             if (!stage(A[0], nullptr, 4, k, c, dt, S[nxt])) return -1;
         } else {
-            const int k0[1] = {0};
-            const double c1[1] = {1.0};
-            if (!stage(nullptr, nullptr, 1, k0, c1, dt, A[0])) return -1;
+            if (with_first && !first_stage(dt)) return -1;
             if (poll_between && poll_hit()) return 1;
             const int k[2] = {0, -1};
             const double c[2] = {0.5, 0.5};
             if (!stage(A[0], nullptr, 2, k, c, dt, S[nxt])) return -1;
         }
+        if (prepare) return final_prepare(S[nxt], dt, poll_between) ? 0 : -1;
         return final_eval(S[nxt], K[0], 0, nullptr, nullptr, dt, poll_between) ? 0 : -1;
     }
 
@@ -845,7 +888,8 @@ struct Engine {
         const uint64_t l0 = launches;
         cudaGraph_t graph = nullptr;
         if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
-        const int rc = enqueue_fixed_step(dt, false);
+        // the graph starts at the second pass: the first runs before it unless prepared
+        const int rc = enqueue_fixed_step(dt, false, false, true);
         const cudaError_t e = cudaStreamEndCapture(stream, &graph);
         launches = l0;
         if (rc != 0 || e != cudaSuccess || graph == nullptr) {
@@ -872,6 +916,7 @@ struct Engine {
         // the stages see I(t) and the step's thermal counter; the final evaluation gives the
         // next step's k1, at I(t + dt) and the next counter
         if (!set_oersted(time, time + dt) || !set_thermal(th_step, th_step + 1)) return -1;
+        const bool ready = first_ready(dt);
         if (poll == nullptr && use_graphs && !ktime) {
             if ((!gexec[cur] || gdt[cur] != dt) && !capture_step(dt)) {
                 // capture unavailable: clear the sticky state and fall back to eager launches
@@ -880,16 +925,19 @@ struct Engine {
                 last_error.clear();
             }
             if (use_graphs) {
+                if (!ready && !first_stage(dt)) return -1;
                 if (cuda_fail("graph launch", cudaGraphLaunch(gexec[cur], stream))) return -1;
                 launches += gkernels[cur];
                 if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
                 commit(dt, hstats);
+                mark_next(dt);
                 return 0;
             }
         }
-        const int rc = enqueue_fixed_step(dt, true);
+        const int rc = enqueue_fixed_step(dt, true, !ready, true);
         if (rc != 0) return rc;
         commit(dt, hstats);
+        mark_next(dt);
         return 0;
     }
 
@@ -1082,10 +1130,12 @@ struct Engine {
             use_graphs = false;
             last_error.clear();
         }
+        const bool ready = first_ready(dt);
         if (use_graphs) {
+            if (!ready && !first_stage(dt)) return -1;
             if (cuda_fail("graph launch", cudaGraphLaunch(gexec[cur], stream))) return -1;
             launches += gkernels[cur];
-        } else if (enqueue_fixed_step(dt, false) != 0) {
+        } else if (enqueue_fixed_step(dt, false, !ready, true) != 0) {
             return -1;
         }
         fixed_pending = true;
@@ -1097,6 +1147,7 @@ struct Engine {
         fixed_pending = false;
         if (cuda_fail("stream sync", cudaStreamSynchronize(stream))) return -1;
         commit(fixed_dt, hstats);
+        mark_next(fixed_dt);
         return 1;
     }
 
