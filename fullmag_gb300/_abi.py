@@ -19,6 +19,7 @@ MAX_EXCHANGE_REGIONS = 256
 
 PRECISION_SINGLE = 1
 PRECISION_DOUBLE = 2
+BOUNDARY_NONE, BOUNDARY_VOLUME, BOUNDARY_FULL = 0, 1, 2
 
 INTEGRATOR_HEUN = 1
 INTEGRATOR_DP45 = 2

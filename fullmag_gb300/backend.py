@@ -90,9 +90,15 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
               spectra: Optional[np.ndarray] = None,
               adaptive_max_error: float = 0.0, adaptive_dt_min: float = 0.0,
               adaptive_dt_max: float = 0.0, adaptive_headroom: float = 0.0,
-              precision: int = _abi.PRECISION_SINGLE):
+              precision: int = _abi.PRECISION_SINGLE, boundary: Optional[dict] = None):
     """Fill a fullmag_fdm_plan_desc the way native_fdm.rs:132-499 does.
 
+    ``boundary`` (double precision only) holds the boundary-correction geometry the
+    runner computes (native_fdm.rs:379-468): ``tier`` (``_abi.BOUNDARY_VOLUME`` for T0
+    face links, ``_abi.BOUNDARY_FULL`` for T1 distances), ``volume_fraction``, ``face``
+    (six arrays +x -x +y -y +z -z) or ``delta`` (six arrays), ``phi_floor``,
+    ``delta_min``, and optionally ``corr = (target_idx, source_idx, tensor)`` for the
+    sparse demag correction.
     ``spectra`` is an optional (6, 2P) array of interleaved FP64 Newell spectra
     (xx yy zz xy xz yz) as the reference computes them on the host; when omitted the
     engine builds the tensor on the GPU.  Returns (plan, keepalive): the arrays in
@@ -172,6 +178,34 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
             keep.append(lt)
             p.exchange_lut = _dptr(lt)
             p.exchange_lut_len = lt.size
+    if boundary is not None:
+        def arr(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dtype=dt).reshape(-1)
+            keep.append(a)
+            return a
+        p.boundary_correction = int(boundary.get("tier", 0))
+        p.boundary_phi_floor = float(boundary.get("phi_floor", 0.0))
+        p.boundary_delta_min = float(boundary.get("delta_min", 0.0))
+        if boundary.get("volume_fraction") is not None:
+            vf = arr(boundary["volume_fraction"])
+            p.volume_fraction = _dptr(vf)
+            p.volume_fraction_len = vf.size
+        names = ("xp", "xm", "yp", "ym", "zp", "zm")
+        for q, a in enumerate(boundary.get("face") or []):
+            setattr(p, "face_link_" + names[q], _dptr(arr(a)))
+        for q, a in enumerate(boundary.get("delta") or []):
+            setattr(p, "delta_" + names[q], _dptr(arr(a)))
+        if boundary.get("corr") is not None:
+            t, src, ten = boundary["corr"]
+            t = arr(t, np.int32)
+            src = arr(src, np.int32)
+            ten = arr(ten)
+            p.has_demag_boundary_corr = 1
+            p.demag_corr_target_idx = t.ctypes.data_as(C.POINTER(C.c_int32))
+            p.demag_corr_source_idx = src.ctypes.data_as(C.POINTER(C.c_int32))
+            p.demag_corr_tensor = _dptr(ten)
+            p.demag_corr_target_count = t.size
+            p.demag_corr_stencil_size = src.size // max(t.size, 1)
     m = np.ascontiguousarray(m0, dtype=np.float64).reshape(-1)
     keep.append(m)
     p.initial_magnetization_xyz = _dptr(m)

@@ -16,7 +16,7 @@ PKG = Path(__file__).resolve().parent
 SRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libfullmag_fdm.so"
-SOURCES = ["row_pass.cu", "columns.cu", "engine.cu", "newell.cu", "adjoint.cu", "noalloc.cu", "extra_field.cu"]
+SOURCES = ["row_pass.cu", "columns.cu", "engine.cu", "newell.cu", "adjoint.cu", "noalloc.cu", "extra_field.cu", "fp64.cu"]
 # the cuFFT + unfused measurement baseline: a separate library, never linked into the product
 PLAIN_SOURCES = ["plain_baseline.cu"]
 PLAIN_LIB = OUT / "libfullmag_fdm_plain.so"

@@ -27,6 +27,7 @@
 
 #include "../../include/fullmag_fdm.h"
 #include "engine.h"
+#include "fp64.h"
 #include "noalloc.h"
 
 namespace fm {
@@ -174,6 +175,41 @@ struct PinnedPool {
 
 // Snapshot payload: host-synthesised bytes, or a pinned buffer that a device-to-host
 // copy on the backend's snapshot stream fills; `done` marks the end of that copy.
+// Box average of a full AoS field (3 values per cell) onto a pnx x pny x pnz preview grid:
+// x and y bins split the grid evenly, z bins start at z0 and are zs planes thick; FP64
+// sums in z, y, x order.
+template <typename T>
+static void host_preview(const double *full, uint32_t fx, uint32_t fy, uint32_t fz, uint32_t pnx, uint32_t pny,
+                         uint32_t pnz, uint32_t z0, uint32_t zs, T *out) {
+    for (uint32_t pz = 0; pz < pnz; ++pz) {
+        uint32_t zs0 = z0 + pz * zs;
+        if (zs0 >= fz) zs0 = fz - 1;
+        uint32_t ze = z0 + (pz + 1) * zs;
+        if (ze <= zs0) ze = zs0 + 1;
+        if (ze > fz) ze = fz;
+        for (uint32_t py = 0; py < pny; ++py) {
+            uint32_t ys = (uint32_t)(((uint64_t)py * fy) / pny), ye = (uint32_t)(((uint64_t)(py + 1) * fy) / pny);
+            if (ye <= ys) ye = ys + 1;
+            if (ye > fy) ye = fy;
+            for (uint32_t px = 0; px < pnx; ++px) {
+                uint32_t xs = (uint32_t)(((uint64_t)px * fx) / pnx), xe = (uint32_t)(((uint64_t)(px + 1) * fx) / pnx);
+                if (xe <= xs) xe = xs + 1;
+                if (xe > fx) xe = fx;
+                double a[3] = {0, 0, 0}, cnt = 0;
+                for (uint32_t z = zs0; z < ze; ++z)
+                    for (uint32_t y = ys; y < ye; ++y)
+                        for (uint32_t x = xs; x < xe; ++x) {
+                            const size_t i = ((size_t)z * fy + y) * fx + x;
+                            for (int c = 0; c < 3; ++c) a[c] += full[3 * i + c];
+                            cnt += 1.0;
+                        }
+                const size_t o = ((size_t)pz * pny + py) * pnx + px;
+                for (int c = 0; c < 3; ++c) out[3 * o + c] = (T)(a[c] / cnt);
+            }
+        }
+    }
+}
+
 struct SnapshotPayload {
     std::vector<unsigned char> bytes;
     std::shared_ptr<PinnedPool> pool;
@@ -307,7 +343,14 @@ struct Engine {
 
     ~Engine() { release(); }
 
+    // a handle created with FULLMAG_FDM_PRECISION_DOUBLE is served by the FP64 path (fp64.cu)
+    Fp64Engine *f64 = nullptr;
+
     void release() {
+        if (f64) {
+            fp64_destroy(f64);
+            f64 = nullptr;
+        }
         if (stream) cudaStreamSynchronize(stream);
         if (snap_stream) {
             cudaStreamSynchronize(snap_stream);
@@ -1716,34 +1759,7 @@ struct Engine {
         // H_EXT lives on the host: the same box average over the synthesised field
         std::vector<double> full(3 * (size_t)g.n);
         if (!download<double>(obs, full.data())) return false;
-        const uint32_t fx = g.nx, fy = g.ny, fz = g.nz;
-        for (uint32_t pz = 0; pz < pnz; ++pz) {
-            uint32_t zs0 = z0 + pz * zs;
-            if (zs0 >= fz) zs0 = fz - 1;
-            uint32_t ze = z0 + (pz + 1) * zs;
-            if (ze <= zs0) ze = zs0 + 1;
-            if (ze > fz) ze = fz;
-            for (uint32_t py = 0; py < pny; ++py) {
-                uint32_t ys = (uint32_t)(((uint64_t)py * fy) / pny), ye = (uint32_t)(((uint64_t)(py + 1) * fy) / pny);
-                if (ye <= ys) ye = ys + 1;
-                if (ye > fy) ye = fy;
-                for (uint32_t px = 0; px < pnx; ++px) {
-                    uint32_t xs = (uint32_t)(((uint64_t)px * fx) / pnx), xe = (uint32_t)(((uint64_t)(px + 1) * fx) / pnx);
-                    if (xe <= xs) xe = xs + 1;
-                    if (xe > fx) xe = fx;
-                    double a[3] = {0, 0, 0}, cnt = 0;
-                    for (uint32_t z = zs0; z < ze; ++z)
-                        for (uint32_t y = ys; y < ye; ++y)
-                            for (uint32_t x = xs; x < xe; ++x) {
-                                const size_t i = ((size_t)z * fy + y) * fx + x;
-                                for (int c = 0; c < 3; ++c) a[c] += full[3 * i + c];
-                                cnt += 1.0;
-                            }
-                    const size_t o = ((size_t)pz * pny + py) * pnx + px;
-                    for (int c = 0; c < 3; ++c) out[3 * o + c] = (T)(a[c] / cnt);
-                }
-            }
-        }
+        host_preview<T>(full.data(), g.nx, g.ny, g.nz, pnx, pny, pnz, z0, zs, out);
         return true;
     }
 };
@@ -2400,6 +2416,37 @@ using namespace fm;
 
 static Engine *eng(fullmag_fdm_backend *h) { return reinterpret_cast<Engine *>(h); }
 
+// copy of an observable of a double-precision handle (AoS doubles, or floats converted on the host)
+template <typename T>
+static int f64_copy(Engine *e, int observable, T *out, uint64_t out_len) {
+    int nx, ny, nz;
+    fp64_grid(e->f64, nx, ny, nz);
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    if (out_len != 3 * n) {
+        e->last_error = "out_len mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    if (observable < FULLMAG_FDM_OBSERVABLE_M || observable > FULLMAG_FDM_OBSERVABLE_H_EFF) {
+        e->last_error = "unknown observable";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    std::vector<double> tmp;
+    double *dst = reinterpret_cast<double *>(out);
+    if (sizeof(T) != sizeof(double)) {
+        tmp.resize(3 * n);
+        dst = tmp.data();
+    }
+    std::string err;
+    if (!fp64_download(e->f64, observable, dst, err)) {
+        e->last_error = err;
+        return FULLMAG_FDM_ERR_CUDA;
+    }
+    if (sizeof(T) != sizeof(double))
+        for (uint64_t i = 0; i < 3 * n; ++i) out[i] = (T)tmp[i];
+    return FULLMAG_FDM_OK;
+}
+
+
 static int device_from_env() {
     const char *a = std::getenv("FULLMAG_FDM_GPU_INDEX");
     const char *b = std::getenv("FULLMAG_CUDA_DEVICE_INDEX");
@@ -2415,10 +2462,23 @@ template <typename T>
 static int preview_impl(fullmag_fdm_backend *handle, fullmag_fdm_observable obs, uint32_t pnx, uint32_t pny, uint32_t pnz,
                         uint32_t z0, uint32_t zs, T *out, uint64_t out_len) {
     Engine *e = eng(handle);
-    if (!e || !out || pnx == 0 || pny == 0 || pnz == 0 || zs == 0 || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (!e || !out || pnx == 0 || pny == 0 || pnz == 0 || zs == 0 || (!e->arena && !e->f64)) return FULLMAG_FDM_ERR_INVALID;
     if (out_len != (uint64_t)pnx * pny * pnz * 3) {
         e->last_error = "preview out_len mismatch";
         return FULLMAG_FDM_ERR_INVALID;
+    }
+    if (e->f64) {  // the box average of the FP64 field, on the host
+        int nx, ny, nz;
+        fp64_grid(e->f64, nx, ny, nz);
+        if (z0 >= (uint32_t)nz) {
+            e->last_error = "preview z_origin out of range";
+            return FULLMAG_FDM_ERR_INVALID;
+        }
+        std::vector<double> full(3 * (size_t)nx * ny * nz);
+        const int rc = f64_copy<double>(e, obs, full.data(), full.size());
+        if (rc != FULLMAG_FDM_OK) return rc;
+        host_preview<T>(full.data(), nx, ny, nz, pnx, pny, pnz, z0, zs, out);
+        return FULLMAG_FDM_OK;
     }
     return e->preview<T>(obs, pnx, pny, pnz, z0, zs, out) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
 }
@@ -2459,6 +2519,12 @@ fullmag_fdm_backend *fullmag_fdm_backend_create(const fullmag_fdm_plan_desc *pla
             return reinterpret_cast<fullmag_fdm_backend *>(e);
         }
     }
+    if (plan->precision == FULLMAG_FDM_PRECISION_DOUBLE) {
+        std::string err;
+        e->f64 = fp64_create(plan, err);
+        if (!e->f64) e->last_error = err;
+        return reinterpret_cast<fullmag_fdm_backend *>(e);
+    }
     if (!e->setup(plan)) return reinterpret_cast<fullmag_fdm_backend *>(e);
     if (!e->upload<double>(plan->initial_magnetization_xyz)) return reinterpret_cast<fullmag_fdm_backend *>(e);
     if (!e->eval_state(true)) return reinterpret_cast<fullmag_fdm_backend *>(e);
@@ -2468,11 +2534,17 @@ fullmag_fdm_backend *fullmag_fdm_backend_create(const fullmag_fdm_plan_desc *pla
 int fullmag_fdm_backend_step(fullmag_fdm_backend *handle, double dt_seconds, fullmag_fdm_step_stats *out_stats) {
     Engine *e = eng(handle);
     if (!e || !out_stats) return FULLMAG_FDM_ERR_INVALID;
-    if (!e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (!e->arena && !e->f64) return FULLMAG_FDM_ERR_INVALID;
     e->last_error.clear();
     if (!(dt_seconds > 0.0) || !std::isfinite(dt_seconds)) {
         e->last_error = "dt_seconds must be positive and finite";
         return FULLMAG_FDM_ERR_INVALID;
+    }
+    if (e->f64) {
+        std::string err;
+        const int rc = fp64_step(e->f64, dt_seconds, out_stats, e->poll, e->poll_user, err);
+        if (rc != FULLMAG_FDM_OK) e->last_error = err;
+        return rc;
     }
     const auto t0 = std::chrono::steady_clock::now();
     const int rc = e->step(dt_seconds);
@@ -2492,9 +2564,9 @@ int fullmag_fdm_backend_step(fullmag_fdm_backend *handle, double dt_seconds, ful
 int fullmag_fdm_backend_step_many(fullmag_fdm_backend *handle, double dt_seconds, uint64_t n_steps,
                                   fullmag_fdm_step_stats *out_stats) {
     Engine *e = eng(handle);
-    if (!e || !out_stats || !e->arena) return FULLMAG_FDM_ERR_INVALID;
+    if (!e || !out_stats || (!e->arena && !e->f64)) return FULLMAG_FDM_ERR_INVALID;
     e->last_error.clear();
-    if (e->adaptive()) {
+    if (!e->f64 && e->adaptive()) {
         e->last_error = "step_many supports fixed-step integrators only";
         return FULLMAG_FDM_ERR_INVALID;
     }
@@ -2516,6 +2588,7 @@ int fullmag_fdm_backend_set_interrupt_poll(fullmag_fdm_backend *handle, fullmag_
 int fullmag_fdm_backend_copy_field_f64(fullmag_fdm_backend *handle, fullmag_fdm_observable observable, double *out_xyz,
                                        uint64_t out_len) {
     Engine *e = eng(handle);
+    if (e && out_xyz && e->f64) return f64_copy<double>(e, observable, out_xyz, out_len);
     if (!e || !out_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     if (out_len != 3 * (uint64_t)e->g.n) {
         e->last_error = "out_len mismatch";
@@ -2531,6 +2604,7 @@ int fullmag_fdm_backend_copy_field_f64(fullmag_fdm_backend *handle, fullmag_fdm_
 int fullmag_fdm_backend_copy_field_f32(fullmag_fdm_backend *handle, fullmag_fdm_observable observable, float *out_xyz,
                                        uint64_t out_len) {
     Engine *e = eng(handle);
+    if (e && out_xyz && e->f64) return f64_copy<float>(e, observable, out_xyz, out_len);
     if (!e || !out_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     if (out_len != 3 * (uint64_t)e->g.n) {
         e->last_error = "out_len mismatch";
@@ -2558,9 +2632,29 @@ int fullmag_fdm_backend_copy_field_preview_f32(fullmag_fdm_backend *handle, full
 fullmag_fdm_field_snapshot *fullmag_fdm_backend_begin_field_snapshot(fullmag_fdm_backend *handle,
                                                                      fullmag_fdm_observable observable) {
     Engine *e = eng(handle);
-    if (!e || !e->arena) return nullptr;
+    if (!e || (!e->arena && !e->f64)) return nullptr;
     auto *s = new (std::nothrow) SnapshotPayload();
     if (!s) return nullptr;
+    if (e->f64) {  // double precision: captured synchronously, component-major FP64
+        int nx, ny, nz;
+        fp64_grid(e->f64, nx, ny, nz);
+        const size_t n = (size_t)nx * ny * nz;
+        std::vector<double> aos(3 * n);
+        if (f64_copy<double>(e, observable, aos.data(), aos.size()) != FULLMAG_FDM_OK) {
+            delete s;
+            return nullptr;
+        }
+        s->bytes.resize(sizeof(double) * 3 * n);
+        double *soa = reinterpret_cast<double *>(s->bytes.data());
+        for (size_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) soa[c * n + i] = aos[3 * i + c];
+        s->desc.cell_count = n;
+        s->desc.component_count = 3;
+        s->desc.scalar_bytes = 8;
+        s->desc.scalar_type = FULLMAG_FDM_SNAPSHOT_SCALAR_F64;
+        s->ok = true;
+        return reinterpret_cast<fullmag_fdm_field_snapshot *>(s);
+    }
     const size_t n = (size_t)e->g.n;
     if (observable == FULLMAG_FDM_OBSERVABLE_H_EXT) {  // synthesised on the host
         std::vector<float> aos(3 * n);
@@ -2602,10 +2696,25 @@ fullmag_fdm_preview_snapshot *fullmag_fdm_backend_begin_preview_snapshot(fullmag
                                                                          uint32_t preview_nz, uint32_t z_origin,
                                                                          uint32_t z_stride) {
     Engine *e = eng(handle);
-    if (!e || !e->arena || preview_nx == 0 || preview_ny == 0 || preview_nz == 0 || z_stride == 0) return nullptr;
+    if (!e || (!e->arena && !e->f64) || preview_nx == 0 || preview_ny == 0 || preview_nz == 0 || z_stride == 0)
+        return nullptr;
     auto *s = new (std::nothrow) SnapshotPayload();
     if (!s) return nullptr;
     const size_t n = (size_t)preview_nx * preview_ny * preview_nz;
+    if (e->f64) {  // double precision: the FP64 box average, captured synchronously
+        s->bytes.resize(sizeof(double) * 3 * n);
+        if (preview_impl<double>(handle, observable, preview_nx, preview_ny, preview_nz, z_origin, z_stride,
+                                 reinterpret_cast<double *>(s->bytes.data()), 3 * n) != FULLMAG_FDM_OK) {
+            delete s;
+            return nullptr;
+        }
+        s->desc.cell_count = n;
+        s->desc.component_count = 3;
+        s->desc.scalar_bytes = 8;
+        s->desc.scalar_type = FULLMAG_FDM_SNAPSHOT_SCALAR_F64;
+        s->ok = true;
+        return reinterpret_cast<fullmag_fdm_preview_snapshot *>(s);
+    }
     if (z_origin >= (uint32_t)e->g.nz) {
         e->last_error = "preview z_origin out of range";
         delete s;
@@ -2658,8 +2767,25 @@ void fullmag_fdm_preview_snapshot_destroy(fullmag_fdm_preview_snapshot *snapshot
     delete reinterpret_cast<SnapshotPayload *>(snapshot);
 }
 
+// upload to a double-precision handle
+static int f64_upload(Engine *e, const double *m_xyz, uint64_t len) {
+    int nx, ny, nz;
+    fp64_grid(e->f64, nx, ny, nz);
+    if (len != 3 * (uint64_t)nx * ny * nz) {
+        e->last_error = "magnetization length mismatch";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
+    std::string err;
+    if (!fp64_upload(e->f64, m_xyz, err)) {
+        e->last_error = err;
+        return FULLMAG_FDM_ERR_CUDA;
+    }
+    return FULLMAG_FDM_OK;
+}
+
 int fullmag_fdm_backend_upload_magnetization_f64(fullmag_fdm_backend *handle, const double *m_xyz, uint64_t len) {
     Engine *e = eng(handle);
+    if (e && m_xyz && e->f64) return f64_upload(e, m_xyz, len);
     if (!e || !m_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     if (len != 3 * (uint64_t)e->g.n) {
         e->last_error = "magnetization length mismatch";
@@ -2686,6 +2812,10 @@ int fullmag_fdm_backend_upload_magnetization_f64_noalloc(fullmag_fdm_backend *ha
 
 int fullmag_fdm_backend_upload_magnetization_f32(fullmag_fdm_backend *handle, const float *m_xyz, uint64_t len) {
     Engine *e = eng(handle);
+    if (e && m_xyz && e->f64) {
+        std::vector<double> d(m_xyz, m_xyz + len);
+        return f64_upload(e, d.data(), len);
+    }
     if (!e || !m_xyz || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     if (len != 3 * (uint64_t)e->g.n) {
         e->last_error = "magnetization length mismatch";
@@ -2696,18 +2826,37 @@ int fullmag_fdm_backend_upload_magnetization_f32(fullmag_fdm_backend *handle, co
 
 int fullmag_fdm_backend_refresh_observables(fullmag_fdm_backend *handle) {
     Engine *e = eng(handle);
+    if (e && e->f64) {
+        std::string err;
+        if (fp64_refresh(e->f64, err)) return FULLMAG_FDM_OK;
+        e->last_error = err;
+        return FULLMAG_FDM_ERR_CUDA;
+    }
     if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     return e->eval_state(true) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
 }
 
 int fullmag_fdm_backend_refresh_demag_observable(fullmag_fdm_backend *handle) {
     Engine *e = eng(handle);
+    if (e && e->f64) {
+        std::string err;
+        if (fp64_refresh(e->f64, err)) return FULLMAG_FDM_OK;
+        e->last_error = err;
+        return FULLMAG_FDM_ERR_CUDA;
+    }
     if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     return e->eval_state(true) ? FULLMAG_FDM_OK : FULLMAG_FDM_ERR_CUDA;
 }
 
 int fullmag_fdm_backend_snapshot_stats(fullmag_fdm_backend *handle, fullmag_fdm_step_stats *out_stats) {
     Engine *e = eng(handle);
+    if (e && out_stats && e->f64) {
+        fp64_stats(e->f64, out_stats);
+        out_stats->dt_seconds = 0.0;
+        out_stats->suggested_next_dt = 0.0;
+        out_stats->wall_time_ns = 0;
+        return FULLMAG_FDM_OK;
+    }
     if (!e || !out_stats || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     if (!e->stats_valid && !e->eval_state(false)) return FULLMAG_FDM_ERR_CUDA;
     *out_stats = e->cur_stats;
@@ -2843,6 +2992,10 @@ int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_
 int fullmag_fdm_backend_fft_shape(fullmag_fdm_backend *handle, uint32_t *out_px, uint32_t *out_py, uint32_t *out_pz) {
     Engine *e = eng(handle);
     if (!e || !out_px || !out_py || !out_pz) return FULLMAG_FDM_ERR_INVALID;
+    if (e->f64) {
+        fp64_fft_shape(e->f64, *out_px, *out_py, *out_pz);
+        return FULLMAG_FDM_OK;
+    }
     *out_px = e->g.px;
     *out_py = e->g.py;
     *out_pz = e->g.pz;

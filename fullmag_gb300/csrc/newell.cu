@@ -176,13 +176,14 @@ __global__ void axis_transform_kernel(const double *__restrict__ in, double *__r
     }
 }
 
-__global__ void to_float_kernel(const double *__restrict__ in, float *__restrict__ out, long long per, int ncomp,
+template <typename T>
+__global__ void to_float_kernel(const double *__restrict__ in, T *__restrict__ out, long long per, int ncomp,
                                 double scale, unsigned neg_mask) {
     const long long total = per * ncomp;
     for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
         const int c = (int)(id / per);
         const double s = ((neg_mask >> c) & 1u) ? -scale : scale;
-        out[id] = (float)(in[id] * s);
+        out[id] = (T)(in[id] * s);
     }
 }
 
@@ -196,9 +197,10 @@ static bool ck(cudaError_t e, const char *what, std::string &err) {
     return false;
 }
 
-// Builds the octant kernel (layout of engine.h) scaled by ms / P into `kern`.
-bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
-                         std::string &err) {
+// Builds the octant kernel (layout of engine.h) scaled by ms / P into `kern` (FP32) or
+// `kern64` (FP64, for the double-precision state path); exactly one of them is non-null.
+static bool newell_build(const Grid &g, double dx, double dy, double dz, double ms, float *kern, double *kern64,
+                         cudaStream_t s, std::string &err) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int sx = std::min(nx, kAsym) + 2, sy = std::min(ny, kAsym) + 2, sz = std::min(nz, kAsym) + 2;
     const long long tl = (long long)sx * sy * sz;
@@ -241,14 +243,16 @@ bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double 
             const long long per = (long long)g.nky * g.nkx;
             const double scale = ms / ((double)g.px * g.py);
             // components 0..3 of Bb are contiguous blocks of nz*nky*nkx = per (nz == 1)
-            to_float_kernel<<<grid_for(per * 4), 256, 0, s>>>(Bb, kern, per, 4, scale, 1u << 3);
+            if (kern64) to_float_kernel<<<grid_for(per * 4), 256, 0, s>>>(Bb, kern64, per, 4, scale, 1u << 3);
+            else to_float_kernel<<<grid_for(per * 4), 256, 0, s>>>(Bb, kern, per, 4, scale, 1u << 3);
         } else {
             // z: [c][k][(ky,kx)] -> [c][kz][(ky,kx)]
             axis_transform_kernel<<<grid_for(sizeC), 256, 0, s>>>(Bb, Cb, 6, 1, nz, g.nkz, g.nky * g.nkx, g.pz, dtw + off[2],
                                                                   oddz);
             const long long per = (long long)g.nkz * g.nky * g.nkx;
             const double scale = ms / ((double)g.px * g.py * g.pz);
-            to_float_kernel<<<grid_for(per * 6), 256, 0, s>>>(Cb, kern, per, 6, scale, neg);
+            if (kern64) to_float_kernel<<<grid_for(per * 6), 256, 0, s>>>(Cb, kern64, per, 6, scale, neg);
+            else to_float_kernel<<<grid_for(per * 6), 256, 0, s>>>(Cb, kern, per, 6, scale, neg);
         }
         ok = ck(cudaGetLastError(), "newell kernels", err) && ck(cudaStreamSynchronize(s), "newell sync", err);
     }
@@ -260,6 +264,16 @@ bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double 
     cudaFree(Cb);
     cudaFree(dtw);
     return ok;
+}
+
+bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, float *kern, cudaStream_t s,
+                         std::string &err) {
+    return newell_build(g, dx, dy, dz, ms, kern, nullptr, s, err);
+}
+
+bool newell_spectrum_gpu64(const Grid &g, double dx, double dy, double dz, double ms, double *kern, cudaStream_t s,
+                           std::string &err) {
+    return newell_build(g, dx, dy, dz, ms, nullptr, kern, s, err);
 }
 
 }  // namespace fm

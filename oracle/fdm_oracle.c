@@ -435,9 +435,18 @@ struct fo_problem {
     double *hmap; /* optional per-cell applied field (AoS, A/m) */
     uint32_t *region; /* optional region ids */
     double *lut;      /* FO_MAX_REGIONS^2 inter-region exchange stiffness (J/m) when region != NULL */
+    /* boundary correction (copies of the plan arrays) */
+    double *phi, *face[6], *delta[6];
+    int32_t *ctidx, *csidx;
+    double *ctensor;
 };
 
-static inline int active(const fo_problem *pr, long i) { return pr->mask == NULL || pr->mask[i] != 0; }
+/* a cell takes part when the mask allows it and, with a boundary tier, its volume
+ * fraction is positive */
+static inline int active(const fo_problem *pr, long i) {
+    return (pr->mask == NULL || pr->mask[i] != 0) && (pr->p.boundary_tier == 0 || pr->phi[i] > 0.0);
+}
+static inline double phi_w(const fo_problem *pr, long i) { return pr->p.boundary_tier > 0 ? pr->phi[i] : 1.0; }
 
 static void norm3(const double *a, double *o) {
     double n = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
@@ -461,7 +470,17 @@ void fo_destroy(fo_problem *pr) {
     for (int s = 0; s < 3; ++s) free(pr->abm_h[s]);
     for (int s = 0; s < 5; ++s) free(pr->kmap[s]);
     free(pr->h_oe);
+    free(pr->phi);
+    for (int q = 0; q < 6; ++q) { free(pr->face[q]); free(pr->delta[q]); }
+    free(pr->ctidx); free(pr->csidx); free(pr->ctensor);
     free(pr);
+}
+
+static double *dcopy(const double *src, long n) {
+    if (!src) return NULL;
+    double *d = (double *)malloc(sizeof(double) * (size_t)n);
+    memcpy(d, src, sizeof(double) * (size_t)n);
+    return d;
 }
 
 /* A new state or field invalidates the FSAL derivative and the ABM3 history. */
@@ -508,6 +527,28 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     }
     pr->n = (long)p->nx * p->ny * p->nz;
     const long n3 = 3 * pr->n;
+    pr->phi = dcopy(p->volume_fraction, pr->n);
+    for (int q = 0; q < 6; ++q) {
+        pr->face[q] = dcopy(p->face[q], pr->n);
+        pr->delta[q] = dcopy(p->delta[q], pr->n);
+    }
+    if (p->boundary_tier > 0 && (!pr->phi || (p->boundary_tier == 1 && !pr->face[0]) || (p->boundary_tier == 2 && !pr->delta[0]))) {
+        fo_destroy(pr);
+        return NULL;
+    }
+    if (p->corr_targets > 0) {
+        const long ns = (long)p->corr_targets * p->corr_stencil;
+        pr->ctidx = (int32_t *)malloc(sizeof(int32_t) * p->corr_targets);
+        memcpy(pr->ctidx, p->corr_target_idx, sizeof(int32_t) * p->corr_targets);
+        pr->csidx = (int32_t *)malloc(sizeof(int32_t) * (size_t)ns);
+        memcpy(pr->csidx, p->corr_source_idx, sizeof(int32_t) * (size_t)ns);
+        pr->ctensor = dcopy(p->corr_tensor, 6 * ns);
+    }
+    pr->p.volume_fraction = pr->phi;
+    pr->p.corr_target_idx = NULL;
+    pr->p.corr_source_idx = NULL;
+    pr->p.corr_tensor = NULL;
+    for (int q = 0; q < 6; ++q) pr->p.face[q] = pr->p.delta[q] = NULL;
     if (p->active_mask) {
         pr->mask = (uint8_t *)malloc((size_t)pr->n);
         memcpy(pr->mask, p->active_mask, (size_t)pr->n);
@@ -622,6 +663,36 @@ static void exchange_add(const fo_problem *pr, const double *m, double *h) {
         nb[5] = i + (z < nz - 1 ? (long)nx * ny : 0);
         for (int q = 0; q < 6; ++q)
             if (!active(pr, nb[q])) nb[q] = i;
+        if (p->boundary_tier > 0) {
+            /* T0: 2/(mu0 Ms phi_eff) sum_faces f A_ij (m_j - m_i)/d^2; T1: the same with
+             * 2 A_ij / (d (d + delta_opposite)) per face and neighbours with m_j = 0 left out;
+             * phi_eff = max(phi, phi_floor).  A_ij = A without regions (entering once). */
+            const long off[6] = {1, -1, nx, -(long)nx, (long)nx * ny, -(long)nx * ny};
+            const int has[6] = {x + 1 < nx, x > 0, y + 1 < ny, y > 0, z + 1 < nz, z > 0};
+            const double d[6] = {p->dx, p->dx, p->dy, p->dy, p->dz, p->dz};
+            double acc[3] = {0.0, 0.0, 0.0};
+            for (int q = 0; q < 6; ++q) {
+                if (q >= 4 && nz <= 1) continue;
+                if (!has[q]) continue;
+                const long j = i + off[q];
+                const double A = pr->region ? pr->lut[pr->region[i] * FO_MAX_REGIONS + pr->region[j]] : p->a_ex;
+                double w;
+                if (p->boundary_tier == 1) {
+                    const double f = pr->face[q][i];
+                    if (!(f > 0.0)) continue;
+                    w = A * f / (d[q] * d[q]);
+                } else {
+                    const double dsel = fmax(pr->delta[q][i], p->delta_min), dopp = fmax(pr->delta[q ^ 1][i], p->delta_min);
+                    if (!(dsel > 0.0)) continue;
+                    if (m[3 * j] == 0.0 && m[3 * j + 1] == 0.0 && m[3 * j + 2] == 0.0) continue;
+                    w = A * 2.0 / (d[q] * (d[q] + dopp));
+                }
+                for (int c = 0; c < 3; ++c) acc[c] += w * (m[3 * j + c] - m[3 * i + c]);
+            }
+            const double s = 2.0 / (FO_MU0 * p->ms * fmax(pr->phi[i], p->phi_floor));
+            for (int c = 0; c < 3; ++c) h[3 * i + c] += s * acc[c];
+            continue;
+        }
         if (pr->region) {  /* exchange_fp32.cu:48-104: 2/(mu0 Ms) sum_q A[r_i][r_q] (m_q - m_i)/d^2 */
             const double w[6] = {ix2, ix2, iy2, iy2, iz2, iz2};
             const double s = 2.0 / (FO_MU0 * p->ms);
@@ -654,7 +725,7 @@ static void demag_add(fo_problem *pr, const double *m, double *h) {
     for (long i = 0; i < pr->n; ++i) {
         const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
         const long d = (long)x + (long)px * (y + (long)py * z);
-        for (int c = 0; c < 3; ++c) pr->bm[c][2 * d] = active(pr, i) ? m[3 * i + c] * p->ms : 0.0;
+        for (int c = 0; c < 3; ++c) pr->bm[c][2 * d] = active(pr, i) ? m[3 * i + c] * p->ms * phi_w(pr, i) : 0.0;
     }
     for (int c = 0; c < 3; ++c) fo_fft3d(pr->bm[c], px, py, pz, 0);
     double *const *K = pr->kern;
@@ -685,6 +756,21 @@ static void demag_add(fo_problem *pr, const double *m, double *h) {
         for (int c = 0; c < 3; ++c) h[3 * i + c] += pr->bh[c][2 * s] * norm;
     }
     (void)nz;
+    /* sparse boundary correction (targets in order; a repeated target accumulates) */
+    for (uint32_t t = 0; t < p->corr_targets; ++t) {
+        const int32_t ti = pr->ctidx[t];
+        if (ti < 0) continue;
+        for (uint32_t q = 0; q < p->corr_stencil; ++q) {
+            const int32_t si = pr->csidx[(size_t)t * p->corr_stencil + q];
+            if (si < 0) continue;
+            const double *N = pr->ctensor + ((size_t)t * p->corr_stencil + q) * 6;
+            const double w = (pr->phi ? pr->phi[si] : 1.0) * p->ms;
+            const double Mx = w * m[3 * si], My = w * m[3 * si + 1], Mz = w * m[3 * si + 2];
+            h[3 * ti] -= N[0] * Mx + N[1] * My + N[2] * Mz;
+            h[3 * ti + 1] -= N[1] * Mx + N[3] * My + N[4] * Mz;
+            h[3 * ti + 2] -= N[2] * Mx + N[4] * My + N[5] * Mz;
+        }
+    }
 }
 
 /* Uniaxial + cubic anisotropy field (fdm_fields.rs:648-705, 910-1047). The Kc3 term
@@ -996,21 +1082,22 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
                 if (nb[q] < 0 || !active(pr, nb[q])) continue;
                 const double a = m[3 * nb[q]] - mi[0], b = m[3 * nb[q] + 1] - mi[1], c = m[3 * nb[q] + 2] - mi[2];
                 const double A = pr->region ? pr->lut[pr->region[i] * FO_MAX_REGIONS + pr->region[nb[q]]] : p->a_ex;
-                epair += A * V * (a * a + b * b + c * c) * w[q];
+                epair += A * V * phi_w(pr, i) * (a * a + b * b + c * c) * w[q];
             }
             exf += -0.5 * FO_MU0 * p->ms * V * (mi[0] * h_ex[3 * i] + mi[1] * h_ex[3 * i + 1] + mi[2] * h_ex[3 * i + 2]);
         }
+        const double ph = phi_w(pr, i);
         if (p->enable_demag)
-            ed += -0.5 * FO_MU0 * p->ms * V * (mi[0] * h_d[3 * i] + mi[1] * h_d[3 * i + 1] + mi[2] * h_d[3 * i + 2]);
+            ed += -0.5 * FO_MU0 * p->ms * V * ph * (mi[0] * h_d[3 * i] + mi[1] * h_d[3 * i + 1] + mi[2] * h_d[3 * i + 2]);
         if (p->has_external_field)
-            eext += -FO_MU0 * p->ms * V * (mi[0] * p->h_ext[0] + mi[1] * p->h_ext[1] + mi[2] * p->h_ext[2]);
+            eext += -FO_MU0 * p->ms * V * ph * (mi[0] * p->h_ext[0] + mi[1] * p->h_ext[1] + mi[2] * p->h_ext[2]);
         if (pr->hmap)
             eext += -FO_MU0 * p->ms * V *
                     (mi[0] * pr->hmap[3 * i] + mi[1] * pr->hmap[3 * i + 1] + mi[2] * pr->hmap[3 * i + 2]);
         if (p->has_uniaxial) {
             const double mu = mi[0] * pr->u[0] + mi[1] * pr->u[1] + mi[2] * pr->u[2];
             const double s = mu * mu;
-            euni += -V * (kval(pr, 0, i, p->ku1) * s + kval(pr, 1, i, p->ku2) * s * s);
+            euni += -V * ph * (kval(pr, 0, i, p->ku1) * s + kval(pr, 1, i, p->ku2) * s * s);
         }
         if (p->has_cubic) {
             const double m1 = mi[0] * pr->c1[0] + mi[1] * pr->c1[1] + mi[2] * pr->c1[2];
@@ -1018,7 +1105,7 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
             const double m3 = mi[0] * pr->c3[0] + mi[1] * pr->c3[1] + mi[2] * pr->c3[2];
             const double s1 = m1 * m1, s2 = m2 * m2, s3 = m3 * m3;
             const double sig = s1 * s2 + s2 * s3 + s1 * s3;
-            ecub += V * (kval(pr, 2, i, p->kc1) * sig + kval(pr, 3, i, p->kc2) * s1 * s2 * s3 + kval(pr, 4, i, p->kc3) * sig * sig);
+            ecub += V * ph * (kval(pr, 2, i, p->kc1) * sig + kval(pr, 3, i, p->kc2) * s1 * s2 * s3 + kval(pr, 4, i, p->kc3) * sig * sig);
         }
         if (p->has_uniaxial || p->has_cubic) {
             double ha[3] = {0, 0, 0};

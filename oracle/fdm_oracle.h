@@ -93,6 +93,22 @@ typedef struct {
      * (crates/fullmag-engine/src/fdm_fields.rs:818-896, fdm_problem.rs:24-35,244-273) */
     double temperature;
     uint64_t thermal_seed;
+    /* boundary correction of the double-precision path (all copied at create):
+     * tier 0 none, 1 T0 face-link exchange (native/backends/fdm/src/exchange_t0_fp64.cu:27-164),
+     * 2 T1 boundary stencil (exchange_t1_fp64.cu:38-204); with a tier the demag input is
+     * phi Ms m (demag_fp64.cu:55-90) and the energies weight each cell by phi
+     * (reductions_fp64.cu:123-260); face and delta are +x -x +y -y +z -z */
+    int32_t boundary_tier, pad3;
+    double phi_floor, delta_min;
+    const double *volume_fraction;
+    const double *face[6];
+    const double *delta[6];
+    /* sparse demag correction H_d(t) -= sum_s dN(t, s) phi_s Ms m_s, tensor rows xx xy xz yy
+     * yz zz (demag_boundary_fp64.cu:23-76); phi_s = 1 without volume fractions */
+    const int32_t *corr_target_idx;
+    const int32_t *corr_source_idx;
+    const double *corr_tensor;
+    uint32_t corr_targets, corr_stencil;
 } fo_params;
 
 #define FO_MAX_REGIONS 256

@@ -62,6 +62,10 @@ class Params(C.Structure):
         ("oersted_freq", C.c_double), ("oersted_phase", C.c_double), ("oersted_offset", C.c_double),
         ("oersted_t_on", C.c_double), ("oersted_t_off", C.c_double),
         ("temperature", C.c_double), ("thermal_seed", C.c_uint64),
+        ("boundary_tier", C.c_int32), ("pad3", C.c_int32), ("phi_floor", C.c_double), ("delta_min", C.c_double),
+        ("volume_fraction", C.c_void_p), ("face", C.c_void_p * 6), ("delta", C.c_void_p * 6),
+        ("corr_target_idx", C.c_void_p), ("corr_source_idx", C.c_void_p), ("corr_tensor", C.c_void_p),
+        ("corr_targets", C.c_uint32), ("corr_stencil", C.c_uint32),
     ]
 
 
@@ -171,7 +175,7 @@ class Problem:
                  ku1_field=None, ku2_field=None, kc1_field=None, kc2_field=None, kc3_field=None,
                  oersted_current=None, oersted_radius=0.0, oersted_center=(0.0, 0.0, 0.0), oersted_kind=0,
                  oersted_freq=0.0, oersted_phase=0.0, oersted_offset=0.0, oersted_t_on=0.0, oersted_t_off=0.0,
-                 temperature=0.0, thermal_seed=42):
+                 temperature=0.0, thermal_seed=42, boundary=None):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -236,6 +240,32 @@ class Problem:
                 if self._lut.size != 256 * 256:
                     raise ValueError("exchange_lut needs 256 x 256 entries")
                 p.exchange_lut = self._lut.ctypes.data
+        self._bnd = []
+        if boundary is not None:
+            # boundary correction of the double-precision path: dict with tier (1 T0, 2 T1),
+            # volume_fraction, face (6 arrays) or delta (6 arrays), phi_floor, delta_min, and
+            # optionally corr = (target_idx, source_idx, tensor (targets x stencil x 6))
+            def keep(a, dt=np.float64):
+                a = np.ascontiguousarray(a, dtype=dt).reshape(-1)
+                self._bnd.append(a)
+                return a.ctypes.data
+            p.boundary_tier = int(boundary.get("tier", 0))
+            p.phi_floor = float(boundary.get("phi_floor", 0.0))
+            p.delta_min = float(boundary.get("delta_min", 0.0))
+            if boundary.get("volume_fraction") is not None:
+                p.volume_fraction = keep(boundary["volume_fraction"])
+            for q, a in enumerate(boundary.get("face") or []):
+                p.face[q] = keep(a)
+            for q, a in enumerate(boundary.get("delta") or []):
+                p.delta[q] = keep(a)
+            if boundary.get("corr") is not None:
+                t, src, ten = boundary["corr"]
+                t = np.asarray(t)
+                p.corr_target_idx = keep(t, np.int32)
+                p.corr_source_idx = keep(src, np.int32)
+                p.corr_tensor = keep(ten)
+                p.corr_targets = t.size
+                p.corr_stencil = np.asarray(src).size // max(t.size, 1)
         self.n = nx * ny * nz
         self.shape = (nz, ny, nx)
         self.params = p
