@@ -658,7 +658,7 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=4000)
     ap.add_argument("--sweep-count", type=int, default=384)
     ap.add_argument("--sweep-t-end", type=float, default=0.5e-9)
-    ap.add_argument("--sweep-sequential", type=int, default=8, help="problems solved one at a time for the baseline")
+    ap.add_argument("--sweep-sequential", type=int, default=32, help="problems solved one at a time for the baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the cuFFT + unfused baseline leg")
     ap.add_argument("--profile", action="store_true", help="timed steps only: no e2e leg, no CPU baseline")

@@ -362,10 +362,10 @@ class FdmBackend:
         return a.value, b.value, c.value
 
     def tuning(self) -> dict:
-        a = (C.c_uint32 * 6)()
+        a = (C.c_uint32 * 9)()
         self._check(self.lib.fullmag_fdm_backend_tuning(self.handle, a), "tuning")
         return {"rows_per_cta": a[0], "tx_y_forward": a[1], "tx_z": a[2], "tx_y_inverse": a[3], "tx_thin": a[4],
-                "z_pair": a[5]}
+                "z_pair": a[5], "split_y_forward": a[6], "split_z": a[7], "split_y_inverse": a[8]}
 
     def launch_count(self) -> int:
         c = C.c_uint64()

@@ -999,14 +999,18 @@ cudaError_t launch_y_fused(const ColPass &p, cudaStream_t s) {
     else y_forward_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
     return cudaGetLastError();
 }
+// Radix split N = N1 x N2 of the two-level passes: split 0 is the default, split 1 the
+// alternative the autotuner times against it (512 has one split: a 64-point outer pass
+// would not fit the registers).
 template <bool INV>
 cudaError_t launch_y_dispatch(const ColPass &p, cudaStream_t s) {
+    const bool alt = p.split != 0;
     switch (p.g.py) {
-        case 16: return launch_y_fused<4, 4, INV>(p, s);
-        case 32: return launch_y_fused<8, 4, INV>(p, s);
-        case 64: return launch_y_fused<8, 8, INV>(p, s);
-        case 128: return launch_y_fused<16, 8, INV>(p, s);
-        case 256: return launch_y_fused<16, 16, INV>(p, s);
+        case 16: return alt ? launch_y_fused<8, 2, INV>(p, s) : launch_y_fused<4, 4, INV>(p, s);
+        case 32: return alt ? launch_y_fused<4, 8, INV>(p, s) : launch_y_fused<8, 4, INV>(p, s);
+        case 64: return alt ? launch_y_fused<16, 4, INV>(p, s) : launch_y_fused<8, 8, INV>(p, s);
+        case 128: return alt ? launch_y_fused<32, 4, INV>(p, s) : launch_y_fused<16, 8, INV>(p, s);
+        case 256: return alt ? launch_y_fused<32, 8, INV>(p, s) : launch_y_fused<16, 16, INV>(p, s);
         default: return launch_y_fused<32, 16, INV>(p, s);
     }
 }
@@ -1080,12 +1084,13 @@ cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
         return p.g.pz == 64 ? launch_z_pair<8, 8>(p, s) : launch_z_pair<16, 8>(p, s);
     }
     if (z_fused_ok(p.g)) {
+        const bool alt = p.split != 0;  // radix split, as launch_y_dispatch
         switch (p.g.pz) {
-            case 16: return launch_z_fused<4, 4>(p, s);
-            case 32: return launch_z_fused<8, 4>(p, s);
-            case 64: return launch_z_fused<8, 8>(p, s);
-            case 128: return launch_z_fused<16, 8>(p, s);
-            case 256: return launch_z_fused<16, 16>(p, s);
+            case 16: return alt ? launch_z_fused<8, 2>(p, s) : launch_z_fused<4, 4>(p, s);
+            case 32: return alt ? launch_z_fused<4, 8>(p, s) : launch_z_fused<8, 4>(p, s);
+            case 64: return alt ? launch_z_fused<16, 4>(p, s) : launch_z_fused<8, 8>(p, s);
+            case 128: return alt ? launch_z_fused<32, 4>(p, s) : launch_z_fused<16, 8>(p, s);
+            case 256: return alt ? launch_z_fused<32, 8>(p, s) : launch_z_fused<16, 16>(p, s);
             default: return launch_z_fused<32, 16>(p, s);
         }
     }

@@ -616,6 +616,7 @@ struct Engine {
     // column fits in shared memory (use_yz)
     int tx_yf = 1, tx_z = 1, tx_yi = 1, tx_2d = 1;
     int z_pair = 0;  // 1: the z pass runs the packed ky-pair kernel (tile 8)
+    int split_yf = 0, split_z = 0, split_yi = 0;  // radix split of each two-level column pass
     bool use_yz = false;
     int row_blocks = 1;  // CTAs of the row pass at the current rows-per-CTA
 
@@ -659,18 +660,23 @@ struct Engine {
             return !cuda_fail("yz convolve", rc);
         }
         kt_begin(KT_YF);
-        rc = launch_y_forward(col_pass(plan_y, tx_yf, X, Y), stream);
+        ColPass yf = col_pass(plan_y, tx_yf, X, Y);
+        yf.split = split_yf;
+        rc = launch_y_forward(yf, stream);
         kt_end();
         if (cuda_fail("y forward", rc)) return false;
         kt_begin(KT_Z);
         ColPass zp = col_pass(plan_z, tx_z, Y, Y);
         zp.pipe = z_pair;
+        zp.split = split_z;
         rc = launch_z_convolve(zp, stream);
         kt_end();
         if (cuda_fail("z convolve", rc)) return false;
         launches += 3;
         kt_begin(KT_YI);
-        rc = launch_y_inverse(col_pass(plan_y, tx_yi, Y, X), stream);
+        ColPass yi = col_pass(plan_y, tx_yi, Y, X);
+        yi.split = split_yi;
+        rc = launch_y_inverse(yi, stream);
         kt_end();
         return !cuda_fail("y inverse", rc);
     }
@@ -2257,7 +2263,7 @@ struct TuneKey {
     }
 };
 struct TuneChoice {
-    int tx_yf, tx_z, tx_yi, tx_2d, rows, z_pair;
+    int tx_yf, tx_z, tx_yi, tx_2d, rows, z_pair, split_yf, split_z, split_yi;
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneChoice> g_tune_cache;
@@ -2269,6 +2275,25 @@ std::map<TuneKey, TuneChoice> g_tune_cache;
 // so batched problems of the same shape pay for the search once.
 bool Engine::autotune() {
     const TuneKey key{g.nx, g.ny, g.nz, g.px, g.py, g.pz, g.thin, has_mask ? 1 : 0};
+    // FULLMAG_FDM_TUNE="rows,tx_yf,tx_z,tx_yi,tx_2d,z_pair,split_yf,split_z,split_yi" fixes every
+    // choice (the values fullmag_fdm_backend_tuning reports), e.g. so that a profiler run uses
+    // the launch shapes of an unprofiled one
+    if (const char *fix = std::getenv("FULLMAG_FDM_TUNE")) {
+        int v[9];
+        if (std::sscanf(fix, "%d,%d,%d,%d,%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &v[7], &v[8]) == 9) {
+            row_rows = std::max(1, v[0]);
+            tx_yf = std::max(1, v[1]);
+            tx_z = std::max(1, v[2]);
+            tx_yi = std::max(1, v[3]);
+            tx_2d = std::max(1, v[4]);
+            z_pair = v[5] && z_convolve_pair_ok(g, tx_z) ? 1 : 0;
+            split_yf = v[6] != 0;
+            split_z = v[7] != 0;
+            split_yi = v[8] != 0;
+            row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
+            return true;
+        }
+    }
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
@@ -2278,6 +2303,9 @@ bool Engine::autotune() {
             tx_yi = it->second.tx_yi;
             tx_2d = it->second.tx_2d;
             z_pair = it->second.z_pair;
+            split_yf = it->second.split_yf;
+            split_z = it->second.split_z;
+            split_yi = it->second.split_yi;
             if (!std::getenv("FULLMAG_FDM_ROWS_PER_CTA")) row_rows = it->second.rows;
             row_blocks = (g.ny * g.nz + row_rows - 1) / row_rows;
             return true;
@@ -2309,24 +2337,36 @@ bool Engine::autotune() {
             }
             tx_z = best;
         } else {
-            // tile widths of the three column passes, each timed on its own
-            auto tune = [&](int cur_tx, const std::function<size_t(int)> &smem, const std::function<bool(int)> &run) {
-                int best = cur_tx;
+            // tile widths and radix splits of the three column passes, each timed on its own
+            // (power-of-two lengths 16..256 have a second split N1 x N2)
+            auto two_splits = [](int len) { return len >= 16 && len <= 256 && (len & (len - 1)) == 0; };
+            auto tune = [&](int cur_tx, int &split, bool alt, const std::function<size_t(int)> &smem,
+                            const std::function<bool(int, int)> &run) {
+                int best = cur_tx, best_split = 0;
                 float bt = 1e30f;
-                for (int tx : {1, 2, 4, 8, 16}) {
-                    if (tx > std::max(1, g.nkx) || smem(tx) > 200u * 1024u) continue;
-                    const float t = time_ms([&] { return run(tx); });
-                    if (t < bt) {
-                        bt = t;
-                        best = tx;
+                for (int sp = 0; sp < (alt ? 2 : 1); ++sp)
+                    for (int tx : {1, 2, 4, 8, 16}) {
+                        if (tx > std::max(1, g.nkx) || smem(tx) > 200u * 1024u) continue;
+                        const float t = time_ms([&] { return run(tx, sp); });
+                        if (t < bt) {
+                            bt = t;
+                            best = tx;
+                            best_split = sp;
+                        }
                     }
-                }
+                split = best_split;
                 return best;
             };
             auto ysm = [&](int tx) { return y_pass_smem(g, tx); };
-            tx_yf = tune(tx_yf, ysm, [&](int tx) { return launch_y_forward(col_pass(plan_y, tx, X, Y), stream) == cudaSuccess; });
-            tx_z = tune(tx_z, [&](int tx) { return z_convolve_smem(g, tx); },
-                        [&](int tx) { return launch_z_convolve(col_pass(plan_z, tx, Y, Y), stream) == cudaSuccess; });
+            auto cp = [&](const FftPlan &pl, int tx, int sp, const float2 *in, float2 *out) {
+                ColPass c = col_pass(pl, tx, in, out);
+                c.split = sp;
+                return c;
+            };
+            tx_yf = tune(tx_yf, split_yf, two_splits(g.py), ysm,
+                         [&](int tx, int sp) { return launch_y_forward(cp(plan_y, tx, sp, X, Y), stream) == cudaSuccess; });
+            tx_z = tune(tx_z, split_z, two_splits(g.pz), [&](int tx) { return z_convolve_smem(g, tx); },
+                        [&](int tx, int sp) { return launch_z_convolve(cp(plan_z, tx, sp, Y, Y), stream) == cudaSuccess; });
             // the packed ky-pair z pass (tile 8) against the best unpaired launch;
             // FULLMAG_FDM_Z_PAIR=0 or 1 forces the choice
             z_pair = 0;
@@ -2334,17 +2374,20 @@ bool Engine::autotune() {
             if (z_convolve_pair_ok(g, 8) && zp_env && zp_env[0] == '1') {
                 tx_z = 8;
                 z_pair = 1;
+                split_z = 0;
             } else if (z_convolve_pair_ok(g, 8) && !(zp_env && zp_env[0] == '0')) {
-                ColPass best = col_pass(plan_z, tx_z, Y, Y), paired = col_pass(plan_z, 8, Y, Y);
+                ColPass best = cp(plan_z, tx_z, split_z, Y, Y), paired = col_pass(plan_z, 8, Y, Y);
                 paired.pipe = 1;
                 const float t_best = time_ms([&] { return launch_z_convolve(best, stream) == cudaSuccess; });
                 const float t_pair = time_ms([&] { return launch_z_convolve(paired, stream) == cudaSuccess; });
                 if (t_pair < t_best) {
                     tx_z = 8;
                     z_pair = 1;
+                    split_z = 0;
                 }
             }
-            tx_yi = tune(tx_yi, ysm, [&](int tx) { return launch_y_inverse(col_pass(plan_y, tx, Y, X), stream) == cudaSuccess; });
+            tx_yi = tune(tx_yi, split_yi, two_splits(g.py), ysm,
+                         [&](int tx, int sp) { return launch_y_inverse(cp(plan_y, tx, sp, Y, X), stream) == cudaSuccess; });
         }
     }
     if (!std::getenv("FULLMAG_FDM_ROWS_PER_CTA")) {
@@ -2380,7 +2423,7 @@ bool Engine::autotune() {
     // those is rewritten before it is read again
     if (cuda_fail("autotune sync", cudaStreamSynchronize(stream))) return false;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune_cache[key] = TuneChoice{tx_yf, tx_z, tx_yi, tx_2d, row_rows, z_pair};
+    g_tune_cache[key] = TuneChoice{tx_yf, tx_z, tx_yi, tx_2d, row_rows, z_pair, split_yf, split_z, split_yi};
     return true;
 }
 
@@ -2970,15 +3013,18 @@ int fullmag_fdm_backend_kernel_times(fullmag_fdm_backend *handle, double *total_
     return FULLMAG_FDM_OK;
 }
 
-int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out6) {
+int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out9) {
     Engine *e = eng(handle);
-    if (!e || !out6) return FULLMAG_FDM_ERR_INVALID;
-    out6[0] = (uint32_t)e->row_rows;
-    out6[1] = (uint32_t)e->tx_yf;
-    out6[2] = (uint32_t)e->tx_z;
-    out6[3] = (uint32_t)e->tx_yi;
-    out6[4] = (uint32_t)e->tx_2d;
-    out6[5] = (uint32_t)e->z_pair;
+    if (!e || !out9) return FULLMAG_FDM_ERR_INVALID;
+    out9[0] = (uint32_t)e->row_rows;
+    out9[1] = (uint32_t)e->tx_yf;
+    out9[2] = (uint32_t)e->tx_z;
+    out9[3] = (uint32_t)e->tx_yi;
+    out9[4] = (uint32_t)e->tx_2d;
+    out9[5] = (uint32_t)e->z_pair;
+    out9[6] = (uint32_t)e->split_yf;
+    out9[7] = (uint32_t)e->split_z;
+    out9[8] = (uint32_t)e->split_yi;
     return FULLMAG_FDM_OK;
 }
 

@@ -133,6 +133,7 @@ struct ColPass {
     int inverse;
     const double *skip_dt;   // batched rounds: the problem's step size; <= 0 skips its tiles
     int pipe;                // z pass: 1 = the packed ky-pair kernel (tile 8)
+    int split;               // two-level passes: 0 the default radix split N1 x N2, 1 the alternative
 };
 
 // Launchers (kernels.cu)

@@ -366,9 +366,10 @@ int fullmag_fdm_backend_stream(fullmag_fdm_backend *handle, void **out_stream);
 
 /* Launch shapes the autotuner chose at create: rows per CTA of the fused row pass,
  * then the kx tile widths of the y-forward, z-convolution, y-inverse and thin-film
- * passes (out6[0..4]), and 1 in out6[5] when the z convolution runs on y-frequency
- * pairs in packed FP32x2 arithmetic. */
-int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out6);
+ * passes (out9[0..4]), 1 in out9[5] when the z convolution runs on y-frequency pairs
+ * in packed FP32x2 arithmetic, and the radix split (0 default, 1 alternative) of the
+ * y-forward, z and y-inverse passes (out9[6..8]). */
+int fullmag_fdm_backend_tuning(fullmag_fdm_backend *handle, uint32_t *out9);
 
 /* Number of kernels this handle has launched so far (instrumentation). */
 int fullmag_fdm_backend_launch_count(fullmag_fdm_backend *handle, uint64_t *out_count);

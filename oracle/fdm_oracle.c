@@ -217,18 +217,31 @@ int fo_newell_kernels(int nx, int ny, int nz, double dx, double dy, double dz, d
 /* Mixed-radix FFT (own implementation; stands in for rustfft 6.4.1)          */
 /* ------------------------------------------------------------------------- */
 
-typedef struct {
+typedef struct fft_plan {
     int n;
     int nf;
     int f[64];
     int maxp;
     double *w; /* w[2e], w[2e+1] = cos, -sin of 2*pi*e/n */
+    /* lengths with a prime factor above 61: Bluestein's chirp-z algorithm (Bluestein 1970)
+     * through a power-of-two transform of length M >= 2n - 1, the way rustfft handles such
+     * lengths: X_k = c_k sum_j (x_j c_j) conj(c_{k-j}), c_j = e^{-i pi j^2 / n} */
+    int blue, M;
+    struct fft_plan *sub;
+    double *chirp; /* c_j, j < n */
+    double *bhat;  /* FFT_M of conj(c_j) wrapped to j in (-n, n) */
 } fft_plan;
+
+static void fft_rec(const struct fft_plan *P, const double *in, long is, double *out, int n, int fi, int inv, double *tmp);
 
 static int plan_init(fft_plan *P, int n) {
     P->n = n;
     P->nf = 0;
     P->maxp = 4;
+    P->blue = 0;
+    P->M = 0;
+    P->sub = NULL;
+    P->chirp = P->bhat = NULL;
     int m = n;
     while (m % 4 == 0) { P->f[P->nf++] = 4; m /= 4; }
     while (m % 2 == 0) { P->f[P->nf++] = 2; m /= 2; }
@@ -244,12 +257,85 @@ static int plan_init(fft_plan *P, int n) {
         P->w[2 * e] = cos(ang);
         P->w[2 * e + 1] = -sin(ang);
     }
+    if (P->maxp > 61) {
+        P->blue = 1;
+        int M = 1;
+        while (M < 2 * n - 1) M <<= 1;
+        P->M = M;
+        P->sub = (fft_plan *)calloc(1, sizeof(fft_plan));
+        P->chirp = (double *)malloc(sizeof(double) * 2 * (size_t)n);
+        P->bhat = (double *)calloc(2 * (size_t)M, sizeof(double));
+        double *tmp = (double *)malloc(sizeof(double) * 2 * (size_t)M);
+        double *ftmp = (double *)malloc(sizeof(double) * 8);
+        if (!P->sub || !P->chirp || !P->bhat || !tmp || !ftmp || plan_init(P->sub, M)) {
+            free(tmp);
+            free(ftmp);
+            return -1;
+        }
+        for (long j = 0; j < n; ++j) {
+            /* j^2 mod 2n keeps the angle exact */
+            const long q = (j * j) % (2L * n);
+            const double ang = M_PI * (double)q / (double)n;
+            P->chirp[2 * j] = cos(ang);
+            P->chirp[2 * j + 1] = -sin(ang);
+        }
+        for (long j = 0; j < n; ++j) {
+            const double br = P->chirp[2 * j], bi = -P->chirp[2 * j + 1];
+            P->bhat[2 * j] = br;
+            P->bhat[2 * j + 1] = bi;
+            if (j > 0) {
+                P->bhat[2 * (M - j)] = br;
+                P->bhat[2 * (M - j) + 1] = bi;
+            }
+        }
+        memcpy(tmp, P->bhat, sizeof(double) * 2 * (size_t)M);
+        fft_rec(P->sub, tmp, 1, P->bhat, M, 0, 0, ftmp);
+        free(tmp);
+        free(ftmp);
+    }
     return 0;
 }
 
 static void plan_free(fft_plan *P) {
     free(P->w);
     P->w = NULL;
+    if (P->sub) {
+        plan_free(P->sub);
+        free(P->sub);
+        P->sub = NULL;
+    }
+    free(P->chirp);
+    free(P->bhat);
+    P->chirp = P->bhat = NULL;
+}
+
+/* Bluestein transform of x (length n, contiguous) into out; the inverse (unnormalised,
+ * conjugate kernel) as conj(forward(conj x)).  work holds 4 M doubles. */
+static void fft_blue(const fft_plan *P, const double *x, double *out, int inv, double *work, double *tmp) {
+    const int n = P->n, M = P->M;
+    const double sg = inv ? -1.0 : 1.0;
+    double *a = work, *A = work + 2 * (size_t)M;
+    memset(a, 0, sizeof(double) * 2 * (size_t)M);
+    for (int j = 0; j < n; ++j) {
+        const double xr = x[2 * j], xi = sg * x[2 * j + 1];
+        const double cr = P->chirp[2 * j], ci = P->chirp[2 * j + 1];
+        a[2 * j] = xr * cr - xi * ci;
+        a[2 * j + 1] = xr * ci + xi * cr;
+    }
+    fft_rec(P->sub, a, 1, A, M, 0, 0, tmp);
+    for (int k = 0; k < M; ++k) {
+        const double ar = A[2 * k], ai = A[2 * k + 1], br = P->bhat[2 * k], bi = P->bhat[2 * k + 1];
+        A[2 * k] = ar * br - ai * bi;
+        A[2 * k + 1] = ar * bi + ai * br;
+    }
+    fft_rec(P->sub, A, 1, a, M, 0, 1, tmp);
+    const double inv_m = 1.0 / (double)M;
+    for (int k = 0; k < n; ++k) {
+        const double vr = a[2 * k] * inv_m, vi = a[2 * k + 1] * inv_m;
+        const double cr = P->chirp[2 * k], ci = P->chirp[2 * k + 1];
+        out[2 * k] = vr * cr - vi * ci;
+        out[2 * k + 1] = sg * (vr * ci + vi * cr);
+    }
 }
 
 /* Decimation in time: X[k + q m] = sum_r W_p^{rq} W_n^{rk} DFT_m(x[r::p])[k]. */
@@ -320,7 +406,8 @@ static void fft_line(const fft_plan *P, double *base, long stride, int inv, doub
         lin[2 * i] = base[2 * i * stride];
         lin[2 * i + 1] = base[2 * i * stride + 1];
     }
-    fft_rec(P, lin, 1, lout, n, 0, inv, tmp);
+    if (P->blue) fft_blue(P, lin, lout, inv, tmp + 8, tmp);
+    else fft_rec(P, lin, 1, lout, n, 0, inv, tmp);
     for (int i = 0; i < n; ++i) {
         base[2 * i * stride] = lout[2 * i];
         base[2 * i * stride + 1] = lout[2 * i + 1];
@@ -331,7 +418,7 @@ int fo_fft1d(double *data, int n, int inverse) {
     if (n <= 0) return -1;
     fft_plan P;
     if (plan_init(&P, n)) return -2;
-    double *buf = (double *)malloc(sizeof(double) * (4 * (size_t)n + 2 * (size_t)P.maxp));
+    double *buf = (double *)malloc(sizeof(double) * (4 * (size_t)n + 2 * (size_t)P.maxp + 8 + 4 * (size_t)P.M));
     if (!buf) { plan_free(&P); return -2; }
     fft_line(&P, data, 1, inverse, buf, buf + 2 * n, buf + 4 * n);
     free(buf);
@@ -347,6 +434,9 @@ int fo_fft3d(double *data, int px, int py, int pz, int inverse) {
     if (pz > maxn) maxn = pz;
     int maxp = Px.maxp > Py.maxp ? Px.maxp : Py.maxp;
     if (Pz.maxp > maxp) maxp = Pz.maxp;
+    int maxm = Px.M > Py.M ? Px.M : Py.M;
+    if (Pz.M > maxm) maxm = Pz.M;
+    maxp += 4 + 2 * maxm; /* the tmp area also holds Bluestein's work arrays */
     const long sxy = (long)px * py;
 #pragma omp parallel
     {

@@ -1,0 +1,65 @@
+"""The batched sweep against the FP64 oracle on a seeded subsample of the 384-film sweep
+workload (nx 16..256, ny 16..128, nz 1/2/4, 4 nm cells, Ms, A, alpha, B drawn from seed 1;
+Dormand-Prince with max error 1e-5).  Sixteen films are drawn with a fixed seed among
+the films of at most 6000 cells and advanced to 50 ps, each film's oracle run in its own
+process: the single-threaded FP64 oracle needs about 4 minutes per film for the full
+0.5 ns, which no test can afford for sixteen.  Each side runs its own step controller
+(the FP32 error norm picks slightly different steps), so the film-averaged <m> is
+compared with an absolute tolerance of 2e-4 per component."""
+import multiprocessing as mp
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from fullmag_gb300 import FdmBatch
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+T_END, DT0 = 50e-12, 1e-13
+
+
+def _subsample():
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    import bench
+    plans = bench.sweep_plans(384)
+    cells = np.array([p["nx"] * p["ny"] * p["nz"] for p in plans])
+    pool = np.nonzero(cells <= 6000)[0]
+    pick = np.sort(np.random.default_rng(7).choice(pool, 16, replace=False))
+    return [plans[i] for i in pick]
+
+
+def _oracle_mean_m(kw):
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle as O
+    O.set_threads(1)
+    kw = dict(kw)
+    kw.pop("integrator")
+    me = kw.pop("adaptive_max_error")
+    pr = O.Problem(**kw, integrator=O.DP45, max_error=me)
+    t, dt = 0.0, DT0
+    while t < T_END * (1 - 1e-12):
+        st = pr.step(min(dt, T_END - t))
+        t, dt = st["time"], st["suggested_next_dt"]
+    m = pr.get_m().mean(axis=0)
+    pr.close()
+    return m
+
+
+def test_batched_sweep_subsample_vs_oracle(gpu_lib):
+    plans = _subsample()
+    ctx = mp.get_context("spawn")  # the oracle processes never touch the GPU
+    with ctx.Pool(min(len(plans), max(1, mp.cpu_count()))) as pool:
+        pending = pool.map_async(_oracle_mean_m, plans)
+        batch = FdmBatch(plans)
+        steps, _ = batch.step_until(T_END, DT0)
+        got = np.array([batch.copy_field(i).mean(axis=0) for i in range(len(plans))])
+        batch.close()
+        want = np.array(pending.get(timeout=1800))
+    assert np.all(steps > 0)
+    err = np.abs(got - want).max(axis=1)
+    print("max |<m>_gpu - <m>_oracle| per film:", err)
+    assert err.max() < 2e-4, err

@@ -6,7 +6,7 @@ import pytest
 from helpers import random_unit
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7, 8, 12, 16, 17, 34, 64, 100, 128, 251, 502, 1024])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7, 8, 12, 16, 17, 34, 64, 100, 128, 251, 274, 502, 1024])
 def test_fft1d_matches_numpy(oracle, n):
     rng = np.random.default_rng(n)
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
