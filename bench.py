@@ -77,22 +77,23 @@ def kernel_bytes_per_launch(kind, nx, ny, nz, padded):
 
 
 def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
-    """Average algorithmic bytes of one row-pass launch over a fixed step.  Per cell:
-    state / stage vectors 12 B each, the X half spectrum S = 24 (nx + 1) / nx B (read
-    before and written after each evaluation).  RK4 passes: (1) m0 + k1 -> y1, forward x:
-    36 + S; (2), (3) inverse x, y_s, m0 -> k_s, y_{s+1}, forward x: 48 + 2S; (4) inverse x,
-    y3, m0, k1..k3 -> m', forward x: 72 + 2S; (5) inverse x, m' -> k1 (+ statistics):
-    24 + S.  Heun: 36 + S, 60 + 2S, 24 + S."""
+    """Average algorithmic bytes of one row-pass launch over a fixed step at a repeated
+    dt.  Per cell: state / stage vectors 12 B each, the X half spectrum S = 24 (nx + 1) / nx
+    B (read before and written after each evaluation).  RK4 passes: (2), (3) inverse x,
+    y_s, m0 -> k_s, y_{s+1}, forward x: 48 + 2S; (4) inverse x, y3, m0, k1..k3 -> m',
+    forward x: 72 + 2S; (5) inverse x, m' -> k1' (+ statistics), the next step's first
+    stage input N(m' + dt/2 k1'), forward x: 36 + 2S (the first pass of the next step is
+    folded into it).  Heun: 60 + 2S, 36 + 2S."""
     n = nx * ny * nz
     S = 24.0 * (nx + 1) / nx if demag else 0.0
     if integrator == "rk4":
-        per_cell = [36 + S, 48 + 2 * S, 48 + 2 * S, 72 + 2 * S, 24 + S]
+        per_cell = [48 + 2 * S, 48 + 2 * S, 72 + 2 * S, 36 + 2 * S]
     elif integrator == "dp45":
         # first pass m0 + k1 -> y2; stages s = 1..5 read y_s, m0 and s earlier k's, write
         # k_s and y_{s+1}; the last pass writes k7 and reads the 7 k's of the error norm
         per_cell = [36 + S] + [48 + 12 * s + 2 * S for s in range(1, 6)] + [108 + S]
     else:
-        per_cell = [36 + S, 60 + 2 * S, 24 + S]
+        per_cell = [60 + 2 * S, 36 + 2 * S]
     return sum(per_cell) / len(per_cell) * n
 
 

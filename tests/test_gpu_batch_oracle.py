@@ -5,7 +5,11 @@ the films of at most 6000 cells and advanced to 50 ps, each film's oracle run in
 process: the single-threaded FP64 oracle needs about 4 minutes per film for the full
 0.5 ns, which no test can afford for sixteen.  Each side runs its own step controller
 (the FP32 error norm picks slightly different steps), so the film-averaged <m> is
-compared with an absolute tolerance of 2e-4 per component."""
+compared with an absolute tolerance of 2e-4 per component plus ten times the film's own
+sensitivity: some films relax from their random initial state through a bifurcation
+(which domain pattern forms), and there <m> moves by 1e-2 when the initial state moves
+by FP32 rounding.  The sensitivity is measured on the oracle itself: the same film from
+m0 perturbed by 3e-7 (a few FP32 ulps) per component, renormalised."""
 import multiprocessing as mp
 import sys
 from pathlib import Path
@@ -32,11 +36,15 @@ def _subsample():
     return [plans[i] for i in pick]
 
 
-def _oracle_mean_m(kw):
+def _oracle_mean_m(args):
+    kw, eps = args
     sys.path.insert(0, str(ROOT))
     from oracle import oracle as O
     O.set_threads(1)
     kw = dict(kw)
+    if eps:
+        m0 = kw["m0"] + eps * np.random.default_rng(99).standard_normal(kw["m0"].shape)
+        kw["m0"] = m0 / np.linalg.norm(m0, axis=1, keepdims=True)
     kw.pop("integrator")
     me = kw.pop("adaptive_max_error")
     pr = O.Problem(**kw, integrator=O.DP45, max_error=me)
@@ -53,13 +61,18 @@ def test_batched_sweep_subsample_vs_oracle(gpu_lib):
     plans = _subsample()
     ctx = mp.get_context("spawn")  # the oracle processes never touch the GPU
     with ctx.Pool(min(len(plans), max(1, mp.cpu_count()))) as pool:
-        pending = pool.map_async(_oracle_mean_m, plans)
+        pending = pool.map_async(_oracle_mean_m, [(p, 0.0) for p in plans] + [(p, 3e-7) for p in plans])
         batch = FdmBatch(plans)
         steps, _ = batch.step_until(T_END, DT0)
         got = np.array([batch.copy_field(i).mean(axis=0) for i in range(len(plans))])
         batch.close()
-        want = np.array(pending.get(timeout=1800))
+        res = np.array(pending.get(timeout=1800))
+    want, perturbed = res[:len(plans)], res[len(plans):]
     assert np.all(steps > 0)
     err = np.abs(got - want).max(axis=1)
+    sens = np.abs(perturbed - want).max(axis=1)
     print("max |<m>_gpu - <m>_oracle| per film:", err)
-    assert err.max() < 2e-4, err
+    print("oracle sensitivity to a 3e-7 change of m0:", sens)
+    assert np.all(err < 2e-4 + 10.0 * sens), (err, sens)
+    # most films are not near a bifurcation: there the FP32 batch is as close as 2e-4
+    assert np.sum(err < 2e-4) >= 12, err
