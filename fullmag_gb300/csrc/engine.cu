@@ -129,6 +129,55 @@ __global__ void batch_commit_all_kernel(const CommitDesc *__restrict__ cd, const
     }
 }
 
+// Step control of one batched problem, kept on the device: after every round the control
+// kernel applies the C ABI's accept/reject rule (native/backends/fdm/src/llg_dp45_fp32.cu:
+// 286-341, as finish_dp45_attempt does on the host for single problems), advances the
+// problem's time and picks the next attempt's size, so a graph can chain many rounds
+// without the host in between.
+struct BatchState {
+    double time, t_end, next_dt;
+    double max_error, dt_min, dt_max, headroom, ctrl_exp;
+    double acc_stats[kNumStats];  // statistics of the last accepted step
+    double dt_used, suggested;
+    unsigned long long steps;     // steps accepted since the host last read the state
+    int done, pad;
+};
+
+__global__ void batch_control_kernel(BatchCtl *__restrict__ ctl, BatchState *__restrict__ st,
+                                     const double *__restrict__ stats, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    BatchState &s = st[k];
+    BatchCtl &c = ctl[k];
+    if (s.done) {  // any commit it still had ran at the start of this round
+        c.accept_prev = 0;
+        c.dt = 0.0;
+        return;
+    }
+    const double dt = c.dt;
+    const double err = sqrt(stats[(size_t)k * kNumStats + 8]);
+    double nd;
+    if (err <= s.max_error || dt <= s.dt_min) {
+        nd = err > 0.0 ? fmin(fmax(s.headroom * dt * pow(s.max_error / err, s.ctrl_exp), s.dt_min), s.dt_max) : s.dt_max;
+        s.time += dt;
+        s.steps += 1;
+        for (int q = 0; q < kNumStats; ++q) s.acc_stats[q] = stats[(size_t)k * kNumStats + q];
+        s.dt_used = dt;
+        s.suggested = nd;
+        c.accept_prev = 1;
+    } else {
+        nd = fmin(fmax(s.headroom * dt * pow(s.max_error / err, s.ctrl_exp), s.dt_min), s.dt_max);
+        c.accept_prev = 0;
+    }
+    s.next_dt = nd;
+    if (s.time >= s.t_end * (1.0 - 1e-12)) {
+        s.done = 1;
+        c.dt = 0.0;
+    } else {
+        c.dt = fmin(nd, s.t_end - s.time);
+    }
+}
+
 __global__ void soa_to_aos_kernel(const float *__restrict__ in, double *__restrict__ out_d, float *__restrict__ out_f,
                                   long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -1498,40 +1547,20 @@ struct Engine {
         return rc == 0 && rows.size() == 7 && (cols.size() == 6 || (!demag && cols.empty()));
     }
 
-    // Host side of a finished batched attempt (statistics st, control block ctl);
-    // returns 1 accepted, 0 rejected.
-    int batch_decide(const double *st, BatchCtl *ctl, double &next_dt) {
-        const double dt = ctl->dt;
-        const double err = sqrt(st[8]);
-        if (err <= max_error || dt <= dt_min) {
-            double dt_next = dt_max;
-            if (err > 0.0) dt_next = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
-            memcpy(stat_raw, st, sizeof(double) * kNumStats);  // batched rounds carry no extra-field sums
-            step_count += 1;
-            time += dt;
-            stats_valid = true;
-            fields_valid = false;
-            fill_stats(stat_raw, cur_stats);
-            cur_stats.step = step_count;
-            cur_stats.time_seconds = time;
-            cur_stats.dt_seconds = dt;
-            cur_stats.suggested_next_dt = dt_next;
-            ctl->accept_prev = 1;
-            next_dt = dt_next;
-            return 1;
-        }
-        ctl->accept_prev = 0;
-        next_dt = std::min(std::max(headroom * dt * pow(max_error / err, ctrl_exp()), dt_min), dt_max);
-        return 0;
-    }
-
-    // Applies a pending commit outside the round graph.
-    bool batch_flush(BatchCtl *ctl, cudaStream_t s) {
-        if (!ctl->accept_prev) return true;
-        ctl->accept_prev = 0;
-        const size_t b = sizeof(float) * 3 * (size_t)g.n;
-        return !cuda_fail("commit copy", cudaMemcpyAsync(S[0], S[1], b, cudaMemcpyDeviceToDevice, s)) &&
-               !cuda_fail("commit copy", cudaMemcpyAsync(K[0], K[fsal_index()], b, cudaMemcpyDeviceToDevice, s));
+    // Takes over the device step control of the batched rounds: the accepted steps since the
+    // last hand-over, the time they reached and the statistics of the last one.
+    void batch_apply(const BatchState &st) {
+        time = st.time;
+        if (st.steps == 0) return;
+        step_count += st.steps;
+        memcpy(stat_raw, st.acc_stats, sizeof(double) * kNumStats);  // batched rounds carry no extra-field sums
+        stats_valid = true;
+        fields_valid = false;
+        fill_stats(stat_raw, cur_stats);
+        cur_stats.step = step_count;
+        cur_stats.time_seconds = time;
+        cur_stats.dt_seconds = st.dt_used;
+        cur_stats.suggested_next_dt = st.suggested;
     }
 
     int step_dp45(double dt) {
@@ -3064,8 +3093,13 @@ struct BatchRound {
     BatchCtl *d_ctl = nullptr;
     double *h_stats = nullptr;  // pinned [n * kNumStats]
     double *d_stats = nullptr;
+    BatchState *h_state = nullptr;  // pinned [n]
+    BatchState *d_state = nullptr;
+    const CommitDesc *d_com = nullptr;  // inside d_blob
+    long long max_n3 = 0;
     void *d_blob = nullptr;     // descriptors and work tables
     cudaGraphExec_t exec = nullptr;
+    static constexpr int kRounds = 16;  // rounds per graph launch
 
     void release() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -3080,6 +3114,10 @@ struct BatchRound {
         d_stats = nullptr;
         if (d_blob) cudaFree(d_blob);
         d_blob = nullptr;
+        if (h_state) cudaFreeHost(h_state);
+        h_state = nullptr;
+        if (d_state) cudaFree(d_state);
+        d_state = nullptr;
     }
 };
 
@@ -3135,21 +3173,46 @@ struct FdmBatch {
     }
 
     // Builds (and captures) the round for `act`; false when a member cannot run batched.
-    bool build_round(const std::vector<size_t> &act, std::string &err) {
-        // commits still pending in the old round's control blocks run before it goes away
-        for (size_t k = 0; k < round.members.size(); ++k)
-            if (round.h_ctl && !items[round.members[k]]->batch_flush(&round.h_ctl[k], bstream)) {
-                err = "commit failed";
-                return false;
-            }
+    // Runs the commits still pending in the round's control blocks (device side) and
+    // hands every member's device step control back to its engine: time, accepted steps,
+    // statistics of the last accepted step, next step size.
+    bool sync_states(std::string &err) {
+        if (!round.exec) return true;
+        const int n = (int)round.members.size();
+        const unsigned gx = (unsigned)std::min<long long>((round.max_n3 + 255) / 256, 64);
+        batch_commit_all_kernel<<<dim3(gx, n), 256, 0, bstream>>>(round.d_com, round.d_ctl);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(round.h_state, round.d_state, sizeof(BatchState) * n, cudaMemcpyDeviceToHost, bstream) != cudaSuccess ||
+            cudaMemsetAsync(round.d_ctl, 0, sizeof(BatchCtl) * n, bstream) != cudaSuccess ||
+            cudaStreamSynchronize(bstream) != cudaSuccess) {
+            err = "batch commit failed";
+            return false;
+        }
+        for (int k = 0; k < n; ++k) {
+            const size_t i = round.members[k];
+            BatchState &st = round.h_state[k];
+            items[i]->batch_apply(st);
+            next_dt[i] = st.next_dt;
+            st.steps = 0;
+        }
+        return cudaMemcpyAsync(round.d_state, round.h_state, sizeof(BatchState) * n, cudaMemcpyHostToDevice, bstream) ==
+                   cudaSuccess &&
+               cudaStreamSynchronize(bstream) == cudaSuccess;
+    }
+
+    bool build_round(const std::vector<size_t> &act, double t_end, std::string &err) {
+        // the old round's pending commits and step control go back to the engines first
+        if (!sync_states(err)) return false;
         if (bstream) cudaStreamSynchronize(bstream);
         round.release();
         const int n = (int)act.size();
         round.members = act;
         if (cudaMallocHost((void **)&round.h_ctl, sizeof(BatchCtl) * n) != cudaSuccess ||
             cudaMallocHost((void **)&round.h_stats, sizeof(double) * kNumStats * n) != cudaSuccess ||
+            cudaMallocHost((void **)&round.h_state, sizeof(BatchState) * n) != cudaSuccess ||
             cudaMalloc((void **)&round.d_ctl, sizeof(BatchCtl) * n) != cudaSuccess ||
-            cudaMalloc((void **)&round.d_stats, sizeof(double) * kNumStats * n) != cudaSuccess) {
+            cudaMalloc((void **)&round.d_stats, sizeof(double) * kNumStats * n) != cudaSuccess ||
+            cudaMalloc((void **)&round.d_state, sizeof(BatchState) * n) != cudaSuccess) {
             err = "batch round allocation failed";
             return false;
         }
@@ -3170,7 +3233,18 @@ struct FdmBatch {
         std::vector<int> kinds;
         for (int k = 0; k < n; ++k) {
             Engine *e = items[act[k]];
-            round.h_ctl[k] = BatchCtl{0.0, 0, 0};
+            BatchState &st = round.h_state[k];
+            memset(&st, 0, sizeof(st));
+            st.time = e->time;
+            st.t_end = t_end;
+            st.next_dt = next_dt[act[k]];
+            st.max_error = e->max_error;
+            st.dt_min = e->dt_min;
+            st.dt_max = e->dt_max;
+            st.headroom = e->headroom;
+            st.ctrl_exp = e->ctrl_exp();
+            st.done = e->time >= t_end * (1.0 - 1e-12);
+            round.h_ctl[k] = BatchCtl{st.done ? 0.0 : std::min(st.next_dt, t_end - e->time), 0, 0};
             if (!e->record_attempt(&round.d_ctl[k].dt, rec, kinds)) {
                 err = "problem " + std::to_string(act[k]) + ": " + (e->last_error.empty() ? "not batchable" : e->last_error);
                 return false;
@@ -3223,10 +3297,13 @@ struct FdmBatch {
         for (int k = 0; k < NK * NC; ++k) memcpy(hb.data() + o_cw[k], col_work[k].data(), sizeof(int2) * col_work[k].size());
         memcpy(hb.data() + o_fin, fin.data(), sizeof(FinDesc) * n);
         memcpy(hb.data() + o_com, com.data(), sizeof(CommitDesc) * n);
-        if (cudaMemcpy(blob, hb.data(), off, cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (cudaMemcpy(blob, hb.data(), off, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(round.d_ctl, round.h_ctl, sizeof(BatchCtl) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(round.d_state, round.h_state, sizeof(BatchState) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
             err = "batch descriptor upload failed";
             return false;
         }
+        round.d_com = (const CommitDesc *)(blob + o_com);
         // capture the round
         long long max_n3 = 0;
         for (auto &c : com) max_n3 = std::max(max_n3, c.n3);
@@ -3252,27 +3329,35 @@ struct FdmBatch {
             err = "batch capture failed";
             return false;
         }
-        bool ok = cudaMemcpyAsync(round.d_ctl, round.h_ctl, sizeof(BatchCtl) * n, cudaMemcpyHostToDevice, bstream) == cudaSuccess;
-        if (ok) {
+        // kRounds rounds, each: the previous round's commits, the seven passes of an attempt
+        // for every member, the statistics, and the device step control; then the control
+        // state goes to the host once
+        bool ok = true;
+        round.max_n3 = max_n3;
+        for (int r = 0; r < BatchRound::kRounds && ok; ++r) {
             const unsigned gx = (unsigned)std::min<long long>((max_n3 + 255) / 256, 64);
             batch_commit_all_kernel<<<dim3(gx, n), 256, 0, bstream>>>((const CommitDesc *)(blob + o_com), round.d_ctl);
             ok = cudaGetLastError() == cudaSuccess;
-        }
-        for (int s = 0; s < 7 && ok; ++s) {
-            ok = fan_out(row_ids, [&](int rb, cudaStream_t st) {
-                return launch_row_pass_batched((const RowPass *)(blob + o_rows[s]), (const int2 *)(blob + o_rw[rb]),
-                                               (int)row_work[rb].size(), row_smem[rb], st);
-            });
-            if (ok && s < 6)
-                ok = fan_out(col_ids, [&](int cg, cudaStream_t st) {
-                    return launch_col_batched((const ColPass *)(blob + o_cols[cg]), (const int2 *)(blob + o_cw[cg]),
-                                              (int)col_work[cg].size(), cg / NC, col_smem[cg], st);
+            for (int s = 0; s < 7 && ok; ++s) {
+                ok = fan_out(row_ids, [&](int rb, cudaStream_t st) {
+                    return launch_row_pass_batched((const RowPass *)(blob + o_rows[s]), (const int2 *)(blob + o_rw[rb]),
+                                                   (int)row_work[rb].size(), row_smem[rb], st);
                 });
+                if (ok && s < 6)
+                    ok = fan_out(col_ids, [&](int cg, cudaStream_t st) {
+                        return launch_col_batched((const ColPass *)(blob + o_cols[cg]), (const int2 *)(blob + o_cw[cg]),
+                                                  (int)col_work[cg].size(), cg / NC, col_smem[cg], st);
+                    });
+            }
+            if (ok) ok = launch_finalize_batched((const FinDesc *)(blob + o_fin), n, round.d_stats, bstream) == cudaSuccess;
+            if (ok) {
+                batch_control_kernel<<<(n + 127) / 128, 128, 0, bstream>>>(round.d_ctl, round.d_state, round.d_stats, n);
+                ok = cudaGetLastError() == cudaSuccess;
+            }
         }
-        if (ok) ok = launch_finalize_batched((const FinDesc *)(blob + o_fin), n, round.d_stats, bstream) == cudaSuccess;
         if (ok)
-            ok = cudaMemcpyAsync(round.h_stats, round.d_stats, sizeof(double) * kNumStats * n, cudaMemcpyDeviceToHost,
-                                 bstream) == cudaSuccess;
+            ok = cudaMemcpyAsync(round.h_state, round.d_state, sizeof(BatchState) * n, cudaMemcpyDeviceToHost, bstream) ==
+                 cudaSuccess;
         const cudaError_t ce = cudaStreamEndCapture(bstream, &graph);
         if (!ok || ce != cudaSuccess || !graph) {
             if (graph) cudaGraphDestroy(graph);
@@ -3330,6 +3415,11 @@ uint32_t fullmag_fdm_batch_size(fullmag_fdm_batch *batch) {
 // t_end stay in the round's work tables with step size 0, which makes their row and
 // column CTAs return at once, until the round is rebuilt without them (when a tenth
 // of its members have finished).  Returns 1 when not batchable.
+// Batched DP45 rounds: each graph launch runs BatchRound::kRounds rounds with the step
+// control on the device (batch_control_kernel); the host reads the control state once per
+// launch to see which problems reached t_end, and rebuilds the round for the remaining
+// ones when fewer than 90 % of its members are still running.  Time to solution is taken
+// at the end of the launch in which a problem finished.
 static int batch_step_until_batched(FdmBatch *b, double t_end, double dt0, uint64_t *out_steps, uint64_t *out_wall_ns) {
     const size_t n = b->items.size();
     const auto t0 = std::chrono::steady_clock::now();
@@ -3340,6 +3430,13 @@ static int batch_step_until_batched(FdmBatch *b, double t_end, double dt0, uint6
         b->last_error = "cudaStreamCreate failed";
         return FULLMAG_FDM_ERR_CUDA;
     }
+    // a round left by an earlier call hands its state back before anything is read
+    std::string err0;
+    if (!b->sync_states(err0)) {
+        b->last_error = err0;
+        return FULLMAG_FDM_ERR_CUDA;
+    }
+    b->round.release();
     for (size_t i = 0; i < n; ++i) {
         Engine *e = b->items[i];
         steps0[i] = e->step_count;
@@ -3358,59 +3455,36 @@ static int batch_step_until_batched(FdmBatch *b, double t_end, double dt0, uint6
     while (!active.empty()) {
         if (!built || active.size() * 10 < b->round.members.size() * 9) {
             std::string err;
-            if (!b->build_round(active, err)) {
+            if (!b->build_round(active, t_end, err)) {
                 if (!built) return 1;  // not batchable: caller falls back
                 b->last_error = err;
                 return FULLMAG_FDM_ERR_CUDA;
             }
             built = true;
         }
-        const std::vector<size_t> &mem = b->round.members;
-        for (size_t k = 0; k < mem.size(); ++k) {
-            Engine *e = b->items[mem[k]];
-            // a finished problem gets step size 0: its row and column CTAs return at once
-            b->round.h_ctl[k].dt = done[mem[k]] ? 0.0 : std::min(b->next_dt[mem[k]], t_end - e->time);
-        }
         if (cudaGraphLaunch(b->round.exec, b->bstream) != cudaSuccess || cudaStreamSynchronize(b->bstream) != cudaSuccess) {
             b->last_error = "batch round launch failed";
             return FULLMAG_FDM_ERR_CUDA;
         }
+        const auto now = std::chrono::steady_clock::now();
+        const std::vector<size_t> &mem = b->round.members;
         std::vector<size_t> still;
         for (size_t k = 0; k < mem.size(); ++k) {
             const size_t i = mem[k];
-            Engine *e = b->items[i];
-            BatchCtl *ctl = &b->round.h_ctl[k];
-            if (done[i]) {  // proposal discarded; any pending commit ran at this round's start
-                ctl->accept_prev = 0;
-                continue;
-            }
-            e->launches += 7 + (e->demag ? 6 : 0) + 1;
-            double nd = b->next_dt[i];
-            e->batch_decide(b->round.h_stats + k * kNumStats, ctl, nd);
-            b->next_dt[i] = nd;
-            if (e->time >= t_end * (1.0 - 1e-12)) {
+            if (done[i]) continue;
+            b->items[i]->launches += (uint64_t)BatchRound::kRounds * (7 + (b->items[i]->demag ? 6 : 0) + 1);
+            if (b->round.h_state[k].done) {
                 done[i] = 1;
-                if (out_wall_ns)
-                    out_wall_ns[i] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
-                                         std::chrono::steady_clock::now() - t0)
-                                         .count();
-                if (!e->batch_flush(ctl, b->bstream)) {  // commit the final step now
-                    b->last_error = "problem " + std::to_string(i) + ": " + e->last_error;
-                    return FULLMAG_FDM_ERR_CUDA;
-                }
+                if (out_wall_ns) out_wall_ns[i] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(now - t0).count();
             } else {
                 still.push_back(i);
             }
         }
         active.swap(still);
     }
-    for (size_t k = 0; k < b->round.members.size(); ++k)
-        if (!b->items[b->round.members[k]]->batch_flush(&b->round.h_ctl[k], b->bstream)) {
-            b->last_error = "commit failed";
-            return FULLMAG_FDM_ERR_CUDA;
-        }
-    if (cudaStreamSynchronize(b->bstream) != cudaSuccess) {
-        b->last_error = "batch stream sync failed";
+    std::string err;
+    if (!b->sync_states(err)) {
+        b->last_error = err;
         return FULLMAG_FDM_ERR_CUDA;
     }
     for (size_t i = 0; i < n; ++i) {
