@@ -88,3 +88,21 @@ def test_bad_region_ids_are_rejected(gpu_lib):
     reg[5] = 256
     with pytest.raises(FdmError):
         FdmBackend(**problem(8, 4, 1, seed=104, region_mask=reg))
+
+
+def test_high_region_ids(gpu_lib, oracle):
+    """Ids 128 and 255 (one byte per cell on the device: the values a signed or narrowed
+    load would get wrong, and the largest table row offsets) with non-zero stiffness
+    between them and with region 0, against the oracle."""
+    nx, ny, nz = 18, 10, 2
+    rng = np.random.default_rng(9)
+    reg = rng.choice(np.array([0, 128, 255], dtype=np.uint32), size=nx * ny * nz)
+    lut = np.zeros((256, 256))
+    lut[0, 0], lut[128, 128], lut[255, 255] = 1.3e-11, 0.8e-11, 1.9e-11
+    lut[128, 255] = lut[255, 128] = 0.6e-11
+    lut[0, 255] = lut[255, 0] = 0.2e-11
+    kw = problem(nx, ny, nz, seed=103, region_mask=reg, exchange_lut=lut)
+    gpu, orc = make_pair(oracle, kw)
+    ref = orc.fields(kw["m0"])
+    assert rel_l2(gpu.copy_field(_abi.OBSERVABLE_H_EX), ref["h_ex"]) < 1e-5
+    assert abs(gpu.stats()["exchange_energy_joules"] - orc.observe()["e_exchange"]) <= 1e-5 * abs(orc.observe()["e_exchange"])
