@@ -164,3 +164,44 @@ def test_adjoint_misuse(gpu_lib, oracle):
     heun = FdmBackend(**kw, integrator=_abi.INTEGRATOR_HEUN)
     with pytest.raises(FdmError):
         heun.adjoint_forward(DT, 4)
+
+
+def test_config5_full_size_directional_derivative(gpu_lib, oracle):
+    """The adjoint benchmark configuration at its own size (256x64x1 film of 4 nm cells,
+    4000 RK4 steps of 5e-14 s, field map N(0, 2 mT), m0 = +x, the seeded target of eight
+    Gaussian bumps, loss mean |m_T - m*|^2): the gradient through the autograd Function
+    along one seeded field-map direction against the oracle's FP64 tangent-linear RK4
+    of the same 4000 steps, within 1e-4 relative."""
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    if str(root) not in sys.path:
+        sys.path.insert(0, str(root))
+    import bench
+    kw, bmap, target = bench.adjoint_problem()
+    n = kw["nx"] * kw["ny"]
+    steps = 4000
+    gpu = FdmBackend(**kw)
+    b = torch.tensor(bmap, dtype=torch.float64, requires_grad=True)
+    m_t = rk4_final_state(torch.tensor(kw["m0"], dtype=torch.float64), b, gpu, DT, steps)
+    loss = ((m_t - torch.tensor(target)) ** 2).mean()
+    loss.backward()
+    g = b.grad.numpy()  # d loss / d B (tesla)
+    gpu.close()
+    okw = {k: v for k, v in kw.items() if k != "integrator"}
+    orc = oracle.Problem(**okw, integrator=oracle.RK4)
+    hmap = np.zeros((n, 3))
+    hmap[:, :2] = bmap / MU0
+    orc.set_field_map(hmap)
+    rng = np.random.default_rng(21)
+    db = rng.normal(size=(n, 2)) * 1e-3  # direction in tesla
+    dh = np.zeros((n, 3))
+    dh[:, :2] = db / MU0
+    dm = orc.tangent_rk4(DT, steps, dh=dh)
+    m_o = orc.get_m()
+    # d loss = (2/(3n)) sum (m_T - m*) . dm
+    want = float(2.0 / (3 * n) * np.sum((m_o - target) * dm))
+    got = float(np.sum(g * db))
+    assert np.abs(m_t.detach().numpy() - m_o).max() < 5e-4  # FP32 state over 4000 steps
+    assert abs(got - want) <= 1e-4 * abs(want), (got, want)
+    orc.close()
