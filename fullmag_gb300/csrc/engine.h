@@ -52,6 +52,7 @@ struct Grid {
     int thin;        // 1: 2-D transform (nz == 1, pz == 1)
     // dividers for the index arithmetic of the passes
     FastDiv fd_nx, fd_ny, fd_nz, fd_half, fd_nkx, fd_py, fd_pz, fd_padw;
+    FastDiv fd_nx2, fd_nx4;  // nx / 2, nx / 4 (1 when nx is not a multiple)
 };
 
 inline void grid_dividers(Grid &g) {
@@ -63,6 +64,8 @@ inline void grid_dividers(Grid &g) {
     g.fd_py = FastDiv((uint32_t)g.py);
     g.fd_pz = FastDiv((uint32_t)g.pz);
     g.fd_padw = FastDiv((uint32_t)(2 * g.half - g.nx > 0 ? 2 * g.half - g.nx : 1));
+    g.fd_nx2 = FastDiv((uint32_t)(g.nx % 2 == 0 && g.nx >= 2 ? g.nx / 2 : 1));
+    g.fd_nx4 = FastDiv((uint32_t)(g.nx % 4 == 0 && g.nx >= 4 ? g.nx / 4 : 1));
 }
 
 // Fused row pass: one CTA owns `rows` consecutive x-rows.  Depending on the

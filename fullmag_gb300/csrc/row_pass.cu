@@ -26,6 +26,7 @@ namespace fm {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kRowVec = 4;  // cells per thread on the unmasked path (2 measured slower)
 constexpr int kWarps = kThreads / 32;
 
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
@@ -200,6 +201,256 @@ __device__ __forceinline__ A3 a3_cross(A3 a, A3 b) {
 __device__ __forceinline__ float a3_dot(A3 a, A3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ A3 a3_axpy(float s, A3 a, A3 b) { return {s * a.x + b.x, s * a.y + b.y, s * a.z + b.z}; }
 
+// ---- per-cell work on V consecutive cells per thread ----
+// Unmasked grids with nx a multiple of V and at least one group of V cells per thread
+// (the 256x256x64 volume) take this path: every x-contiguous array (state, its y+-1 and
+// z+-1 neighbour rows, stage derivatives, field map, outputs) moves as one V-wide vector
+// per component, the x-neighbours come from the same registers (two scalar loads at the
+// group's ends), and the row / column index arithmetic is done once per group.  Every
+// buffer is a 256-byte aligned arena slice of 3n floats and n is a multiple of V, so the
+// vector accesses are aligned.  The per-cell arithmetic is the scalar loop's; only the
+// forward-pair exchange energy sums its terms per component first.
+template <int V>
+__device__ __forceinline__ void ldv(const float *p, float (&v)[V]) {
+    if constexpr (V == 4) {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = a.z;
+        v[3] = a.w;
+    } else {
+        const float2 a = *reinterpret_cast<const float2 *>(p);
+        v[0] = a.x;
+        v[1] = a.y;
+    }
+}
+template <int V>
+__device__ __forceinline__ void stv(float *p, const float (&v)[V]) {
+    if constexpr (V == 4)
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    else
+        *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+}
+
+template <int V>
+__device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, const float2 *hd, float2 *pack, int lsx,
+                                           float (&sum_hi)[5], float (&sum_lo)[5], float (&mx2)[4], float dt_f,
+                                           double err_dt) {
+    const Grid &g = p.g;
+    const Material &M = p.mat;
+    const int nx = g.nx, nxv = nx / V, ny = g.ny, nz = g.nz;
+    const long long n = g.n;
+    const int plane = nx * ny;
+    for (int gi = threadIdx.x; gi < rows * nxv; gi += blockDim.x) {
+        const int rr = (V == 4 ? g.fd_nx4 : g.fd_nx2).div(gi);
+        const int x0 = (gi - rr * nxv) * V;
+        const int row = row0 + rr;
+        const int z = g.fd_ny.div(row);
+        const int y = row - z * ny;
+        const long long i0 = (long long)row * nx + x0;
+        float kv[3][V] = {};
+        if (p.m_in) {
+            // per component: exchange Laplacian, demag, external and map fields summed into
+            // h in the scalar loop's order; m.h_d, |h_d|^2 and the forward-pair |dm|^2
+            // accumulate across the components (clamped neighbours give zero differences,
+            // so the last cell of a row / column / plane needs no mask)
+            float m0v[3][V], hv[3][V], e_pair[V], dd[V], dn[V];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float *mc = p.m_in + c * n;
+                float cc[V], ex[V], dv[V];
+                ldv<V>(mc + i0, cc);
+#pragma unroll
+                for (int j = 0; j < V; ++j) m0v[c][j] = cc[j];
+                if (M.ex_pref != 0.f) {
+                    float ym[V], yp[V], zm[V], zp[V], xm[V], xp[V];
+                    ldv<V>(mc + i0 - (y > 0 ? nx : 0), ym);
+                    ldv<V>(mc + i0 + (y < ny - 1 ? nx : 0), yp);
+                    ldv<V>(mc + i0 - (z > 0 ? plane : 0), zm);
+                    ldv<V>(mc + i0 + (z < nz - 1 ? plane : 0), zp);
+                    xm[0] = x0 > 0 ? mc[i0 - 1] : cc[0];
+                    xp[V - 1] = x0 + V < nx ? mc[i0 + V] : cc[V - 1];
+#pragma unroll
+                    for (int j = 1; j < V; ++j) {
+                        xm[j] = cc[j - 1];
+                        xp[j - 1] = cc[j];
+                    }
+#pragma unroll
+                    for (int j = 0; j < V; ++j) {
+                        ex[j] = M.ex_pref * ((xp[j] - 2.f * cc[j] + xm[j]) * M.idx2 + (yp[j] - 2.f * cc[j] + ym[j]) * M.idy2 +
+                                             (zp[j] - 2.f * cc[j] + zm[j]) * M.idz2);
+                        if (p.partials) {
+                            const float d0 = xp[j] - cc[j], d1 = yp[j] - cc[j], d2 = zp[j] - cc[j];
+                            const float t = d0 * d0 * M.idx2 + d1 * d1 * M.idy2 + d2 * d2 * M.idz2;
+                            e_pair[j] = c ? e_pair[j] + t : t;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < V; ++j) {
+                        ex[j] = 0.f;
+                        e_pair[j] = 0.f;
+                    }
+                }
+                if (hd) {
+#pragma unroll
+                    for (int j = 0; j < V; j += 2) {
+                        const float2 h2 = hd[(rr * 3 + c) * lsx + sk((x0 + j) >> 1)];
+                        dv[j] = h2.x;
+                        dv[j + 1] = h2.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < V; ++j) dv[j] = 0.f;
+                }
+                float hm[V];
+                if (p.hmap) ldv<V>(p.hmap + c * n + i0, hm);
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                    float h = ex[j] + dv[j];
+                    if (M.has_ext) h += M.hext[c];
+                    if (p.hmap) h += hm[j];
+                    hv[c][j] = h;
+                    dd[j] = c ? dd[j] + cc[j] * dv[j] : cc[j] * dv[j];
+                    dn[j] = c ? dn[j] + dv[j] * dv[j] : dv[j] * dv[j];
+                }
+                if (p.h_ex_out) stv<V>(p.h_ex_out + c * n + i0, ex);
+                if (p.h_d_out) stv<V>(p.h_d_out + c * n + i0, dv);
+            }
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                const float m0x = m0v[0][j], m0y = m0v[1][j], m0z = m0v[2][j];
+                float hx = hv[0][j], hy = hv[1][j], hz = hv[2][j];
+                float e_uni = 0.f, e_cub = 0.f;
+                if (M.has_uni) {
+                    const float mu = m0x * M.u[0] + m0y * M.u[1] + m0z * M.u[2];
+                    const float cf = M.ku1c * mu + M.ku2c * mu * mu * mu;
+                    hx += cf * M.u[0];
+                    hy += cf * M.u[1];
+                    hz += cf * M.u[2];
+                    const float s = mu * mu;
+                    e_uni = M.ku1f * s + M.ku2f * s * s;
+                }
+                if (M.has_cub) {
+                    const float a1 = m0x * M.c1[0] + m0y * M.c1[1] + m0z * M.c1[2];
+                    const float a2 = m0x * M.c2[0] + m0y * M.c2[1] + m0z * M.c2[2];
+                    const float a3 = m0x * M.c3[0] + m0y * M.c3[1] + m0z * M.c3[2];
+                    const float s1 = a1 * a1, s2 = a2 * a2, s3 = a3 * a3;
+                    const float sig = s1 * s2 + s2 * s3 + s1 * s3;
+                    const float g1 = M.kc1c * a1 * (s2 + s3) + M.kc2c * a1 * s2 * s3 + M.kc3c * sig * a1 * (s2 + s3);
+                    const float g2 = M.kc1c * a2 * (s1 + s3) + M.kc2c * a2 * s1 * s3 + M.kc3c * sig * a2 * (s1 + s3);
+                    const float g3 = M.kc1c * a3 * (s1 + s2) + M.kc2c * a3 * s1 * s2 + M.kc3c * sig * a3 * (s1 + s2);
+                    hx += g1 * M.c1[0] + g2 * M.c2[0] + g3 * M.c3[0];
+                    hy += g1 * M.c1[1] + g2 * M.c2[1] + g3 * M.c3[1];
+                    hz += g1 * M.c1[2] + g2 * M.c2[2] + g3 * M.c3[2];
+                    e_cub = M.kc1f * sig + M.kc2f * s1 * s2 * s3 + M.kc3f * sig * sig;
+                }
+                const float px_ = m0y * hz - m0z * hy;
+                const float py_ = m0z * hx - m0x * hz;
+                const float pz_ = m0x * hy - m0y * hx;
+                const float qx = m0y * pz_ - m0z * py_;
+                const float qy = m0z * px_ - m0x * pz_;
+                const float qz = m0x * py_ - m0y * px_;
+                kv[0][j] = -M.gbar * (M.prec * px_ + M.alpha * qx);
+                kv[1][j] = -M.gbar * (M.prec * py_ + M.alpha * qy);
+                kv[2][j] = -M.gbar * (M.prec * pz_ + M.alpha * qz);
+                if (p.partials) {
+                    ff_add(sum_hi[0], sum_lo[0], e_pair[j]);
+                    ff_add(sum_hi[1], sum_lo[1], dd[j]);
+                    if (M.has_ext) ff_add(sum_hi[2], sum_lo[2], m0x * M.hext[0] + m0y * M.hext[1] + m0z * M.hext[2]);
+                    if (p.hmap) {
+                        const long long i = i0 + j;
+                        ff_add(sum_hi[2], sum_lo[2], m0x * p.hmap[i] + m0y * p.hmap[n + i] + m0z * p.hmap[2 * n + i]);
+                    }
+                    ff_add(sum_hi[3], sum_lo[3], e_uni);
+                    ff_add(sum_hi[V], sum_lo[V], e_cub);
+                    mx2[0] = fmaxf(mx2[0], hx * hx + hy * hy + hz * hz);
+                    mx2[1] = fmaxf(mx2[1], dn[j]);
+                    mx2[2] = fmaxf(mx2[2], kv[0][j] * kv[0][j] + kv[1][j] * kv[1][j] + kv[2][j] * kv[2][j]);
+                }
+                if (p.h_eff_out) {
+                    const long long i = i0 + j;
+                    p.h_eff_out[i] = hx;
+                    p.h_eff_out[n + i] = hy;
+                    p.h_eff_out[2 * n + i] = hz;
+                }
+            }
+            if (p.partials && p.n_err > 0) {
+                // |dt sum_t e_t k_t|^2 per cell in FP64, one component at a time
+                double esq[V];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    double e[V] = {};
+                    for (int t = 0; t < p.n_err; ++t) {
+                        const float *kk = p.err_k[t];
+                        const double w = p.err_c[t];
+                        float kc[V];
+                        if (kk) ldv<V>(kk + c * n + i0, kc);
+#pragma unroll
+                        for (int j = 0; j < V; ++j) e[j] += w * (double)(kk ? kc[j] : kv[c][j]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < V; ++j) {
+                        const double ej = e[j] * err_dt;
+                        esq[j] = c ? esq[j] + ej * ej : ej * ej;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < V; ++j) mx2[3] = fmaxf(mx2[3], (float)esq[j]);
+            }
+            if (p.k_out)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) stv<V>(p.k_out + c * n + i0, kv[c]);
+        }
+        // ---- next stage input: m0 + dt sum_t c_t k_t, normalised ----
+        float nv[3][V];
+        if (p.m0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float sv[V] = {};
+                for (int t = 0; t < p.n_comb; ++t) {
+                    const float *kk = p.comb_k[t];
+                    const float w = p.comb_c[t];
+                    float kc[V];
+                    if (kk) ldv<V>(kk + c * n + i0, kc);
+#pragma unroll
+                    for (int j = 0; j < V; ++j) sv[j] += w * (kk ? kc[j] : kv[c][j]);
+                }
+                float mb[V];
+                ldv<V>(p.m0 + c * n + i0, mb);
+#pragma unroll
+                for (int j = 0; j < V; ++j) nv[c][j] = mb[j] + dt_f * sv[j];
+            }
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                const float vx = nv[0][j], vy = nv[1][j], vz = nv[2][j];
+                const float nn = sqrtf(vx * vx + vy * vy + vz * vz);
+                const float inv = nn > 0.f ? 1.0f / nn : 0.f;
+                nv[0][j] = vx * inv;
+                nv[1][j] = vy * inv;
+                nv[2][j] = vz * inv;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) stv<V>(p.m_next + c * n + i0, nv[c]);
+        } else if (p.m_fwd) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ldv<V>(p.m_fwd + c * n + i0, nv[c]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int j = 0; j < V; ++j) nv[c][j] = 0.f;
+        }
+        if (p.x_out) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+#pragma unroll
+                for (int j = 0; j < V; j += 2) pack[(rr * 3 + c) * lsx + sk((x0 + j) >> 1)] = make_float2(nv[c][j], nv[c][j + 1]);
+            }
+        }
+    }
+}
+
 // Body of the row pass for CTA `bid` of `nblk`; shared by the single-problem kernel
 // and the batched kernel that walks a (problem, block) work table.  ADJ compiles the
 // adjoint modes (a separate kernel, so the forward kernel's registers are unaffected).
@@ -261,7 +512,10 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     const double dt_d = p.dt_dev ? *p.dt_dev : (double)p.dt;  // step size of this pass
     const float dt_f = (float)dt_d;
     const double err_dt = p.dt_dev ? dt_d : p.err_dt;
-    for (int idx = threadIdx.x; idx < rows * nx; idx += blockDim.x) {
+    bool vec = false;
+    if constexpr (!ADJ) vec = p.mask == nullptr && (nx & (kRowVec - 1)) == 0 && rows * (nx / kRowVec) >= (int)blockDim.x;
+    if (vec) cells_vec<kRowVec>(p, rows, row0, hd, pack, lsx, sum_hi, sum_lo, mx2, dt_f, err_dt);
+    for (int idx = vec ? rows * nx : threadIdx.x; idx < rows * nx; idx += blockDim.x) {
         const int rr = g.fd_nx.div(idx);
         const int x = idx - rr * nx;
         const int row = row0 + rr;
@@ -588,11 +842,11 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     }
 }
 
-__global__ void __launch_bounds__(kThreads) row_pass_kernel(const RowPass p) { row_pass_body<false>(p, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kThreads, 3) row_pass_kernel(const RowPass p) { row_pass_body<false>(p, blockIdx.x, gridDim.x); }
 __global__ void __launch_bounds__(kThreads) row_pass_adj_kernel(const RowPass p) { row_pass_body<true>(p, blockIdx.x, gridDim.x); }
 
 // One launch for many problems: work[blockIdx.x] = (problem, block within problem).
-__global__ void __launch_bounds__(kThreads) row_pass_batched_kernel(const RowPass *__restrict__ ps,
+__global__ void __launch_bounds__(kThreads, 3) row_pass_batched_kernel(const RowPass *__restrict__ ps,
                                                                     const int2 *__restrict__ work) {
     // stage the problem's descriptor in shared memory once per CTA: the body reads its
     // fields in every loop, and global reads could not be hoisted past the stores
