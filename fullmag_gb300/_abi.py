@@ -192,6 +192,10 @@ class SnapshotDesc(C.Structure):
                 ("scalar_type", _i)]
 
 
+class PeriodicityDesc(C.Structure):
+    _fields_ = [("periodic", _u32 * 3), ("has_image_counts", _u32), ("image_counts", _u32 * 3)]
+
+
 POLL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
 
 # (name, restype, argtypes) of every exported entry point, in header order.
@@ -241,6 +245,7 @@ SIGNATURES = [
     ("fullmag_fdm_batch_destroy", None, [_vp]),
     ("fullmag_fdm_backend_fft_shape", _i, [_vp, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     ("fullmag_fdm_backend_upload_magnetization_f64_noalloc", _i, [_vp, _pd, _u64]),
+    ("fullmag_fdm_backend_create_periodic", _vp, [C.POINTER(PlanDesc), C.POINTER(PeriodicityDesc)]),
 ]
 
 REFERENCE_SYMBOLS = [s[0] for s in SIGNATURES[:22]]

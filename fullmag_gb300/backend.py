@@ -218,15 +218,31 @@ def make_plan(*, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float,
 
 
 class FdmBackend:
-    """One FDM problem on the GPU behind the C ABI (keyword arguments: ``make_plan``)."""
+    """One FDM problem on the GPU behind the C ABI (keyword arguments: ``make_plan``).
 
-    def __init__(self, **plan_kwargs):
+    ``periodic`` (x, y, z flags) selects periodic axes and ``image_counts`` the demag
+    images per periodic axis (default 10), the reference CPU engine's FdmBoundaryPolicy
+    and demag_image_counts (crates/fullmag-engine/src/fdm_problem.rs:19-23); the problem
+    is then created through fullmag_fdm_backend_create_periodic."""
+
+    def __init__(self, periodic: Optional[Sequence[int]] = None, image_counts: Optional[Sequence[int]] = None,
+                 **plan_kwargs):
         self.lib = load_library()
         p, keep = make_plan(**plan_kwargs)
         self.n = p.grid.nx * p.grid.ny * p.grid.nz
         self.shape = (p.grid.nz, p.grid.ny, p.grid.nx)
         self._poll = None
-        self.handle = self.lib.fullmag_fdm_backend_create(C.byref(p))
+        if periodic is not None or image_counts is not None:
+            d = _abi.PeriodicityDesc()
+            for a, v in enumerate(periodic or (0, 0, 0)):
+                d.periodic[a] = int(v)
+            if image_counts is not None:
+                d.has_image_counts = 1
+                for a, v in enumerate(image_counts):
+                    d.image_counts[a] = int(v)
+            self.handle = self.lib.fullmag_fdm_backend_create_periodic(C.byref(p), C.byref(d))
+        else:
+            self.handle = self.lib.fullmag_fdm_backend_create(C.byref(p))
         del keep
         if not self.handle:
             raise FdmError(_abi.ERR_INTERNAL, "fullmag_fdm_backend_create returned NULL")

@@ -30,6 +30,26 @@ __device__ __forceinline__ void kernel_mirror(int k, int p, int &km, float &sg) 
     }
 }
 
+// H = -K M with the complex kernel of a periodic grid: K points at component xx of one
+// frequency, the other components follow at stride kc (xx yy zz xy xz yz; 2-D: the
+// first four, xz = yz = 0).
+__device__ __forceinline__ float2 cmadd(float2 k, float2 m, float2 acc) {
+    return make_float2(acc.x + k.x * m.x - k.y * m.y, acc.y + k.x * m.y + k.y * m.x);
+}
+__device__ __forceinline__ void multiply_periodic(const float2 *K, size_t kc, bool thin, float2 *lx, float2 *ly,
+                                                  float2 *lz) {
+    const float2 kxx = __ldg(K), kyy = __ldg(K + kc), kzz = __ldg(K + 2 * kc), kxy = __ldg(K + 3 * kc);
+    const float2 z0 = make_float2(0.f, 0.f);
+    const float2 kxz = thin ? z0 : __ldg(K + 4 * kc), kyz = thin ? z0 : __ldg(K + 5 * kc);
+    const float2 mx = *lx, my = *ly, mz = *lz;
+    const float2 hx = cmadd(kxz, mz, cmadd(kxy, my, cmadd(kxx, mx, z0)));
+    const float2 hy = cmadd(kyz, mz, cmadd(kyy, my, cmadd(kxy, mx, z0)));
+    const float2 hz = cmadd(kzz, mz, cmadd(kyz, my, cmadd(kxz, mx, z0)));
+    *lx = make_float2(-hx.x, -hx.y);
+    *ly = make_float2(-hy.x, -hy.y);
+    *lz = make_float2(-hz.x, -hz.y);
+}
+
 // X[c][z][y<ny][kx] -> Y[c][z][ky<py][kx] (forward along y, zero rows pruned)
 __global__ void __launch_bounds__(kThreads) y_forward_kernel(const ColPass p) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -143,8 +163,19 @@ __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
     __syncthreads();
     float2 *r = fft_lines(a, b, nl, ls, p.plan, false);
     float2 *o = (r == a) ? b : a;
+    if (g.per) {  // complex kernel K[c][kz][ky][kx]
+        const size_t kcp = (size_t)g.pz * g.py * g.nkx;
+        for (int idx = threadIdx.x; idx < np * g.pz * tx; idx += blockDim.x) {
+            const int r1 = p.fd_tx.div(idx), col = idx - r1 * tx;
+            const int q = r1 >= g.pz ? 1 : 0, kz = r1 - q * g.pz;
+            const int kx = min(kx0 + col, g.nkx - 1), ky = q ? kyb : kya;
+            const float2 *K = reinterpret_cast<const float2 *>(p.kern) + ((size_t)kz * g.py + ky) * g.nkx + kx;
+            multiply_periodic(K, kcp, false, r + ((q * 3 + 0) * tx + col) * ls + sk(kz), r + ((q * 3 + 1) * tx + col) * ls + sk(kz),
+                              r + ((q * 3 + 2) * tx + col) * ls + sk(kz));
+        }
+    }
     const size_t kc = (size_t)g.nkz * g.nky * g.nkx;
-    for (int idx = threadIdx.x; idx < g.pz * tx; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < (g.per ? 0 : g.pz * tx); idx += blockDim.x) {
         const int kz = p.fd_tx.div(idx), col = idx - kz * tx;
         const int kx = min(kx0 + col, g.nkx - 1);
         int kzm;
@@ -510,7 +541,7 @@ __device__ __forceinline__ void z_small_convolve(float2 *line, size_t lstride, i
 
 __host__ __device__ __forceinline__ bool yz_fused_ok(const Grid &g) {
     const int py = g.py, pz = g.pz;
-    return (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py &&
+    return g.per == 0 && (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py &&
            (pz == 2 || pz == 4 || pz == 8) && 2 * g.nz <= pz;
 }
 
@@ -789,7 +820,7 @@ __device__ __forceinline__ void y_convolve_2d_fused_body(const ColPass &p, const
 // (py = 512 keeps the general path: its inner pass would hold 3 x 16 complex values)
 __host__ __device__ __forceinline__ bool y2d_fused_ok(const Grid &g) {
     const int py = g.py;
-    return (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py;
+    return g.per == 0 && (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py;
 }
 
 __device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, const int tile);
@@ -835,8 +866,18 @@ __device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, con
     __syncthreads();
     float2 *r = fft_lines(a, b, nl, ls, p.plan, false);
     float2 *o = (r == a) ? b : a;
+    if (g.per) {  // complex kernel K[c][ky][kx]
+        const size_t kcp = (size_t)g.py * g.nkx;
+        for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
+            const int ky = p.fd_tx.div(idx), col = idx - ky * tx;
+            const int kx = min(kx0 + col, g.nkx - 1);
+            const float2 *K = reinterpret_cast<const float2 *>(p.kern) + (size_t)ky * g.nkx + kx;
+            multiply_periodic(K, kcp, true, r + (0 * tx + col) * ls + sk(ky), r + (1 * tx + col) * ls + sk(ky),
+                              r + (2 * tx + col) * ls + sk(ky));
+        }
+    }
     const size_t kc = (size_t)g.nky * g.nkx;
-    for (int idx = threadIdx.x; idx < g.py * tx; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < (g.per ? 0 : g.py * tx); idx += blockDim.x) {
         const int ky = p.fd_tx.div(idx), col = idx - ky * tx;
         const int kx = min(kx0 + col, g.nkx - 1);
         int kym;
@@ -1051,7 +1092,7 @@ cudaError_t launch_z_fused(const ColPass &p, cudaStream_t s) {
 // power-of-two pz with every physical plane in the lower half: the pruned fused kernel
 bool z_fused_ok(const Grid &g) {
     const int pz = g.pz;
-    return (pz == 16 || pz == 32 || pz == 64 || pz == 128 || pz == 256 || pz == 512) && 2 * g.nz <= pz;
+    return g.per == 0 && (pz == 16 || pz == 32 || pz == 64 || pz == 128 || pz == 256 || pz == 512) && 2 * g.nz <= pz;
 }
 }  // namespace
 
@@ -1110,6 +1151,7 @@ size_t yz_convolve_smem(const Grid &g, int tx) {
 }
 
 cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s) {
+    if (p.g.per) return cudaErrorInvalidValue;  // the fused y+z pass reads the octant kernel only
     const size_t sm = yz_convolve_smem(p.g, p.tx);
     cudaError_t e = ensure_smem((const void *)yz_convolve_kernel, sm);
     if (e != cudaSuccess) return e;

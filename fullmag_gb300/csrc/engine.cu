@@ -496,6 +496,10 @@ struct Engine {
     }
 
     bool use_gpu_newell = false;
+    // periodic boundary policy requested at create (bit 0 x, 1 y, 2 z) and the demag
+    // image counts per axis (fdm_problem.rs:19-23,89-90)
+    int per_req = 0;
+    uint32_t images[3] = {10, 10, 10};
 
     // largest prime factor <= 7 for the fast radix kernels; up to 64 still works
     static bool smooth_enough(int n) {
@@ -1887,7 +1891,23 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     use_gpu_newell = false;
     g.px = 2 * g.nx;
     g.py = 2 * g.ny;
-    if (demag) {
+    g.per = per_req;
+    if (g.per) {
+        // periodic axes (fdm_fft.rs:140-160): the extent is the cell count, unpadded; open
+        // axes keep a padded extent >= 2n - 1; the tensor is always built here
+        if ((g.per & 1) && (g.nx & 1)) {
+            last_error = "a periodic x axis needs an even number of cells";
+            return false;
+        }
+        if (demag && plan->demag_kernel_spectrum_len != 0) {
+            last_error = "periodic boundaries: the backend builds the image-sum demag tensor, the plan must carry no spectra";
+            return false;
+        }
+        thin = g.nz == 1;
+        use_gpu_newell = demag;
+        g.px = (g.per & 1) ? g.nx : pad_extent(2 * g.nx - 1, true);
+        g.py = (g.per & 2) ? g.ny : pad_extent(2 * g.ny - 1, false);
+    } else if (demag) {
         const uint64_t len3 = 2ull * (uint64_t)(2 * g.nx) * (2 * g.ny) * (2 * g.nz);
         const uint64_t len2 = 2ull * (uint64_t)(2 * g.nx) * (2 * g.ny);
         if (plan->demag_kernel_spectrum_len == 0) {
@@ -1917,7 +1937,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
         }
     }
     g.thin = thin ? 1 : 0;
-    g.pz = thin ? 1 : (use_gpu_newell ? pad_extent(2 * g.nz - 1, false) : 2 * g.nz);
+    g.pz = thin ? 1 : (g.per & 4) ? g.nz : (use_gpu_newell ? pad_extent(2 * g.nz - 1, false) : 2 * g.nz);
     if (g.px < 2) g.px = 2;
     g.half = g.px / 2;
     g.nkx = g.half + 1;
@@ -2133,7 +2153,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     tx_2d = col_tile(g, 3, g.py);
     {
         const char *no_yz = std::getenv("FULLMAG_FDM_NO_FUSED_YZ");
-        use_yz = demag && !thin && !(no_yz && *no_yz && *no_yz != '0') && yz_convolve_smem(g, 1) <= 200u * 1024u;
+        use_yz = demag && !thin && !g.per && !(no_yz && *no_yz && *no_yz != '0') && yz_convolve_smem(g, 1) <= 200u * 1024u;
         if (use_yz) {
             tx_z = 1;
             while (tx_z < 8 && yz_convolve_smem(g, 2 * tx_z) <= 200u * 1024u) tx_z *= 2;
@@ -2142,7 +2162,9 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     const size_t vec = sizeof(float) * 3 * (size_t)g.n;
     const size_t xlen = demag ? sizeof(float2) * 3 * (size_t)g.nz * g.ny * g.nkx : 0;
     const size_t ylen = (demag && !thin && !use_yz) ? sizeof(float2) * 3 * (size_t)g.nz * g.py * g.nkx : 0;
-    const size_t klen = demag ? sizeof(float) * (thin ? 4 : 6) * (size_t)g.nkz * g.nky * g.nkx : 0;
+    const size_t klen = !demag ? 0
+                        : g.per ? sizeof(float2) * (thin ? 4 : 6) * (size_t)g.pz * g.py * g.nkx
+                                : sizeof(float) * (thin ? 4 : 6) * (size_t)g.nkz * g.nky * g.nkx;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     size_t off = 0;
     std::vector<size_t> o;
@@ -2259,7 +2281,13 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     if (has_mask && cuda_fail("cudaMemcpy(mask)", cudaMemcpyAsync(mask, mask_host.data(), (size_t)g.n, cudaMemcpyHostToDevice, stream)))
         return false;
     if (demag) {
-        if (use_gpu_newell) {
+        if (g.per) {
+            std::string err;
+            if (!newell_periodic_spectrum_gpu(g, dx, dy, dz, ms, images, reinterpret_cast<float2 *>(kern), stream, err)) {
+                last_error = err;
+                return false;
+            }
+        } else if (use_gpu_newell) {
             std::string err;
             if (!newell_spectrum_gpu(g, dx, dy, dz, ms, kern, stream, err)) {
                 last_error = err;
@@ -2286,9 +2314,10 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
 
 namespace {
 struct TuneKey {
-    int nx, ny, nz, px, py, pz, thin, masked;
+    int nx, ny, nz, px, py, pz, thin, masked, per;
     bool operator<(const TuneKey &o) const {
-        return std::tie(nx, ny, nz, px, py, pz, thin, masked) < std::tie(o.nx, o.ny, o.nz, o.px, o.py, o.pz, o.thin, o.masked);
+        return std::tie(nx, ny, nz, px, py, pz, thin, masked, per) <
+               std::tie(o.nx, o.ny, o.nz, o.px, o.py, o.pz, o.thin, o.masked, o.per);
     }
 };
 struct TuneChoice {
@@ -2303,7 +2332,7 @@ std::map<TuneKey, TuneChoice> g_tune_cache;
 // the live, still-unused buffers.  Results are cached per grid shape in the process,
 // so batched problems of the same shape pay for the search once.
 bool Engine::autotune() {
-    const TuneKey key{g.nx, g.ny, g.nz, g.px, g.py, g.pz, g.thin, has_mask ? 1 : 0};
+    const TuneKey key{g.nx, g.ny, g.nz, g.px, g.py, g.pz, g.thin, has_mask ? 1 : 0, g.per};
     // FULLMAG_FDM_TUNE="rows,tx_yf,tx_z,tx_yi,tx_2d,z_pair,split_yf,split_z,split_yi" fixes every
     // choice (the values fullmag_fdm_backend_tuning reports), e.g. so that a profiler run uses
     // the launch shapes of an unprofiled one
@@ -2596,6 +2625,43 @@ fullmag_fdm_backend *fullmag_fdm_backend_create(const fullmag_fdm_plan_desc *pla
         e->f64 = fp64_create(plan, err);
         if (!e->f64) e->last_error = err;
         return reinterpret_cast<fullmag_fdm_backend *>(e);
+    }
+    if (!e->setup(plan)) return reinterpret_cast<fullmag_fdm_backend *>(e);
+    if (!e->upload<double>(plan->initial_magnetization_xyz)) return reinterpret_cast<fullmag_fdm_backend *>(e);
+    if (!e->eval_state(true)) return reinterpret_cast<fullmag_fdm_backend *>(e);
+    return reinterpret_cast<fullmag_fdm_backend *>(e);
+}
+
+fullmag_fdm_backend *fullmag_fdm_backend_create_periodic(const fullmag_fdm_plan_desc *plan,
+                                                         const fullmag_fdm_periodicity_desc *periodicity) {
+    if (!plan || !periodicity) return nullptr;
+    Engine *e = new (std::nothrow) Engine();
+    if (!e) return nullptr;
+    const int sel = device_from_env();
+    if (sel >= 0) {
+        cudaError_t err = cudaSetDevice(sel);
+        if (err != cudaSuccess) {
+            e->last_error = std::string("cudaSetDevice: ") + cudaGetErrorString(err);
+            return reinterpret_cast<fullmag_fdm_backend *>(e);
+        }
+    }
+    if (plan->precision == FULLMAG_FDM_PRECISION_DOUBLE) {
+        e->last_error = "periodic boundaries are available with single-precision state (use SINGLE)";
+        return reinterpret_cast<fullmag_fdm_backend *>(e);
+    }
+    for (int a = 0; a < 3; ++a) {
+        if (periodicity->periodic[a] > 1) {
+            e->last_error = "periodic[] entries must be 0 (open) or 1 (periodic)";
+            return reinterpret_cast<fullmag_fdm_backend *>(e);
+        }
+        if (periodicity->periodic[a]) e->per_req |= 1 << a;
+        if (periodicity->has_image_counts) {
+            if (periodicity->image_counts[a] > 4096) {
+                e->last_error = "image_counts above 4096";
+                return reinterpret_cast<fullmag_fdm_backend *>(e);
+            }
+            e->images[a] = periodicity->image_counts[a];
+        }
     }
     if (!e->setup(plan)) return reinterpret_cast<fullmag_fdm_backend *>(e);
     if (!e->upload<double>(plan->initial_magnetization_xyz)) return reinterpret_cast<fullmag_fdm_backend *>(e);
@@ -3002,6 +3068,12 @@ int fullmag_fdm_adjoint_forward(fullmag_fdm_backend *handle, double dt_seconds, 
     Engine *e = eng(handle);
     if (!e || !e->arena) return FULLMAG_FDM_ERR_INVALID;
     e->last_error.clear();
+    if (e->g.per && e->demag) {
+        // the backward pass applies the demag convolution as its own transpose, which
+        // the truncated image sum (not symmetric under i -> -i) is not
+        e->last_error = "adjoint gradients are not available with periodic demag";
+        return FULLMAG_FDM_ERR_INVALID;
+    }
     return e->adjoint_forward(dt_seconds, n_steps, checkpoint_every);
 }
 

@@ -6,7 +6,9 @@
 //   X spectrum    : x-transformed half spectrum, float2 X[c][z][y][kx],
 //                   kx in [0, px/2], rows only for y < ny, z < nz (zero rows pruned)
 //   Y spectrum    : (3-D only) y-transformed, float2 Y[c][z][ky][kx], ky in [0, py)
-//   demag kernel  : real, octant-unique, pre-scaled by Ms/P:
+//   demag kernel  : with a periodic axis complex and full, pre-scaled by Ms/P:
+//                   float2 K[6][pz][py][kx] (2-D: K[4][py][kx]); otherwise
+//                   real, octant-unique, pre-scaled by Ms/P:
 //                   3-D K[6][pz/2+1][py/2+1][kx]   (xx yy zz xy xz yz)
 //                   2-D K[4][py/2+1][kx]           (xx yy zz xy)
 //                   engines on the fused y+z path (small 3-D grids, every batched
@@ -16,6 +18,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <string>
 
 #include "fft_smem.cuh"
 
@@ -50,6 +54,7 @@ struct Grid {
     int half;        // px/2
     int nky, nkz;    // py/2+1, pz/2+1 (kernel octant extents)
     int thin;        // 1: 2-D transform (nz == 1, pz == 1)
+    int per;         // periodic axes (bit 0 x, 1 y, 2 z): wrap-around stencils, unpadded transforms
     // dividers for the index arithmetic of the passes
     FastDiv fd_nx, fd_ny, fd_nz, fd_half, fd_nkx, fd_py, fd_pz, fd_padw;
     FastDiv fd_nx2, fd_nx4;  // nx / 2, nx / 4 (1 when nx is not a multiple)
@@ -149,6 +154,9 @@ cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
 cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s);  // X -> X (small 3-D, uses plan2 for z)
 size_t yz_convolve_smem(const Grid &g, int tx);
+// The truncated-image periodic kernel (layout above) of a grid with g.per != 0
+bool newell_periodic_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, const uint32_t images[3],
+                                  float2 *kern, cudaStream_t s, std::string &err);
 // K[c][kz][ky][kx] -> K[c][kz][kx][ky] (the fused y+z path's layout), out of place
 cudaError_t launch_kern_ky_fast(const float *in, float *out, int ncomp, int nkz, int nky, int nkx, cudaStream_t s);
 size_t z_convolve_smem(const Grid &g, int tx);

@@ -110,14 +110,19 @@ __global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(cons
             const float mx = m[i], my = m[n + i], mz = m[2 * n + i];
             float ax = 0.f, ay = 0.f, az = 0.f;  // DMI + magnetoelastic
             if ((kNb || kRg) && (p.has_int || p.has_bulk || (kRg && p.region))) {
-                // neighbours with the Neumann clamp: a missing or inactive neighbour is the cell itself
+                // neighbours with the Neumann clamp: a missing or inactive neighbour is the cell
+                // itself; on a periodic axis the neighbour wraps around (fdm_types.rs:126-132)
                 const int x = (int)(i % g.nx);
                 const long long r = i / g.nx;
                 const int y = (int)(r % g.ny), z = (int)(r / g.ny);
                 const long long sxy = (long long)g.nx * g.ny;
-                long long xm = x > 0 ? i - 1 : i, xp = x < g.nx - 1 ? i + 1 : i;
-                long long ym = y > 0 ? i - g.nx : i, yp = y < g.ny - 1 ? i + g.nx : i;
-                long long zm = z > 0 ? i - sxy : i, zp = z < g.nz - 1 ? i + sxy : i;
+                const int per = g.per;
+                long long xm = x > 0 ? i - 1 : (per & 1) ? i + g.nx - 1 : i;
+                long long xp = x < g.nx - 1 ? i + 1 : (per & 1) ? i - (g.nx - 1) : i;
+                long long ym = y > 0 ? i - g.nx : (per & 2) ? i + sxy - g.nx : i;
+                long long yp = y < g.ny - 1 ? i + g.nx : (per & 2) ? i - sxy + g.nx : i;
+                long long zm = z > 0 ? i - sxy : (per & 4) ? i + sxy * (g.nz - 1) : i;
+                long long zp = z < g.nz - 1 ? i + sxy : (per & 4) ? i - sxy * (g.nz - 1) : i;
                 if (p.mask) {
                     if (!p.mask[xm]) xm = i;
                     if (!p.mask[xp]) xp = i;
@@ -237,13 +242,16 @@ __global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(cons
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
                         const float u = p.zl_u[a];
-                        if (u > 0.f && pos[a] > 0) {
-                            const long long q = i - st[a];
+                        // a periodic axis always has its upwind neighbour, wrapped around
+                        // (fdm_fields.rs:1288-1320)
+                        const bool wrap = (g.per >> a) & 1;
+                        if (u > 0.f && (pos[a] > 0 || wrap)) {
+                            const long long q = pos[a] > 0 ? i - st[a] : i + st[a] * (ext[a] - 1);
                             Dx += u * (mx - m[q]) * inv[a];
                             Dy += u * (my - m[n + q]) * inv[a];
                             Dz += u * (mz - m[2 * n + q]) * inv[a];
-                        } else if (u < 0.f && pos[a] < ext[a] - 1) {
-                            const long long q = i + st[a];
+                        } else if (u < 0.f && (pos[a] < ext[a] - 1 || wrap)) {
+                            const long long q = pos[a] < ext[a] - 1 ? i + st[a] : i - st[a] * (ext[a] - 1);
                             Dx += u * (m[q] - mx) * inv[a];
                             Dy += u * (m[n + q] - my) * inv[a];
                             Dz += u * (m[2 * n + q] - mz) * inv[a];

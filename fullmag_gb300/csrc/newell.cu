@@ -18,6 +18,7 @@
 // kernel, with no padded complex array and no FP64 FFT.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -274,6 +275,185 @@ bool newell_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double 
 bool newell_spectrum_gpu64(const Grid &g, double dx, double dy, double dz, double ms, double *kern, cudaStream_t s,
                            std::string &err) {
     return newell_build(g, dx, dy, dz, ms, nullptr, kern, s, err);
+}
+
+}  // namespace fm
+
+// ---- periodic boundaries: truncated image sums (fdm_fft.rs:140-233, 614-717) ----
+namespace fm {
+namespace {
+
+// Open-boundary tensor component values at the signed offset (i, j, k) cells: the
+// first-octant value at (|i|, |j|, |k|) (table stencil or point-dipole asymptotics, the
+// criterion on the absolute offsets) with the parity sign of each off-diagonal
+// component (newell.rs:393-425).  The f/g table covers offsets up to kAsym + 1.
+__device__ void open_tensor_at(const double *T, int sx, int sy, long long tl, int i, int j, int k, double dx, double dy,
+                               double dz, double vol, double inv4piv, double v[6]) {
+    const int ai = i < 0 ? -i : i, aj = j < 0 ? -j : j, ak = k < 0 ? -k : k;
+    const long long d2 = (long long)ai * ai + (long long)aj * aj + (long long)ak * ak;
+    if (ai >= kAsym || aj >= kAsym || ak >= kAsym || d2 >= (long long)kAsym * kAsym) {
+        const double x = ai * dx, y = aj * dy, z = ak * dz;
+        v[0] = asym_diag(x, y, z, vol);
+        v[1] = asym_diag(y, x, z, vol);
+        v[2] = asym_diag(z, y, x, vol);
+        v[3] = asym_off(x, y, z, vol);
+        v[4] = asym_off(x, z, y, vol);
+        v[5] = asym_off(y, z, x, vol);
+    } else {
+#pragma unroll 1
+        for (int c = 0; c < 6; ++c) v[c] = stencil27(T + c * tl, ai, aj, ak, sx, sy, inv4piv);
+    }
+    const double sxg = i < 0 ? -1.0 : 1.0, syg = j < 0 ? -1.0 : 1.0, szg = k < 0 ? -1.0 : 1.0;
+    v[3] *= sxg * syg;
+    v[4] *= sxg * szg;
+    v[5] *= syg * szg;
+}
+
+struct PerAxis {
+    int n, p, images, periodic;
+};
+
+// Signed offset of padded index i on an open axis, or a flag for the empty gap.
+__device__ __forceinline__ bool open_offset(const PerAxis &a, int i, int &o) {
+    if (i < a.n) {
+        o = i;
+        return true;
+    }
+    if (i > a.p - a.n) {
+        o = i - a.p;
+        return true;
+    }
+    return false;
+}
+
+// S[c][k][j][i] over the padded grid (px, py, qz): on a periodic axis index i stands for
+// the offsets i + m n, |m| <= I, summed image by image in the order z, y, x (outer to
+// inner); on an open axis for its one signed offset.  qz = 1 on the thin-film path
+// (the z = 0 plane, with z images when z is periodic).
+__global__ void periodic_tensor_kernel(double *S, const double *T, int sx, int sy, long long tl, PerAxis ax, PerAxis ay,
+                                       PerAxis az, int qz, double dx, double dy, double dz) {
+    const long long len = (long long)ax.p * ay.p * qz;
+    const double vol = dx * dy * dz, inv = 1.0 / (4.0 * M_PI * vol);
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < len; id += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(id % ax.p);
+        const int j = (int)((id / ax.p) % ay.p);
+        const int k = (int)(id / ((long long)ax.p * ay.p));
+        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        int oi = i, oj = j, ok = k;
+        const bool live = (ax.periodic || open_offset(ax, i, oi)) && (ay.periodic || open_offset(ay, j, oj)) &&
+                          (az.periodic || qz == 1 || open_offset(az, k, ok));
+        if (live) {
+            const int iz = az.periodic ? az.images : 0, iy = ay.periodic ? ay.images : 0, ix = ax.periodic ? ax.images : 0;
+            for (int mz = -iz; mz <= iz; ++mz)
+                for (int my = -iy; my <= iy; ++my)
+                    for (int mx = -ix; mx <= ix; ++mx) {
+                        double v[6];
+                        open_tensor_at(T, sx, sy, tl, oi + mx * ax.n, oj + my * ay.n, ok + mz * az.n, dx, dy, dz, vol, inv, v);
+                        for (int c = 0; c < 6; ++c) acc[c] += v[c];
+                    }
+        }
+        for (int c = 0; c < 6; ++c) S[c * len + id] = acc[c];
+    }
+}
+
+// Direct complex DFT along one axis of layout [comp][outer][axis][inner], e^{-2 pi i k a / p}:
+// real input (in_re, imaginary part zero) or complex input (in_c); nout outputs.
+__global__ void dft_axis_kernel(const double *__restrict__ in_re, const double2 *__restrict__ in_c,
+                                double2 *__restrict__ out, int ncomp, int outer, int p, int nout, int inner,
+                                const double2 *__restrict__ tw) {
+    const long long per_out = (long long)outer * nout * inner;
+    const long long total = per_out * ncomp;
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(id / per_out);
+        long long r = id - c * per_out;
+        const int b = (int)(r % inner);
+        r /= inner;
+        const int kk = (int)(r % nout);
+        const int o = (int)(r / nout);
+        const long long base = (((long long)c * outer + o) * p) * inner + b;
+        double re = 0.0, im = 0.0;
+        int e = 0;  // (kk * a) mod p
+        for (int a = 0; a < p; ++a) {
+            const double2 w = tw[e];  // cos, sin of 2 pi e / p
+            if (in_c) {
+                const double2 v = in_c[base + (long long)a * inner];
+                re += v.x * w.x + v.y * w.y;
+                im += v.y * w.x - v.x * w.y;
+            } else {
+                const double v = in_re[base + (long long)a * inner];
+                re += v * w.x;
+                im -= v * w.y;
+            }
+            e += kk;
+            if (e >= p) e -= p;
+        }
+        out[(((long long)c * outer + o) * nout + kk) * inner + b] = make_double2(re, im);
+    }
+}
+
+__global__ void to_float2_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, long long total, double scale) {
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x)
+        out[id] = make_float2((float)(in[id].x * scale), (float)(in[id].y * scale));
+}
+
+}  // namespace
+
+bool newell_periodic_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, const uint32_t images[3],
+                                  float2 *kern, cudaStream_t s, std::string &err) {
+    const int per = g.per;
+    const PerAxis ax{g.nx, g.px, (int)images[0], (per & 1) ? 1 : 0};
+    const PerAxis ay{g.ny, g.py, (int)images[1], (per & 2) ? 1 : 0};
+    const PerAxis az{g.nz, g.thin ? 1 : g.pz, (int)images[2], (per & 4) ? 1 : 0};
+    const int qz = g.thin ? 1 : g.pz;
+    const int ncomp = g.thin ? 4 : 6;
+    // f/g table over the offsets the sums reach (at most the asymptotic distance)
+    auto reach = [](const PerAxis &a) { return a.periodic ? (long long)a.n * (2LL * a.images + 1) : (long long)a.n; };
+    const int sx = (int)std::min<long long>(reach(ax), kAsym) + 2, sy = (int)std::min<long long>(reach(ay), kAsym) + 2,
+              sz = (int)std::min<long long>(reach(az), kAsym) + 2;
+    const long long tl = (long long)sx * sy * sz;
+    const long long len = (long long)g.px * g.py * qz;
+    std::vector<double2> tw;
+    std::vector<size_t> off;
+    for (int p : {g.px, g.py, qz}) {
+        off.push_back(tw.size());
+        for (int e = 0; e < p; ++e) {
+            const double a = 2.0 * M_PI * (double)e / (double)p;
+            tw.push_back(make_double2(cos(a), sin(a)));
+        }
+    }
+    const long long nA = (long long)6 * qz * g.py * g.nkx;  // after x
+    double *T = nullptr, *S = nullptr;
+    double2 *A = nullptr, *B = nullptr, *dtw = nullptr;
+    bool ok = ck(cudaMalloc(&T, sizeof(double) * 6 * tl), "cudaMalloc(newell table)", err) &&
+              ck(cudaMalloc(&S, sizeof(double) * 6 * len), "cudaMalloc(periodic tensor)", err) &&
+              ck(cudaMalloc(&A, sizeof(double2) * nA), "cudaMalloc(periodic x)", err) &&
+              ck(cudaMalloc(&B, sizeof(double2) * nA), "cudaMalloc(periodic y)", err) &&
+              ck(cudaMalloc(&dtw, sizeof(double2) * tw.size()), "cudaMalloc(periodic twiddles)", err);
+    if (ok) ok = ck(cudaMemcpyAsync(dtw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice, s), "twiddle copy", err);
+    if (ok) {
+        fg_table_kernel<<<grid_for(tl), 256, 0, s>>>(T, sx, sy, sz, dx, dy, dz);
+        periodic_tensor_kernel<<<grid_for(len), 256, 0, s>>>(S, T, sx, sy, tl, ax, ay, az, qz, dx, dy, dz);
+        // x: [c][(k,j)][i] real -> [c][(k,j)][kx < nkx]
+        dft_axis_kernel<<<grid_for(nA), 256, 0, s>>>(S, nullptr, A, 6, qz * g.py, g.px, g.nkx, 1, dtw + off[0]);
+        // y: [c][k][j][kx] -> [c][k][ky][kx]
+        dft_axis_kernel<<<grid_for(nA), 256, 0, s>>>(nullptr, A, B, 6, qz, g.py, g.py, g.nkx, dtw + off[1]);
+        const double2 *R = B;
+        if (qz > 1) {
+            // z: [c][k][(ky,kx)] -> [c][kz][(ky,kx)]
+            dft_axis_kernel<<<grid_for(nA), 256, 0, s>>>(nullptr, B, A, 6, 1, qz, qz, g.py * g.nkx, dtw + off[2]);
+            R = A;
+        }
+        // components xx yy zz xy (xz yz) are the first ncomp blocks of R, scaled by Ms / P
+        const double scale = ms / ((double)g.px * g.py * qz);
+        to_float2_kernel<<<grid_for(nA), 256, 0, s>>>(R, kern, (long long)ncomp * qz * g.py * g.nkx, scale);
+        ok = ck(cudaGetLastError(), "periodic newell kernels", err) && ck(cudaStreamSynchronize(s), "periodic newell sync", err);
+    }
+    cudaFree(T);
+    cudaFree(S);
+    cudaFree(A);
+    cudaFree(B);
+    cudaFree(dtw);
+    return ok;
 }
 
 }  // namespace fm

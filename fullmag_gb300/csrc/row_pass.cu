@@ -264,12 +264,14 @@ __device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, 
                 for (int j = 0; j < V; ++j) m0v[c][j] = cc[j];
                 if (M.ex_pref != 0.f) {
                     float ym[V], yp[V], zm[V], zp[V], xm[V], xp[V];
-                    ldv<V>(mc + i0 - (y > 0 ? nx : 0), ym);
-                    ldv<V>(mc + i0 + (y < ny - 1 ? nx : 0), yp);
-                    ldv<V>(mc + i0 - (z > 0 ? plane : 0), zm);
-                    ldv<V>(mc + i0 + (z < nz - 1 ? plane : 0), zp);
-                    xm[0] = x0 > 0 ? mc[i0 - 1] : cc[0];
-                    xp[V - 1] = x0 + V < nx ? mc[i0 + V] : cc[V - 1];
+                    // open axes clamp (Neumann), periodic axes wrap around
+                    const int per = g.per;
+                    ldv<V>(mc + i0 + (y > 0 ? -nx : (per & 2) ? plane - nx : 0), ym);
+                    ldv<V>(mc + i0 + (y < ny - 1 ? nx : (per & 2) ? nx - plane : 0), yp);
+                    ldv<V>(mc + i0 + (z > 0 ? -(long long)plane : (per & 4) ? (long long)plane * (nz - 1) : 0), zm);
+                    ldv<V>(mc + i0 + (z < nz - 1 ? (long long)plane : (per & 4) ? -(long long)plane * (nz - 1) : 0), zp);
+                    xm[0] = x0 > 0 ? mc[i0 - 1] : (per & 1) ? mc[i0 + nx - 1] : cc[0];
+                    xp[V - 1] = x0 + V < nx ? mc[i0 + V] : (per & 1) ? mc[i0 + V - nx] : cc[V - 1];
 #pragma unroll
                     for (int j = 1; j < V; ++j) {
                         xm[j] = cc[j - 1];
@@ -533,13 +535,15 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
             float e_pair = 0.f;
             if (act) {
                 if (M.ex_pref != 0.f) {
+                    // open axes clamp (Neumann), periodic axes wrap around (fdm_types.rs:126-132)
                     long long nb[6];
-                    nb[0] = x > 0 ? i - 1 : i;
-                    nb[1] = x < nx - 1 ? i + 1 : i;
-                    nb[2] = y > 0 ? i - nx : i;
-                    nb[3] = y < g.ny - 1 ? i + nx : i;
-                    nb[4] = z > 0 ? i - (long long)nx * g.ny : i;
-                    nb[5] = z < g.nz - 1 ? i + (long long)nx * g.ny : i;
+                    const long long pl = (long long)nx * g.ny;
+                    nb[0] = x > 0 ? i - 1 : (g.per & 1) ? i + nx - 1 : i;
+                    nb[1] = x < nx - 1 ? i + 1 : (g.per & 1) ? i - (nx - 1) : i;
+                    nb[2] = y > 0 ? i - nx : (g.per & 2) ? i + pl - nx : i;
+                    nb[3] = y < g.ny - 1 ? i + nx : (g.per & 2) ? i - pl + nx : i;
+                    nb[4] = z > 0 ? i - pl : (g.per & 4) ? i + pl * (g.nz - 1) : i;
+                    nb[5] = z < g.nz - 1 ? i + pl : (g.per & 4) ? i - pl * (g.nz - 1) : i;
                     if (p.mask) {
 #pragma unroll
                         for (int q = 0; q < 6; ++q)
@@ -565,7 +569,7 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
                     if (p.partials) {
                         // forward pairs only (x+1, y+1, z+1), each active pair once
                         const float w[3] = {M.idx2, M.idy2, M.idz2};
-                        const bool has[3] = {x < nx - 1, y < g.ny - 1, z < g.nz - 1};
+                        const bool has[3] = {x < nx - 1 || (g.per & 1), y < g.ny - 1 || (g.per & 2), z < g.nz - 1 || (g.per & 4)};
 #pragma unroll
                         for (int a = 0; a < 3; ++a) {
                             const int q = 2 * a + 1;

@@ -444,6 +444,27 @@ void fullmag_fdm_batch_destroy(fullmag_fdm_batch *batch);
 int fullmag_fdm_backend_upload_magnetization_f64_noalloc(fullmag_fdm_backend *handle, const double *m_xyz,
                                                          uint64_t len);
 
+/* ---- Periodic boundaries (additive) ----
+ * The reference carries periodicity only into its Rust CPU engine: per-axis open /
+ * periodic policy (crates/fullmag-engine/src/fdm_types.rs:84-117, FdmBoundaryPolicy,
+ * fed from FdmPeriodicityIR by crates/fullmag-runner/src/cpu_reference.rs:272-285) and
+ * the demag image counts (fdm_problem.rs:19-23, default 10 per axis).  On a periodic
+ * axis the exchange, DMI and Zhang-Li stencils wrap around (fdm_types.rs:126-132,
+ * fdm_fields.rs:109-160,356-445,1253-1340), the FFT extent is the cell count (no zero padding)
+ * and the demag tensor is the truncated image sum N(i) = sum_{|m| <= I} N_open(i + m n)
+ * for i in [0, n) (fdm_fft.rs:140-233,614-717), whose spectrum is complex.  This entry
+ * point is fullmag_fdm_backend_create with that policy added.  Single-precision state
+ * only; the backend builds the tensor itself, so the plan must carry no demag spectra;
+ * a periodic x extent must be even. */
+typedef struct fullmag_fdm_periodicity_desc {
+    uint32_t periodic[3];       /* x, y, z: 0 open, 1 periodic */
+    uint32_t has_image_counts;  /* 0: 10 images on every periodic axis */
+    uint32_t image_counts[3];   /* images on each side along a periodic axis */
+} fullmag_fdm_periodicity_desc;
+
+fullmag_fdm_backend *fullmag_fdm_backend_create_periodic(const fullmag_fdm_plan_desc *plan,
+                                                         const fullmag_fdm_periodicity_desc *periodicity);
+
 #ifdef __cplusplus
 }
 #endif

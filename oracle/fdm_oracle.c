@@ -213,6 +213,105 @@ int fo_newell_kernels(int nx, int ny, int nz, double dx, double dy, double dz, d
     return 0;
 }
 
+/* Open-boundary tensor at a signed offset (i, j, k) cells: first-octant value at the
+ * absolute offsets (stencil on the f/g table, or the asymptotic form past the asymptotic
+ * distance) with the parity signs of the octant placement (newell.rs:356-425). */
+typedef struct {
+    const double *tab;  /* six tables of sx*sy*sz values, offsets -1 .. s-2 */
+    int sx, sy, sz;
+    long flen;
+    double dx, dy, dz, vol;
+} newell_ctx;
+
+static int newell_ctx_init(newell_ctx *c, long rx, long ry, long rz, double dx, double dy, double dz) {
+    const int AD = FO_ASYMPTOTIC_DISTANCE;
+    c->sx = (int)((rx < AD ? rx : AD) + 2);
+    c->sy = (int)((ry < AD ? ry : AD) + 2);
+    c->sz = (int)((rz < AD ? rz : AD) + 2);
+    c->flen = (long)c->sx * c->sy * c->sz;
+    c->dx = dx, c->dy = dy, c->dz = dz, c->vol = dx * dy * dz;
+    double *t = (double *)malloc(sizeof(double) * 6 * (size_t)c->flen);
+    if (!t) return -2;
+    const long flen = c->flen;
+#pragma omp parallel for schedule(dynamic)
+    for (int cc = 0; cc < c->sz; ++cc)
+        for (int b = 0; b < c->sy; ++b)
+            for (int a = 0; a < c->sx; ++a) {
+                const double x = (a - 1) * dx, y = (b - 1) * dy, z = (cc - 1) * dz;
+                const long id = (long)cc * c->sy * c->sx + (long)b * c->sx + a;
+                t[id] = fo_newell_f(x, y, z);
+                t[flen + id] = fo_newell_f(y, x, z);
+                t[2 * flen + id] = fo_newell_f(z, y, x);
+                t[3 * flen + id] = fo_newell_g(x, y, z);
+                t[4 * flen + id] = fo_newell_g(x, z, y);
+                t[5 * flen + id] = fo_newell_g(y, z, x);
+            }
+    c->tab = t;
+    return 0;
+}
+
+static void newell_at(const newell_ctx *c, long i, long j, long k, double v[6]) {
+    const long ai = i < 0 ? -i : i, aj = j < 0 ? -j : j, ak = k < 0 ? -k : k;
+    const long AD = FO_ASYMPTOTIC_DISTANCE;
+    if (ai >= AD || aj >= AD || ak >= AD || ai * ai + aj * aj + ak * ak >= AD * AD) {
+        const double x = ai * c->dx, y = aj * c->dy, z = ak * c->dz;
+        v[0] = asym_diag(x, y, z, c->vol);
+        v[1] = asym_diag(y, x, z, c->vol);
+        v[2] = asym_diag(z, y, x, c->vol);
+        v[3] = asym_off(x, y, z, c->vol);
+        v[4] = asym_off(x, z, y, c->vol);
+        v[5] = asym_off(y, z, x, c->vol);
+    } else {
+        for (int q = 0; q < 6; ++q) v[q] = stencil27((int)ai, (int)aj, (int)ak, c->tab + q * c->flen, c->sx, c->sy, c->vol);
+    }
+    const double sx = i < 0 ? -1.0 : 1.0, sy = j < 0 ? -1.0 : 1.0, sz = k < 0 ? -1.0 : 1.0;
+    v[3] *= sx * sy;
+    v[4] *= sx * sz;
+    v[5] *= sy * sz;
+}
+
+int fo_periodic_newell_kernels(int nx, int ny, int nz, double dx, double dy, double dz, const int32_t periodic[3],
+                               const uint32_t images[3], double *out) {
+    if (nx <= 0 || ny <= 0 || nz <= 0) return -1;
+    const int n3[3] = {nx, ny, nz};
+    int pd[3], im[3];
+    long reach[3];
+    for (int a = 0; a < 3; ++a) {
+        pd[a] = periodic[a] ? n3[a] : 2 * n3[a];
+        im[a] = periodic[a] ? (int)images[a] : 0;
+        reach[a] = (long)n3[a] * (1 + 2 * (long)im[a]);
+    }
+    newell_ctx c;
+    if (newell_ctx_init(&c, reach[0], reach[1], reach[2], dx, dy, dz)) return -2;
+    const long plen = (long)pd[0] * pd[1] * pd[2];
+#pragma omp parallel for schedule(dynamic)
+    for (long id = 0; id < plen; ++id) {
+        const long i = id % pd[0], j = (id / pd[0]) % pd[1], k = id / ((long)pd[0] * pd[1]);
+        const long idx3[3] = {i, j, k};
+        long off[3] = {0, 0, 0};
+        int live = 1;
+        for (int a = 0; a < 3; ++a) {
+            /* open axis: index i < n is the offset i, i > n the offset i - 2n, i == n empty */
+            if (periodic[a]) off[a] = idx3[a];
+            else if (idx3[a] < n3[a]) off[a] = idx3[a];
+            else if (idx3[a] > n3[a]) off[a] = idx3[a] - pd[a];
+            else live = 0;
+        }
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        if (live)
+            for (int mz = -im[2]; mz <= im[2]; ++mz)
+                for (int my = -im[1]; my <= im[1]; ++my)
+                    for (int mx = -im[0]; mx <= im[0]; ++mx) {
+                        double v[6];
+                        newell_at(&c, off[0] + (long)mx * nx, off[1] + (long)my * ny, off[2] + (long)mz * nz, v);
+                        for (int q = 0; q < 6; ++q) acc[q] += v[q];
+                    }
+        for (int q = 0; q < 6; ++q) out[q * plen + id] = acc[q];
+    }
+    free((void *)c.tab);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Mixed-radix FFT (own implementation; stands in for rustfft 6.4.1)          */
 /* ------------------------------------------------------------------------- */
@@ -688,7 +787,28 @@ fo_problem *fo_create(const fo_params *p, const double *m0_aos) {
     pr->c3[0] = pr->c1[1] * pr->c2[2] - pr->c1[2] * pr->c2[1];
     pr->c3[1] = pr->c1[2] * pr->c2[0] - pr->c1[0] * pr->c2[2];
     pr->c3[2] = pr->c1[0] * pr->c2[1] - pr->c1[1] * pr->c2[0];
-    if (p->enable_demag) {
+    const int any_periodic = p->periodic[0] || p->periodic[1] || p->periodic[2];
+    if (p->enable_demag && any_periodic) {
+        /* FftWorkspace::new_with_boundary (fdm_fft.rs:140-233): periodic axes unpadded, the
+         * truncated image-sum tensor transformed by the full complex 3-D FFT */
+        pr->px = p->periodic[0] ? p->nx : 2 * p->nx;
+        pr->py = p->periodic[1] ? p->ny : 2 * p->ny;
+        pr->pz = p->periodic[2] ? p->nz : 2 * p->nz;
+        pr->P = (long)pr->px * pr->py * pr->pz;
+        double *real = dalloc(6 * pr->P);
+        if (!real || fo_periodic_newell_kernels(p->nx, p->ny, p->nz, p->dx, p->dy, p->dz, p->periodic, p->image_counts, real)) {
+            free(real);
+            fo_destroy(pr);
+            return NULL;
+        }
+        for (int c = 0; c < 6; ++c) {
+            pr->kern[c] = dalloc(2 * pr->P);
+            for (long i = 0; i < pr->P; ++i) pr->kern[c][2 * i] = real[c * pr->P + i];
+            fo_fft3d(pr->kern[c], pr->px, pr->py, pr->pz, 0);
+        }
+        free(real);
+        for (int c = 0; c < 3; ++c) { pr->bm[c] = dalloc(2 * pr->P); pr->bh[c] = dalloc(2 * pr->P); }
+    } else if (p->enable_demag) {
         pr->px = 2 * p->nx; pr->py = 2 * p->ny; pr->pz = 2 * p->nz;
         pr->P = (long)pr->px * pr->py * pr->pz;
         double *sp = dalloc(12 * pr->P);
@@ -735,6 +855,20 @@ int fo_set_field_map(fo_problem *pr, const double *h_aos) {
 }
 
 /* exchange_field_add_into (fdm_fields.rs:445-527), Neumann clamp (fdm_types.rs:126-132). */
+/* x-, x+, y-, y+, z-, z+ neighbours of cell i: clamped to the cell on an open axis
+ * (Neumann), wrapped around on a periodic one (neighbor_index, fdm_types.rs:126-132). */
+static void axis_neighbours(const fo_params *p, long i, long nb[6]) {
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
+    const long sxy = (long)nx * ny;
+    nb[0] = x > 0 ? i - 1 : (p->periodic[0] ? i + nx - 1 : i);
+    nb[1] = x < nx - 1 ? i + 1 : (p->periodic[0] ? i - (nx - 1) : i);
+    nb[2] = y > 0 ? i - nx : (p->periodic[1] ? i + sxy - nx : i);
+    nb[3] = y < ny - 1 ? i + nx : (p->periodic[1] ? i - sxy + nx : i);
+    nb[4] = z > 0 ? i - sxy : (p->periodic[2] ? i + sxy * (nz - 1) : i);
+    nb[5] = z < nz - 1 ? i + sxy : (p->periodic[2] ? i - sxy * (nz - 1) : i);
+}
+
 static void exchange_add(const fo_problem *pr, const double *m, double *h) {
     const fo_params *p = &pr->p;
     const double pref = 2.0 * p->a_ex / (FO_MU0 * p->ms);
@@ -745,12 +879,7 @@ static void exchange_add(const fo_problem *pr, const double *m, double *h) {
         if (!active(pr, i)) continue;
         const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
         long nb[6];
-        nb[0] = i - (x > 0 ? 1 : 0);
-        nb[1] = i + (x < nx - 1 ? 1 : 0);
-        nb[2] = i - (y > 0 ? nx : 0);
-        nb[3] = i + (y < ny - 1 ? nx : 0);
-        nb[4] = i - (z > 0 ? (long)nx * ny : 0);
-        nb[5] = i + (z < nz - 1 ? (long)nx * ny : 0);
+        axis_neighbours(p, i, nb);
         for (int q = 0; q < 6; ++q)
             if (!active(pr, nb[q])) nb[q] = i;
         if (p->boundary_tier > 0) {
@@ -914,16 +1043,7 @@ static void rhs_cell(const fo_params *p, const double *m, const double *h, doubl
 /* Neighbours x-, x+, y-, y+, z-, z+ of cell i with the Neumann clamp and the active mask
  * (a missing or inactive neighbour is the cell itself; demag_fp32.cu:324-340). */
 static void clamped_neighbours(const fo_problem *pr, long i, long nb[6]) {
-    const fo_params *p = &pr->p;
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
-    const long sxy = (long)nx * ny;
-    nb[0] = x > 0 ? i - 1 : i;
-    nb[1] = x < nx - 1 ? i + 1 : i;
-    nb[2] = y > 0 ? i - nx : i;
-    nb[3] = y < ny - 1 ? i + nx : i;
-    nb[4] = z > 0 ? i - sxy : i;
-    nb[5] = z < nz - 1 ? i + sxy : i;
+    axis_neighbours(&pr->p, i, nb);
     for (int q = 0; q < 6; ++q)
         if (!active(pr, nb[q])) nb[q] = i;
 }
@@ -1057,11 +1177,13 @@ static void torque_add(const fo_problem *pr, const double *m, long i, double *k)
         double D[3] = {0, 0, 0};
         for (int a = 0; a < 3; ++a) {
             const double u = pr->zl_u[a];
-            if (u > 0.0 && pos[a] > 0) {
-                const double *q = m + 3 * (i - stride[a]);
+            /* a periodic axis always has the upwind neighbour, wrapped (fdm_fields.rs:1288-1320) */
+            const int wrap = p->periodic[a] != 0;
+            if (u > 0.0 && (pos[a] > 0 || wrap)) {
+                const double *q = m + 3 * (pos[a] > 0 ? i - stride[a] : i + stride[a] * (ext[a] - 1));
                 for (int c = 0; c < 3; ++c) D[c] += u * (mi[c] - q[c]) * inv[a];
-            } else if (u < 0.0 && pos[a] < ext[a] - 1) {
-                const double *q = m + 3 * (i + stride[a]);
+            } else if (u < 0.0 && (pos[a] < ext[a] - 1 || wrap)) {
+                const double *q = m + 3 * (pos[a] < ext[a] - 1 ? i + stride[a] : i - stride[a] * (ext[a] - 1));
                 for (int c = 0; c < 3; ++c) D[c] += u * (q[c] - mi[c]) * inv[a];
             }
         }
@@ -1156,7 +1278,6 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
                      const double *h_eff, const double *rhs, fo_stats *st) {
     const fo_params *p = &pr->p;
     const double V = p->dx * p->dy * p->dz;
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
     const double ix2 = 1.0 / (p->dx * p->dx), iy2 = 1.0 / (p->dy * p->dy), iz2 = 1.0 / (p->dz * p->dz);
     double epair = 0.0, exf = 0.0, ed = 0.0, eext = 0.0, euni = 0.0, ecub = 0.0, eacpu = 0.0, edmi = 0.0;
 #pragma omp parallel for reduction(+ : epair, exf, ed, eext, euni, ecub, eacpu, edmi) schedule(static)
@@ -1164,12 +1285,14 @@ static void energies(fo_problem *pr, const double *m, const double *h_ex, const 
         if (!active(pr, i)) continue;
         const double *mi = m + 3 * i;
         edmi += V * dmi_energy_cell(pr, m, i);
-        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long)nx * ny));
         if (p->enable_exchange) {
-            long nb[3] = {x + 1 < nx ? i + 1 : -1, y + 1 < ny ? i + nx : -1, z + 1 < nz ? i + (long)nx * ny : -1};
+            /* forward pairs; on a periodic axis the last cell pairs with the first */
+            long all[6];
+            axis_neighbours(p, i, all);
+            long nb[3] = {all[1], all[3], all[5]};
             const double w[3] = {ix2, iy2, iz2};
             for (int q = 0; q < 3; ++q) {
-                if (nb[q] < 0 || !active(pr, nb[q])) continue;
+                if (nb[q] == i || !active(pr, nb[q])) continue;
                 const double a = m[3 * nb[q]] - mi[0], b = m[3 * nb[q] + 1] - mi[1], c = m[3 * nb[q] + 2] - mi[2];
                 const double A = pr->region ? pr->lut[pr->region[i] * FO_MAX_REGIONS + pr->region[nb[q]]] : p->a_ex;
                 epair += A * V * phi_w(pr, i) * (a * a + b * b + c * c) * w[q];
@@ -1583,8 +1706,54 @@ int fo_tangent_rk4(fo_problem *pr, double dt, uint64_t n_steps, const double *dh
 }
 
 /* Direct real-space sum H_i = -sum_j N(r_i - r_j) Ms m_j over the padded tensor. */
+static int demag_direct_periodic(fo_problem *pr, const double *m_aos, double *h_demag) {
+    const fo_params *p = &pr->p;
+    const int n3[3] = {p->nx, p->ny, p->nz};
+    int im[3];
+    long reach[3];
+    for (int a = 0; a < 3; ++a) {
+        im[a] = p->periodic[a] ? (int)p->image_counts[a] : 0;
+        reach[a] = (long)n3[a] * (1 + 2 * (long)im[a]);
+    }
+    newell_ctx c;
+    if (newell_ctx_init(&c, reach[0], reach[1], reach[2], p->dx, p->dy, p->dz)) return -2;
+    const long n = pr->n;
+#pragma omp parallel for schedule(dynamic)
+    for (long i = 0; i < n; ++i) {
+        double h[3] = {0, 0, 0};
+        if (active(pr, i)) {
+            const long pi[3] = {i % p->nx, (i / p->nx) % p->ny, i / ((long)p->nx * p->ny)};
+            for (long j = 0; j < n; ++j) {
+                if (!active(pr, j)) continue;
+                const long pj[3] = {j % p->nx, (j / p->nx) % p->ny, j / ((long)p->nx * p->ny)};
+                long d[3];
+                for (int a = 0; a < 3; ++a) {
+                    d[a] = pi[a] - pj[a];
+                    if (p->periodic[a] && d[a] < 0) d[a] += n3[a];  /* offset modulo n, in [0, n) */
+                }
+                double K[6] = {0, 0, 0, 0, 0, 0};
+                for (int mz = -im[2]; mz <= im[2]; ++mz)
+                    for (int my = -im[1]; my <= im[1]; ++my)
+                        for (int mx = -im[0]; mx <= im[0]; ++mx) {
+                            double v[6];
+                            newell_at(&c, d[0] + (long)mx * p->nx, d[1] + (long)my * p->ny, d[2] + (long)mz * p->nz, v);
+                            for (int q = 0; q < 6; ++q) K[q] += v[q];
+                        }
+                const double Mx = p->ms * m_aos[3 * j], My = p->ms * m_aos[3 * j + 1], Mz = p->ms * m_aos[3 * j + 2];
+                h[0] -= K[0] * Mx + K[3] * My + K[4] * Mz;
+                h[1] -= K[3] * Mx + K[1] * My + K[5] * Mz;
+                h[2] -= K[4] * Mx + K[5] * My + K[2] * Mz;
+            }
+        }
+        for (int q = 0; q < 3; ++q) h_demag[3 * i + q] = h[q];
+    }
+    free((void *)c.tab);
+    return 0;
+}
+
 int fo_demag_direct(fo_problem *pr, const double *m_aos, double *h_demag) {
     const fo_params *p = &pr->p;
+    if (p->periodic[0] || p->periodic[1] || p->periodic[2]) return demag_direct_periodic(pr, m_aos, h_demag);
     const int nx = p->nx, ny = p->ny, nz = p->nz, px = 2 * nx, py = 2 * ny, pz = 2 * nz;
     const long plen = (long)px * py * pz;
     double *kr = dalloc(6 * plen);

@@ -109,6 +109,11 @@ typedef struct {
     const int32_t *corr_source_idx;
     const double *corr_tensor;
     uint32_t corr_targets, corr_stencil;
+    /* periodic boundaries of the reference CPU engine (crates/fullmag-engine/src/fdm_types.rs:84-132,
+     * fdm_problem.rs:19-23): per axis 0 open, 1 periodic, and the demag images on each side
+     * of a periodic axis (the reference default is 10) */
+    int32_t periodic[3];
+    uint32_t image_counts[3];
 } fo_params;
 
 #define FO_MAX_REGIONS 256
@@ -149,7 +154,15 @@ int fo_step(fo_problem *pr, double dt, fo_stats *st);
  * anisotropy (not differentiated). */
 int fo_tangent_rk4(fo_problem *pr, double dt, uint64_t n_steps, const double *dh_aos, const double *dm0_aos,
                    double *dm_out);
-/* Demag field by direct O(N^2) real-space Newell sum (FFT-independent check). */
+/* Spatial truncated-image tensor of a grid with periodic axes (fdm_fft.rs:614-717): six
+ * real arrays over (px, py, pz), px = nx on a periodic axis and 2 nx on an open one, entry
+ * (i, j, k) = sum over |m_a| <= images_a on periodic axes of the open tensor at offset
+ * (i + m_x nx, ...), open axes at their one signed offset; images summed z, y, x (outer
+ * to inner).  Components xx yy zz xy xz yz, each px*py*pz values. */
+int fo_periodic_newell_kernels(int nx, int ny, int nz, double dx, double dy, double dz, const int32_t periodic[3],
+                               const uint32_t images[3], double *out);
+/* Demag field by direct O(N^2) real-space Newell sum (FFT-independent check); with
+ * periodic axes the offset along each is taken modulo n and summed over the images. */
 int fo_demag_direct(fo_problem *pr, const double *m_aos, double *h_demag);
 
 int fo_num_threads(void);

@@ -66,6 +66,7 @@ class Params(C.Structure):
         ("volume_fraction", C.c_void_p), ("face", C.c_void_p * 6), ("delta", C.c_void_p * 6),
         ("corr_target_idx", C.c_void_p), ("corr_source_idx", C.c_void_p), ("corr_tensor", C.c_void_p),
         ("corr_targets", C.c_uint32), ("corr_stencil", C.c_uint32),
+        ("periodic", C.c_int32 * 3), ("image_counts", C.c_uint32 * 3),
     ]
 
 
@@ -94,6 +95,8 @@ def lib():
         L.fo_newell_g.argtypes = [C.c_double] * 3
         L.fo_newell_kernels.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [dp]
         L.fo_newell_spectra.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int, dp]
+        L.fo_periodic_newell_kernels.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [
+            C.POINTER(C.c_int32), C.POINTER(C.c_uint32), dp]
         L.fo_fft1d.argtypes = [dp, C.c_int, C.c_int]
         L.fo_fft3d.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.fo_create.restype = C.c_void_p
@@ -133,6 +136,18 @@ def newell_kernels(nx, ny, nz, dx, dy, dz):
     rc = lib().fo_newell_kernels(nx, ny, nz, dx, dy, dz, _dp(out))
     assert rc == 0
     return out.reshape(6, 2 * nz, 2 * ny, 2 * nx)
+
+
+def periodic_newell_kernels(nx, ny, nz, dx, dy, dz, periodic, images):
+    """Truncated-image tensors of a grid with periodic axes, shape (6, pz, py, px) with
+    p = n on a periodic axis and 2n on an open one: xx yy zz xy xz yz."""
+    pd = [n if per else 2 * n for n, per in zip((nx, ny, nz), periodic)]
+    out = np.zeros(6 * pd[0] * pd[1] * pd[2])
+    per = (C.c_int32 * 3)(*[int(bool(v)) for v in periodic])
+    img = (C.c_uint32 * 3)(*[int(v) for v in images])
+    rc = lib().fo_periodic_newell_kernels(nx, ny, nz, dx, dy, dz, per, img, _dp(out))
+    assert rc == 0
+    return out.reshape(6, pd[2], pd[1], pd[0])
 
 
 def newell_spectra(nx, ny, nz, dx, dy, dz, thin_film_2d=False):
@@ -175,7 +190,7 @@ class Problem:
                  ku1_field=None, ku2_field=None, kc1_field=None, kc2_field=None, kc3_field=None,
                  oersted_current=None, oersted_radius=0.0, oersted_center=(0.0, 0.0, 0.0), oersted_kind=0,
                  oersted_freq=0.0, oersted_phase=0.0, oersted_offset=0.0, oersted_t_on=0.0, oersted_t_off=0.0,
-                 temperature=0.0, thermal_seed=42, boundary=None):
+                 temperature=0.0, thermal_seed=42, boundary=None, periodic=None, image_counts=None):
         p = Params()
         p.nx, p.ny, p.nz, p.integrator = nx, ny, nz, integrator
         p.dx, p.dy, p.dz = dx, dy, dz
@@ -217,6 +232,9 @@ class Problem:
         p.oersted_kind, p.oersted_freq, p.oersted_phase = oersted_kind, oersted_freq, oersted_phase
         p.oersted_offset, p.oersted_t_on, p.oersted_t_off = oersted_offset, oersted_t_on, oersted_t_off
         p.temperature, p.thermal_seed = temperature, thermal_seed
+        # periodic axes (x, y, z flags) and demag images per periodic axis (default 10)
+        p.periodic[:] = [int(bool(v)) for v in (periodic or (0, 0, 0))]
+        p.image_counts[:] = [int(v) for v in (image_counts if image_counts is not None else (10, 10, 10))]
         self._kmaps = {}
         for name, arr in (("ku1_field", ku1_field), ("ku2_field", ku2_field), ("kc1_field", kc1_field),
                           ("kc2_field", kc2_field), ("kc3_field", kc3_field)):
