@@ -99,8 +99,8 @@ def row_pass_bytes_per_launch(integrator, nx, ny, nz, demag=True):
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
 # the timed steps of each workload
-NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 457.4e6, ("volume_256x256x64_rk4", "y_inverse"): 274.0e6,
-               ("volume_256x256x64_rk4", "y_forward"): 242.6e6, ("volume_256x256x64_rk4", "row_pass"): 307.4e6,
+NCU_TRAFFIC = {("volume_256x256x64_rk4", "z_convolve"): 453.0e6, ("volume_256x256x64_rk4", "y_inverse"): 270.3e6,
+               ("volume_256x256x64_rk4", "y_forward"): 241.1e6, ("volume_256x256x64_rk4", "row_pass"): 377.8e6,
                # the extra-field pass's stage launch
                ("volume_256x256x64_rk4_allterms", "extra_field"): 189.1e6}
 # the column passes of the all-terms volume are the same launches on the same grid as the
