@@ -30,7 +30,8 @@ def _c_offsets(tmp_path, struct_name, ctype):
 @pytest.mark.parametrize("sname,ctype", [
     ("fullmag_fdm_plan_desc", _abi.PlanDesc), ("fullmag_fdm_step_stats", _abi.StepStats),
     ("fullmag_fdm_device_info", _abi.DeviceInfo), ("fullmag_fdm_snapshot_desc", _abi.SnapshotDesc),
-    ("fullmag_fdm_grid_desc", _abi.GridDesc), ("fullmag_fdm_material_desc", _abi.MaterialDesc)])
+    ("fullmag_fdm_grid_desc", _abi.GridDesc), ("fullmag_fdm_material_desc", _abi.MaterialDesc),
+    ("fullmag_fdm_periodicity_desc", _abi.PeriodicityDesc)])
 def test_struct_layout_matches_c(tmp_path, sname, ctype):
     off = _c_offsets(tmp_path, sname, ctype)
     assert off.pop("sizeof") == C.sizeof(ctype)
@@ -76,6 +77,7 @@ def test_null_safety_without_gpu():
     from fullmag_gb300 import load_library
     lib = load_library()
     assert lib.fullmag_fdm_backend_create(None) is None
+    assert lib.fullmag_fdm_backend_create_periodic(None, None) is None
     lib.fullmag_fdm_backend_destroy(None)
     lib.fullmag_fdm_field_snapshot_destroy(None)
     lib.fullmag_fdm_preview_snapshot_destroy(None)
