@@ -2283,7 +2283,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     if (demag) {
         if (g.per) {
             std::string err;
-            if (!newell_periodic_spectrum_gpu(g, dx, dy, dz, ms, images, reinterpret_cast<float2 *>(kern), stream, err)) {
+            if (!newell_periodic_spectrum_gpu(g, dx, dy, dz, ms, images, reinterpret_cast<float2 *>(kern), nullptr, stream, err)) {
                 last_error = err;
                 return false;
             }
@@ -2645,10 +2645,6 @@ fullmag_fdm_backend *fullmag_fdm_backend_create_periodic(const fullmag_fdm_plan_
             return reinterpret_cast<fullmag_fdm_backend *>(e);
         }
     }
-    if (plan->precision == FULLMAG_FDM_PRECISION_DOUBLE) {
-        e->last_error = "periodic boundaries are available with single-precision state (use SINGLE)";
-        return reinterpret_cast<fullmag_fdm_backend *>(e);
-    }
     for (int a = 0; a < 3; ++a) {
         if (periodicity->periodic[a] > 1) {
             e->last_error = "periodic[] entries must be 0 (open) or 1 (periodic)";
@@ -2662,6 +2658,12 @@ fullmag_fdm_backend *fullmag_fdm_backend_create_periodic(const fullmag_fdm_plan_
             }
             e->images[a] = periodicity->image_counts[a];
         }
+    }
+    if (plan->precision == FULLMAG_FDM_PRECISION_DOUBLE) {
+        std::string err;
+        e->f64 = fp64_create(plan, err, e->per_req, e->images);
+        if (!e->f64) e->last_error = err;
+        return reinterpret_cast<fullmag_fdm_backend *>(e);
     }
     if (!e->setup(plan)) return reinterpret_cast<fullmag_fdm_backend *>(e);
     if (!e->upload<double>(plan->initial_magnetization_xyz)) return reinterpret_cast<fullmag_fdm_backend *>(e);

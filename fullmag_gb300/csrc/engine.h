@@ -154,9 +154,10 @@ cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s);     // Y -> X  (
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s); // X -> X  (thin film)
 cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s);  // X -> X (small 3-D, uses plan2 for z)
 size_t yz_convolve_smem(const Grid &g, int tx);
-// The truncated-image periodic kernel (layout above) of a grid with g.per != 0
+// The truncated-image periodic kernel (layout above) of a grid with g.per != 0, as FP32
+// (kern) or FP64 (kern64) complex values; exactly one of the two is non-null
 bool newell_periodic_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, const uint32_t images[3],
-                                  float2 *kern, cudaStream_t s, std::string &err);
+                                  float2 *kern, double2 *kern64, cudaStream_t s, std::string &err);
 // K[c][kz][ky][kx] -> K[c][kz][kx][ky] (the fused y+z path's layout), out of place
 cudaError_t launch_kern_ky_fast(const float *in, float *out, int ncomp, int nkz, int nky, int nkx, cudaStream_t s);
 size_t z_convolve_smem(const Grid &g, int tx);

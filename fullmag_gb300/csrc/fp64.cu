@@ -126,7 +126,8 @@ struct Conv64 {
     int nx, ny, nz, px, py, pz, nkx, nky, nkz, thin;
     long long n;
     Plan64 plx, ply, plz;
-    const double *kern;  // octant kernel scaled by Ms / P
+    const double *kern;    // octant kernel scaled by Ms / P
+    const double2 *kernc;  // periodic grids: complex kernel K[c][kz][ky][kx] (full ky, kz), else NULL
 };
 
 // row (y, z) and component c: phi m along x, zero padded to px -> X[c][row][kx < nkx]
@@ -193,8 +194,28 @@ __global__ void y_inverse64(const Conv64 C, const double2 *__restrict__ Y, doubl
     for (int y = threadIdx.x; y < C.ny; y += blockDim.x) dst[(long long)y * C.nkx] = r[y];
 }
 
-// H(k) = -N(k) M(k) on three lines a[0..2] at (kx, ky, kz) of the octant kernel
+__device__ __forceinline__ double2 zmadd(double2 k, double2 m, double2 acc) {
+    return make_double2(acc.x + k.x * m.x - k.y * m.y, acc.y + k.x * m.y + k.y * m.x);
+}
+
+// H(k) = -N(k) M(k) on three lines a[0..2] at (kx, ky, kz) of the octant kernel, or of the
+// complex kernel of a periodic grid (components xx yy zz xy xz yz; 2-D: the first four)
 __device__ __forceinline__ void multiply3(const Conv64 &C, double2 *mx, double2 *my, double2 *mz, int kx, int ky, int kz) {
+    if (C.kernc) {
+        const long long kc = (long long)C.pz * C.py * C.nkx;
+        const double2 *K = C.kernc + ((long long)kz * C.py + ky) * C.nkx + kx;
+        const double2 z0 = make_double2(0.0, 0.0);
+        const double2 kxx = K[0], kyy = K[kc], kzz = K[2 * kc], kxy = K[3 * kc];
+        const double2 kxz = C.thin ? z0 : K[4 * kc], kyz = C.thin ? z0 : K[5 * kc];
+        const double2 a = *mx, b = *my, d = *mz;
+        const double2 hx = zmadd(kxz, d, zmadd(kxy, b, zmadd(kxx, a, z0)));
+        const double2 hy = zmadd(kyz, d, zmadd(kyy, b, zmadd(kxy, a, z0)));
+        const double2 hz = zmadd(kzz, d, zmadd(kyz, b, zmadd(kxz, a, z0)));
+        *mx = make_double2(-hx.x, -hx.y);
+        *my = make_double2(-hy.x, -hy.y);
+        *mz = make_double2(-hz.x, -hz.y);
+        return;
+    }
     int kym, kzm;
     double sy, sz;
     mirror(ky, C.py, kym, sy);
@@ -307,6 +328,7 @@ struct Field64 {
     const double *delta[6];
     double phi_floor, delta_min;
     int exchange;
+    int per;                  // periodic axes (bit 0 x, 1 y, 2 z): neighbours wrap around
     double a_ex, ms, dx, dy, dz;
     int has_ext;
     double hext[3];
@@ -331,9 +353,11 @@ __device__ void exchange64(const Field64 &P, long long i, int x, int y, int z, d
     const double c0[3] = {m[i], m[n + i], m[2 * n + i]};
     const int ri = P.region ? P.region[i] : 0;
     if (P.tier == 0) {
-        // clamped neighbours: out of range or inactive -> the centre (no contribution)
+        // clamped neighbours: out of range or inactive -> the centre (no contribution); on a
+        // periodic axis the neighbour wraps around (fdm_types.rs:126-132)
+        const int ext[3] = {P.nx, P.ny, P.nz};
         for (int q = 0; q < 6; ++q) {
-            long long j = has[q] ? i + off[q] : i;
+            long long j = has[q] ? i + off[q] : ((P.per >> (q >> 1)) & 1) ? i - off[q] * (ext[q >> 1] - 1) : i;
             if (P.mask && P.mask[j] == 0) j = i;
             if (j == i) continue;
             const double w = (P.region ? P.lut[ri * FULLMAG_FDM_MAX_EXCHANGE_REGIONS + P.region[j]] : P.a_ex) * inv2[q];
@@ -378,12 +402,16 @@ __device__ double exchange_pairs64(const Field64 &P, long long i, int x, int y, 
     const long long n = P.n, nxy = (long long)P.nx * P.ny;
     const bool has[3] = {x + 1 < P.nx, y + 1 < P.ny, z + 1 < P.nz};
     const long long off[3] = {1, P.nx, nxy};
+    const int ext[3] = {P.nx, P.ny, P.nz};
     const double inv2[3] = {1.0 / (P.dx * P.dx), 1.0 / (P.dy * P.dy), 1.0 / (P.dz * P.dz)};
     const int ri = P.region ? P.region[i] : 0;
     double e = 0.0;
     for (int a = 0; a < 3; ++a) {
-        if (!has[a]) continue;
-        const long long j = i + off[a];
+        // forward pairs; on a periodic axis the last cell pairs with the first
+        const bool wrap = !has[a] && ((P.per >> a) & 1);
+        if (!has[a] && !wrap) continue;
+        const long long j = has[a] ? i + off[a] : i - off[a] * (ext[a] - 1);
+        if (j == i) continue;
         if (P.mask && P.mask[j] == 0) continue;
         if (P.phi && !(P.phi[j] > 0.0)) continue;
         const double A = P.region ? P.lut[ri * FULLMAG_FDM_MAX_EXCHANGE_REGIONS + P.region[j]] : P.a_ex;
@@ -599,6 +627,8 @@ struct Fp64Engine {
     double max_error = 1e-5, dt_min = 1e-18, dt_max = 1e-10, headroom = 0.8;
     int tier = 0;
     double phi_floor = 0.0, delta_min = 0.0;
+    int per = 0;                     // periodic axes (bit 0 x, 1 y, 2 z)
+    uint32_t images[3] = {10, 10, 10};
     bool has_mask = false;
     std::vector<uint8_t> mask_host;
     uint32_t corr_targets = 0, corr_stencil = 0;
@@ -616,6 +646,7 @@ struct Fp64Engine {
     Conv64 conv{};
     double2 *X = nullptr, *Y = nullptr;
     double *kern = nullptr;
+    double2 *kernc = nullptr;  // periodic grids: the complex image-sum kernel
     double2 *twid = nullptr;
     // state
     int cur = 0;
@@ -703,6 +734,7 @@ struct Fp64Engine {
         P.phi_floor = phi_floor;
         P.delta_min = delta_min;
         P.exchange = exchange;
+        P.per = per;
         P.a_ex = a_ex;
         P.ms = ms;
         P.dx = dx;
@@ -1047,6 +1079,8 @@ bool Fp64Engine::setup(const fullmag_fdm_plan_desc *plan) {
     }
     phi_floor = plan->boundary_phi_floor;
     delta_min = plan->boundary_delta_min;
+    if (per && (tier > 0 || (plan->has_demag_boundary_corr && plan->demag_corr_target_count > 0)))
+        return err = "boundary correction is not available with periodic boundaries", false;
     if (plan->has_demag_boundary_corr && plan->demag_corr_target_count > 0) {
         if (!plan->demag_corr_target_idx || !plan->demag_corr_source_idx || !plan->demag_corr_tensor ||
             plan->demag_corr_stencil_size == 0)
@@ -1122,8 +1156,12 @@ bool Fp64Engine::setup(const fullmag_fdm_plan_desc *plan) {
         C.ny = ny;
         C.nz = nz;
         C.n = n;
-        C.px = 2 * nx;
-        C.py = 2 * ny;
+        // periodic axes (fdm_fft.rs:140-160): unpadded, and the backend builds the tensor
+        C.px = (per & 1) ? nx : 2 * nx;
+        C.py = (per & 2) ? ny : 2 * ny;
+        if (per && plan->demag_kernel_spectrum_len != 0)
+            return err = "periodic boundaries: the backend builds the image-sum demag tensor, the plan must carry no spectra",
+                   false;
         const uint64_t len3 = 2ull * (uint64_t)(2 * nx) * (2 * ny) * (2 * nz);
         const uint64_t len2 = 2ull * (uint64_t)(2 * nx) * (2 * ny);
         const bool given = plan->demag_kernel_spectrum_len != 0;
@@ -1142,7 +1180,7 @@ bool Fp64Engine::setup(const fullmag_fdm_plan_desc *plan) {
                        false;
         }
         C.thin = thin;
-        C.pz = thin ? 1 : 2 * nz;
+        C.pz = thin ? 1 : (per & 4) ? nz : 2 * nz;
         C.nkx = C.px / 2 + 1;
         C.nky = C.py / 2 + 1;
         C.nkz = C.pz / 2 + 1;
@@ -1156,8 +1194,8 @@ bool Fp64Engine::setup(const fullmag_fdm_plan_desc *plan) {
         C.ply.tw = twid + off[1];
         if (!thin) C.plz.tw = twid + off[2];
         const int ncomp = thin ? 4 : 6;
-        const size_t per = (size_t)C.nkz * C.nky * C.nkx;
-        if (!alloc(kern, ncomp * per)) return false;
+        const size_t kper = per ? (size_t)C.pz * C.py * C.nkx : (size_t)C.nkz * C.nky * C.nkx;
+        if (per ? !alloc(kernc, ncomp * kper) : !alloc(kern, ncomp * kper)) return false;
         if (!alloc(X, 3 * (size_t)nz * ny * C.nkx)) return false;
         if (!thin && !alloc(Y, 3 * (size_t)nz * C.py * C.nkx)) return false;
         const size_t smz = sizeof(double2) * 6 * std::max(C.pz, thin ? C.py : 1);
@@ -1172,13 +1210,13 @@ bool Fp64Engine::setup(const fullmag_fdm_plan_desc *plan) {
             const double *src[6] = {plan->demag_kernel_xx_spectrum, plan->demag_kernel_yy_spectrum, plan->demag_kernel_zz_spectrum,
                                     plan->demag_kernel_xy_spectrum, plan->demag_kernel_xz_spectrum, plan->demag_kernel_yz_spectrum};
             const double scale = ms / ((double)C.px * C.py * C.pz);
-            std::vector<double> h(ncomp * per);
+            std::vector<double> h(ncomp * kper);
             for (int c = 0; c < ncomp; ++c)
                 for (int kz = 0; kz < C.nkz; ++kz)
                     for (int ky = 0; ky < C.nky; ++ky)
                         for (int kx = 0; kx < C.nkx; ++kx) {
                             const size_t s = (size_t)kx + (size_t)C.px * (ky + (size_t)C.py * kz);
-                            h[(size_t)c * per + ((size_t)kz * C.nky + ky) * C.nkx + kx] = src[c][2 * s] * scale;
+                            h[(size_t)c * kper + ((size_t)kz * C.nky + ky) * C.nkx + kx] = src[c][2 * s] * scale;
                         }
             if (fail("cudaMemcpy(kernel)", cudaMemcpyAsync(kern, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, stream)) ||
                 fail("kernel sync", cudaStreamSynchronize(stream)))
@@ -1197,9 +1235,13 @@ bool Fp64Engine::setup(const fullmag_fdm_plan_desc *plan) {
             g.nky = C.nky;
             g.nkz = C.nkz;
             g.thin = thin;
-            if (!newell_spectrum_gpu64(g, dx, dy, dz, ms, kern, stream, err)) return false;
+            g.per = per;
+            if (per ? !newell_periodic_spectrum_gpu(g, dx, dy, dz, ms, images, nullptr, kernc, stream, err)
+                    : !newell_spectrum_gpu64(g, dx, dy, dz, ms, kern, stream, err))
+                return false;
         }
         C.kern = kern;
+        C.kernc = kernc;
     }
     return true;
 }
@@ -1217,12 +1259,15 @@ bool Fp64Engine::upload(const double *m_xyz) {
 
 bool fp64_refresh(Fp64Engine *e, std::string &err);
 
-Fp64Engine *fp64_create(const fullmag_fdm_plan_desc *plan, std::string &err) {
+Fp64Engine *fp64_create(const fullmag_fdm_plan_desc *plan, std::string &err, int periodic, const uint32_t *images) {
     Fp64Engine *e = new (std::nothrow) Fp64Engine();
     if (!e) {
         err = "out of host memory";
         return nullptr;
     }
+    e->per = periodic;
+    if (images)
+        for (int a = 0; a < 3; ++a) e->images[a] = images[a];
     if (!e->setup(plan) || !e->upload(plan->initial_magnetization_xyz)) {
         err = e->err;
         delete e;

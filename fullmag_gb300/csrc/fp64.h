@@ -16,7 +16,10 @@ struct Fp64Engine;
 
 // Validates the plan, builds the engine on the current device and evaluates the initial
 // state.  nullptr and a message in err when the plan is rejected or a CUDA call fails.
-Fp64Engine *fp64_create(const fullmag_fdm_plan_desc *plan, std::string &err);
+// periodic: axes with periodic boundaries (bit 0 x, 1 y, 2 z), images: demag images per
+// periodic axis.
+Fp64Engine *fp64_create(const fullmag_fdm_plan_desc *plan, std::string &err, int periodic = 0,
+                        const uint32_t *images = nullptr);
 void fp64_destroy(Fp64Engine *e);
 // One accepted step (the adaptive integrators retry internally, as the FP32 path does).
 // Returns a FULLMAG_FDM_* code; interrupted steps leave the state untouched.

@@ -391,15 +391,18 @@ __global__ void dft_axis_kernel(const double *__restrict__ in_re, const double2 
     }
 }
 
-__global__ void to_float2_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, long long total, double scale) {
-    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x)
-        out[id] = make_float2((float)(in[id].x * scale), (float)(in[id].y * scale));
+__global__ void scale_complex_kernel(const double2 *__restrict__ in, float2 *__restrict__ out32, double2 *__restrict__ out64,
+                                     long long total, double scale) {
+    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
+        if (out64) out64[id] = make_double2(in[id].x * scale, in[id].y * scale);
+        else out32[id] = make_float2((float)(in[id].x * scale), (float)(in[id].y * scale));
+    }
 }
 
 }  // namespace
 
 bool newell_periodic_spectrum_gpu(const Grid &g, double dx, double dy, double dz, double ms, const uint32_t images[3],
-                                  float2 *kern, cudaStream_t s, std::string &err) {
+                                  float2 *kern, double2 *kern64, cudaStream_t s, std::string &err) {
     const int per = g.per;
     const PerAxis ax{g.nx, g.px, (int)images[0], (per & 1) ? 1 : 0};
     const PerAxis ay{g.ny, g.py, (int)images[1], (per & 2) ? 1 : 0};
@@ -445,7 +448,7 @@ bool newell_periodic_spectrum_gpu(const Grid &g, double dx, double dy, double dz
         }
         // components xx yy zz xy (xz yz) are the first ncomp blocks of R, scaled by Ms / P
         const double scale = ms / ((double)g.px * g.py * qz);
-        to_float2_kernel<<<grid_for(nA), 256, 0, s>>>(R, kern, (long long)ncomp * qz * g.py * g.nkx, scale);
+        scale_complex_kernel<<<grid_for(nA), 256, 0, s>>>(R, kern, kern64, (long long)ncomp * qz * g.py * g.nkx, scale);
         ok = ck(cudaGetLastError(), "periodic newell kernels", err) && ck(cudaStreamSynchronize(s), "periodic newell sync", err);
     }
     cudaFree(T);

@@ -453,9 +453,10 @@ int fullmag_fdm_backend_upload_magnetization_f64_noalloc(fullmag_fdm_backend *ha
  * fdm_fields.rs:109-160,356-445,1253-1340), the FFT extent is the cell count (no zero padding)
  * and the demag tensor is the truncated image sum N(i) = sum_{|m| <= I} N_open(i + m n)
  * for i in [0, n) (fdm_fft.rs:140-233,614-717), whose spectrum is complex.  This entry
- * point is fullmag_fdm_backend_create with that policy added.  Single-precision state
- * only; the backend builds the tensor itself, so the plan must carry no demag spectra;
- * a periodic x extent must be even. */
+ * point is fullmag_fdm_backend_create with that policy added, for single- and
+ * double-precision state.  The backend builds the tensor itself, so the plan must carry
+ * no demag spectra; with single-precision state a periodic x extent must be even; the
+ * boundary-correction tiers are not combined with periodic axes. */
 typedef struct fullmag_fdm_periodicity_desc {
     uint32_t periodic[3];       /* x, y, z: 0 open, 1 periodic */
     uint32_t has_image_counts;  /* 0: 10 images on every periodic axis */

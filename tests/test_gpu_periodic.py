@@ -110,11 +110,44 @@ def test_error_paths(gpu_lib, oracle):
     with pytest.raises(FdmError, match="even"):
         FdmBackend(**kw, integrator=_abi.INTEGRATOR_HEUN, periodic=(1, 0, 0))
     kw = problem(8, 8, 2, seed=76)
-    with pytest.raises(FdmError, match="single-precision"):
-        FdmBackend(**kw, integrator=_abi.INTEGRATOR_HEUN, periodic=(0, 1, 0), precision=_abi.PRECISION_DOUBLE)
     sp = oracle.newell_spectra(8, 8, 2, kw["dx"], kw["dy"], kw["dz"])
     with pytest.raises(FdmError, match="no spectra"):
         FdmBackend(**kw, integrator=_abi.INTEGRATOR_HEUN, periodic=(0, 1, 0), spectra=sp)
+    with pytest.raises(FdmError, match="no spectra"):
+        FdmBackend(**kw, integrator=_abi.INTEGRATOR_HEUN, periodic=(0, 1, 0), spectra=sp,
+                   precision=_abi.PRECISION_DOUBLE)
+    with pytest.raises(FdmError, match="boundary correction"):
+        FdmBackend(**kw, integrator=_abi.INTEGRATOR_HEUN, periodic=(1, 0, 0), precision=_abi.PRECISION_DOUBLE,
+                   boundary={"tier": _abi.BOUNDARY_VOLUME, "volume_fraction": np.ones(8 * 8 * 2),
+                             "face": [np.ones(8 * 8 * 2)] * 6})
     gpu = FdmBackend(**kw, integrator=_abi.INTEGRATOR_RK4, periodic=(0, 1, 0), image_counts=(0, 1, 0))
     with pytest.raises(FdmError, match="periodic"):
         gpu.adjoint_forward(1e-13, 4)
+
+
+@pytest.mark.parametrize("shape,periodic,images", [
+    ((24, 16, 1), (1, 1, 0), (3, 3, 0)),
+    ((12, 10, 6), (0, 1, 1), (0, 2, 1)),
+    ((9, 8, 3), (1, 0, 0), (2, 0, 0)),      # odd periodic x: the FP64 transforms take any length
+    ((8, 6, 5), (1, 1, 1), (1, 1, 1)),
+])
+def test_double_precision_periodic(gpu_lib, oracle, shape, periodic, images):
+    # the double-precision path against the FP64 oracle: both compute in FP64; the tensor is
+    # built on the GPU, whose f/g evaluations (log1p, atan) differ from the host's by an
+    # ulp that the 27-point second difference amplifies, so the bound is the one of the
+    # GPU-built FP64 tensor elsewhere: 1e-9 relative L2
+    nx, ny, nz = shape
+    kw = problem(nx, ny, nz, seed=78, ku1=4e4, u_axis=(0.3, 0.2, 1.0))
+    orc = oracle.Problem(**kw, integrator=oracle.RK4, periodic=periodic, image_counts=images)
+    gpu = FdmBackend(**kw, integrator=_abi.INTEGRATOR_RK4, periodic=periodic, image_counts=images,
+                     precision=_abi.PRECISION_DOUBLE)
+    ref = orc.fields(kw["m0"])
+    assert rel_l2(gpu.copy_field(_abi.OBSERVABLE_H_DEMAG), ref["h_demag"]) < 1e-9
+    assert rel_l2(gpu.copy_field(_abi.OBSERVABLE_H_EFF), ref["h_eff"]) < 1e-9
+    st, ost = gpu.stats(), orc.observe()
+    assert abs(st["exchange_energy_joules"] - ost["e_exchange"]) <= 1e-9 * abs(ost["e_exchange"])
+    assert abs(st["demag_energy_joules"] - ost["e_demag"]) <= 1e-9 * abs(ost["e_demag"])
+    for _ in range(20):
+        gpu.step(1e-13)
+        orc.step(1e-13)
+    assert np.abs(gpu.copy_field(_abi.OBSERVABLE_M) - orc.get_m()).max() < 1e-9
