@@ -254,7 +254,7 @@ __device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, 
             // h in the scalar loop's order; m.h_d, |h_d|^2 and the forward-pair |dm|^2
             // accumulate across the components (clamped neighbours give zero differences,
             // so the last cell of a row / column / plane needs no mask)
-            float m0v[3][V], hv[3][V], e_pair[V], dd[V], dn[V];
+            float m0v[3][V], hv[3][V], e_pair[V];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const float *mc = p.m_in + c * n;
@@ -313,8 +313,6 @@ __device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, 
                     if (M.has_ext) h += M.hext[c];
                     if (p.hmap) h += hm[j];
                     hv[c][j] = h;
-                    dd[j] = c ? dd[j] + cc[j] * dv[j] : cc[j] * dv[j];
-                    dn[j] = c ? dn[j] + dv[j] * dv[j] : dv[j] * dv[j];
                 }
                 if (p.h_ex_out) stv<V>(p.h_ex_out + c * n + i0, ex);
                 if (p.h_d_out) stv<V>(p.h_d_out + c * n + i0, dv);
@@ -357,8 +355,17 @@ __device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, 
                 kv[1][j] = -M.gbar * (M.prec * py_ + M.alpha * qy);
                 kv[2][j] = -M.gbar * (M.prec * pz_ + M.alpha * qz);
                 if (p.partials) {
+                    // H_d of this cell again from shared memory (no registers held across the loop)
+                    float dx_ = 0.f, dy_ = 0.f, dz_ = 0.f;
+                    if (hd) {
+                        const int h = sk((x0 + j) >> 1);
+                        const float2 a = hd[(rr * 3 + 0) * lsx + h], b = hd[(rr * 3 + 1) * lsx + h], d = hd[(rr * 3 + 2) * lsx + h];
+                        dx_ = (j & 1) ? a.y : a.x;
+                        dy_ = (j & 1) ? b.y : b.x;
+                        dz_ = (j & 1) ? d.y : d.x;
+                    }
                     ff_add(sum_hi[0], sum_lo[0], e_pair[j]);
-                    ff_add(sum_hi[1], sum_lo[1], dd[j]);
+                    ff_add(sum_hi[1], sum_lo[1], m0x * dx_ + m0y * dy_ + m0z * dz_);
                     if (M.has_ext) ff_add(sum_hi[2], sum_lo[2], m0x * M.hext[0] + m0y * M.hext[1] + m0z * M.hext[2]);
                     if (p.hmap) {
                         const long long i = i0 + j;
@@ -367,7 +374,7 @@ __device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, 
                     ff_add(sum_hi[3], sum_lo[3], e_uni);
                     ff_add(sum_hi[V], sum_lo[V], e_cub);
                     mx2[0] = fmaxf(mx2[0], hx * hx + hy * hy + hz * hz);
-                    mx2[1] = fmaxf(mx2[1], dn[j]);
+                    mx2[1] = fmaxf(mx2[1], dx_ * dx_ + dy_ * dy_ + dz_ * dz_);
                     mx2[2] = fmaxf(mx2[2], kv[0][j] * kv[0][j] + kv[1][j] * kv[1][j] + kv[2][j] * kv[2][j]);
                 }
                 if (p.h_eff_out) {
