@@ -32,6 +32,7 @@
 #include "fft_smem.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace fm {
 
@@ -365,10 +366,22 @@ __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSum
 
 }  // namespace
 
-// 1824 CTAs, threads striding over the cells: on the 152 SMs of a GB300 that is three full
-// waves of the four-CTA-per-SM instances (no region exchange) and four of the three-CTA
-// region instances
-int extra_field_blocks(const Grid &g) { return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, 152 * 3 * 4); }
+// 12 CTAs per SM (1824 on the 152 SMs of a GB300), threads striding over the cells: three
+// full waves of the four-CTA-per-SM instances (no region exchange) and four of the
+// three-CTA region instances.  The SM count is read once from the current device.
+int extra_field_blocks(const Grid &g) {
+    static std::atomic<int> sms{0};
+    int k = sms.load(std::memory_order_relaxed);
+    if (k == 0) {
+        int dev = 0, v = 0;
+        k = (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+             v > 0)
+                ? v
+                : 152;
+        sms.store(k, std::memory_order_relaxed);
+    }
+    return (int)std::min<long long>((g.n + kThreads - 1) / kThreads, (long long)k * 3 * 4);
+}
 
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {
     const bool rg = p.region != nullptr, th = p.th != nullptr;
