@@ -127,6 +127,11 @@ WORKLOADS = {
     "film_512x128x1_dp45": dict(nx=512, ny=128, nz=1, d=(3.90625e-9, 3.90625e-9, 3e-9), ms=8e5, a_ex=1.3e-11,
                                 alpha=0.02, ku1=5e3, b_mt=(-24.6, 4.3, 0.0), dt=2e-13, integrator="dp45",
                                 max_error=1e-5, m0="tilt5", seed=4),
+    # thin film periodic in x and y (the reference CPU engine's periodic boundaries: unpadded
+    # transforms, the truncated image-sum demag kernel with 10 images per periodic axis)
+    "film_256x256x1_periodic_rk4": dict(nx=256, ny=256, nz=1, d=(4e-9, 4e-9, 2e-9), ms=8e5, a_ex=1.3e-11,
+                                        alpha=0.02, b_mt=(0.0, 0.0, 20.0), dt=5e-14, integrator="rk4", seed=6,
+                                        periodic=(1, 1, 0), images=(10, 10, 0)),
 }
 DEFAULT_WORKLOAD = "volume_256x256x64_rk4"
 SWEEP_WORKLOAD = "sweep_384_films_dp45"
@@ -417,6 +422,8 @@ def plan_kwargs(w):
         kw.update(ku1=w["ku1"], u_axis=(1.0, 0.0, 0.0))
     if w.get("terms") == "all":
         kw.update(extra_terms(w["nx"], w["ny"], w["nz"], d, w["seed"]))
+    if "periodic" in w:
+        kw.update(periodic=w["periodic"], image_counts=w.get("images"))
     integ = {"rk4": _abi.INTEGRATOR_RK4, "heun": _abi.INTEGRATOR_HEUN, "dp45": _abi.INTEGRATOR_DP45}[w["integrator"]]
     return kw, integ
 
@@ -824,8 +831,8 @@ def main():
         "m_norm_max_dev": float(np.abs(np.linalg.norm(m_out, axis=1) - 1).max()),
     }
     be.close()
-    # the plain path has Heun and RK4 and none of the extra-field terms
-    if not args.no_plain and w["integrator"] != "dp45" and w.get("terms") is None:
+    # the plain path has Heun and RK4, open boundaries and none of the extra-field terms
+    if not args.no_plain and w["integrator"] != "dp45" and w.get("terms") is None and "periodic" not in w:
         # the cuFFT + unfused path (reference per-step kernel structure), same workload;
         # each of its steps ends in blocking copies, so wall clock is its device time
         from fullmag_gb300.plain import PlainBaseline

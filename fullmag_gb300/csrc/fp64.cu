@@ -613,7 +613,49 @@ bool make_plan64(int n, std::vector<double2> &tw, std::vector<size_t> &off, Plan
     return true;
 }
 
+// One FP64 line of length p per CTA along an axis of layout [outer][p][inner] (real
+// input in_re with zero imaginary part, or complex c_in), forward transform
+// e^{-2 pi i k a / p}, the first nout outputs written to out[outer][nout][inner].
+__global__ void fft_axis64_kernel(const double *__restrict__ in_re, const double2 *__restrict__ c_in,
+                                  double2 *__restrict__ out, int p, int nout, int inner, const Plan64 plan) {
+    extern __shared__ double2 sm64[];
+    double2 *a = sm64, *b = sm64 + p;
+    const long long line = blockIdx.x;
+    const long long o = line / inner, q = line - o * inner;
+    const long long base = o * p * inner + q;
+    for (int i = threadIdx.x; i < p; i += blockDim.x)
+        a[i] = in_re ? make_double2(in_re[base + (long long)i * inner], 0.0) : c_in[base + (long long)i * inner];
+    __syncthreads();
+    const double2 *r = fft_line64(a, b, plan, false);
+    for (int k = threadIdx.x; k < nout; k += blockDim.x) out[(o * nout + k) * inner + q] = r[k];
+}
+
 }  // namespace
+
+bool fft64_axis(const double *in_re, const double2 *c_in, double2 *out, long long outer, int p, int nout, int inner,
+                cudaStream_t s, std::string &err) {
+    std::vector<double2> tw;
+    std::vector<size_t> off;
+    Plan64 plan;
+    if (!make_plan64(p, tw, off, plan)) return err = "FFT length has too many factors", false;
+    const size_t smem = sizeof(double2) * 2 * (size_t)p;
+    if (smem > 227 * 1024) return err = "FFT length too large for the double-precision lines", false;
+    double2 *dtw = nullptr;
+    cudaError_t e = cudaMalloc(&dtw, sizeof(double2) * tw.size());
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void *)fft_axis64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+        plan.tw = dtw;
+        const long long lines = outer * inner;
+        fft_axis64_kernel<<<(unsigned)lines, 128, smem, s>>>(in_re, c_in, out, p, nout, inner, plan);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(dtw);
+    if (e != cudaSuccess) return err = std::string("fft64_axis: ") + cudaGetErrorString(e), false;
+    return true;
+}
 
 struct Fp64Engine {
     // configuration

@@ -34,6 +34,11 @@ void fp64_grid(const Fp64Engine *e, int &nx, int &ny, int &nz);
 int fp64_device(const Fp64Engine *e);
 void fp64_fft_shape(const Fp64Engine *e, uint32_t &px, uint32_t &py, uint32_t &pz);
 
+// Forward FP64 FFT along one axis of layout [outer][p][inner] (real input in_re, or
+// complex c_in), the first nout outputs into out[outer][nout][inner]; synchronises s.
+bool fft64_axis(const double *in_re, const double2 *c_in, double2 *out, long long outer, int p, int nout, int inner,
+                cudaStream_t s, std::string &err);
+
 // GPU Newell builder with FP64 output (newell.cu)
 bool newell_spectrum_gpu64(const Grid &g, double dx, double dy, double dz, double ms, double *kern, cudaStream_t s,
                            std::string &err);

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "fp64.h"
 
 namespace fm {
 
@@ -292,13 +293,17 @@ __device__ void open_tensor_at(const double *T, int sx, int sy, long long tl, in
     const int ai = i < 0 ? -i : i, aj = j < 0 ? -j : j, ak = k < 0 ? -k : k;
     const long long d2 = (long long)ai * ai + (long long)aj * aj + (long long)ak * ak;
     if (ai >= kAsym || aj >= kAsym || ak >= kAsym || d2 >= (long long)kAsym * kAsym) {
+        // the point-dipole forms of asym_diag / asym_off with 1/r^3 and 1/r^5 formed once
+        // for the six components (the image sums evaluate millions of far offsets)
         const double x = ai * dx, y = aj * dy, z = ak * dz;
-        v[0] = asym_diag(x, y, z, vol);
-        v[1] = asym_diag(y, x, z, vol);
-        v[2] = asym_diag(z, y, x, vol);
-        v[3] = asym_off(x, y, z, vol);
-        v[4] = asym_off(x, z, y, vol);
-        v[5] = asym_off(y, z, x, vol);
+        const double r2 = x * x + y * y + z * z, r = sqrt(r2);
+        const double w = vol / (4.0 * M_PI), i3 = 1.0 / (r2 * r), i5 = i3 / r2;
+        v[0] = (i3 - 3.0 * x * x * i5) * w;
+        v[1] = (i3 - 3.0 * y * y * i5) * w;
+        v[2] = (i3 - 3.0 * z * z * i5) * w;
+        v[3] = -3.0 * x * y * i5 * w;
+        v[4] = -3.0 * x * z * i5 * w;
+        v[5] = -3.0 * y * z * i5 * w;
     } else {
 #pragma unroll 1
         for (int c = 0; c < 6; ++c) v[c] = stencil27(T + c * tl, ai, aj, ak, sx, sy, inv4piv);
@@ -356,41 +361,6 @@ __global__ void periodic_tensor_kernel(double *S, const double *T, int sx, int s
     }
 }
 
-// Direct complex DFT along one axis of layout [comp][outer][axis][inner], e^{-2 pi i k a / p}:
-// real input (in_re, imaginary part zero) or complex input (in_c); nout outputs.
-__global__ void dft_axis_kernel(const double *__restrict__ in_re, const double2 *__restrict__ in_c,
-                                double2 *__restrict__ out, int ncomp, int outer, int p, int nout, int inner,
-                                const double2 *__restrict__ tw) {
-    const long long per_out = (long long)outer * nout * inner;
-    const long long total = per_out * ncomp;
-    for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(id / per_out);
-        long long r = id - c * per_out;
-        const int b = (int)(r % inner);
-        r /= inner;
-        const int kk = (int)(r % nout);
-        const int o = (int)(r / nout);
-        const long long base = (((long long)c * outer + o) * p) * inner + b;
-        double re = 0.0, im = 0.0;
-        int e = 0;  // (kk * a) mod p
-        for (int a = 0; a < p; ++a) {
-            const double2 w = tw[e];  // cos, sin of 2 pi e / p
-            if (in_c) {
-                const double2 v = in_c[base + (long long)a * inner];
-                re += v.x * w.x + v.y * w.y;
-                im += v.y * w.x - v.x * w.y;
-            } else {
-                const double v = in_re[base + (long long)a * inner];
-                re += v * w.x;
-                im -= v * w.y;
-            }
-            e += kk;
-            if (e >= p) e -= p;
-        }
-        out[(((long long)c * outer + o) * nout + kk) * inner + b] = make_double2(re, im);
-    }
-}
-
 __global__ void scale_complex_kernel(const double2 *__restrict__ in, float2 *__restrict__ out32, double2 *__restrict__ out64,
                                      long long total, double scale) {
     for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total; id += (long long)gridDim.x * blockDim.x) {
@@ -415,47 +385,37 @@ bool newell_periodic_spectrum_gpu(const Grid &g, double dx, double dy, double dz
               sz = (int)std::min<long long>(reach(az), kAsym) + 2;
     const long long tl = (long long)sx * sy * sz;
     const long long len = (long long)g.px * g.py * qz;
-    std::vector<double2> tw;
-    std::vector<size_t> off;
-    for (int p : {g.px, g.py, qz}) {
-        off.push_back(tw.size());
-        for (int e = 0; e < p; ++e) {
-            const double a = 2.0 * M_PI * (double)e / (double)p;
-            tw.push_back(make_double2(cos(a), sin(a)));
-        }
-    }
     const long long nA = (long long)6 * qz * g.py * g.nkx;  // after x
     double *T = nullptr, *S = nullptr;
-    double2 *A = nullptr, *B = nullptr, *dtw = nullptr;
+    double2 *A = nullptr, *B = nullptr;
     bool ok = ck(cudaMalloc(&T, sizeof(double) * 6 * tl), "cudaMalloc(newell table)", err) &&
               ck(cudaMalloc(&S, sizeof(double) * 6 * len), "cudaMalloc(periodic tensor)", err) &&
               ck(cudaMalloc(&A, sizeof(double2) * nA), "cudaMalloc(periodic x)", err) &&
-              ck(cudaMalloc(&B, sizeof(double2) * nA), "cudaMalloc(periodic y)", err) &&
-              ck(cudaMalloc(&dtw, sizeof(double2) * tw.size()), "cudaMalloc(periodic twiddles)", err);
-    if (ok) ok = ck(cudaMemcpyAsync(dtw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice, s), "twiddle copy", err);
+              ck(cudaMalloc(&B, sizeof(double2) * nA), "cudaMalloc(periodic y)", err);
     if (ok) {
         fg_table_kernel<<<grid_for(tl), 256, 0, s>>>(T, sx, sy, sz, dx, dy, dz);
         periodic_tensor_kernel<<<grid_for(len), 256, 0, s>>>(S, T, sx, sy, tl, ax, ay, az, qz, dx, dy, dz);
-        // x: [c][(k,j)][i] real -> [c][(k,j)][kx < nkx]
-        dft_axis_kernel<<<grid_for(nA), 256, 0, s>>>(S, nullptr, A, 6, qz * g.py, g.px, g.nkx, 1, dtw + off[0]);
-        // y: [c][k][j][kx] -> [c][k][ky][kx]
-        dft_axis_kernel<<<grid_for(nA), 256, 0, s>>>(nullptr, A, B, 6, qz, g.py, g.py, g.nkx, dtw + off[1]);
+        ok = ck(cudaGetLastError(), "periodic newell tensor", err);
+        // FP64 FFTs: x [c][(k,j)][i] real -> [c][(k,j)][kx < nkx]; y [c][k][j][kx] ->
+        // [c][k][ky][kx]; z [c][k][(ky,kx)] -> [c][kz][(ky,kx)]
+        ok = ok && fft64_axis(S, nullptr, A, 6LL * qz * g.py, g.px, g.nkx, 1, s, err) &&
+             fft64_axis(nullptr, A, B, 6LL * qz, g.py, g.py, g.nkx, s, err);
         const double2 *R = B;
-        if (qz > 1) {
-            // z: [c][k][(ky,kx)] -> [c][kz][(ky,kx)]
-            dft_axis_kernel<<<grid_for(nA), 256, 0, s>>>(nullptr, B, A, 6, 1, qz, qz, g.py * g.nkx, dtw + off[2]);
+        if (ok && qz > 1) {
+            ok = fft64_axis(nullptr, B, A, 6, qz, qz, g.py * g.nkx, s, err);
             R = A;
         }
-        // components xx yy zz xy (xz yz) are the first ncomp blocks of R, scaled by Ms / P
-        const double scale = ms / ((double)g.px * g.py * qz);
-        scale_complex_kernel<<<grid_for(nA), 256, 0, s>>>(R, kern, kern64, (long long)ncomp * qz * g.py * g.nkx, scale);
-        ok = ck(cudaGetLastError(), "periodic newell kernels", err) && ck(cudaStreamSynchronize(s), "periodic newell sync", err);
+        if (ok) {
+            // components xx yy zz xy (xz yz) are the first ncomp blocks of R, scaled by Ms / P
+            const double scale = ms / ((double)g.px * g.py * qz);
+            scale_complex_kernel<<<grid_for(nA), 256, 0, s>>>(R, kern, kern64, (long long)ncomp * qz * g.py * g.nkx, scale);
+            ok = ck(cudaGetLastError(), "periodic newell kernels", err) && ck(cudaStreamSynchronize(s), "periodic newell sync", err);
+        }
     }
     cudaFree(T);
     cudaFree(S);
     cudaFree(A);
     cudaFree(B);
-    cudaFree(dtw);
     return ok;
 }
 
