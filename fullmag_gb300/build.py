@@ -69,7 +69,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         os.replace(tmp, out)
 
     link(LIB, [objs[s] for s in SOURCES if s in objs], ["-lcudart"])
-    link(PLAIN_LIB, [objs[s] for s in PLAIN_SOURCES if s in objs] + [objs["newell.cu"]], ["-lcufft", "-lcudart"])
+    # the plain baseline builds its tensor with newell.cu, whose periodic builder uses the
+    # FP64 line transforms of fp64.cu
+    link(PLAIN_LIB, [objs[s] for s in PLAIN_SOURCES if s in objs] + [objs["newell.cu"], objs["fp64.cu"]],
+         ["-lcufft", "-lcudart"])
     return LIB
 
 

@@ -67,6 +67,15 @@ def test_library_exports_every_declared_symbol():
     assert len(_abi.REFERENCE_SYMBOLS) == 22
 
 
+def test_libraries_resolve_every_symbol():
+    # dlopen with RTLD_NOW fails on any undefined symbol, in both the engine and the
+    # plain baseline library (which links the shared Newell builder)
+    from fullmag_gb300 import build
+    lib_path = build.build()
+    for path in (lib_path, build.PLAIN_LIB):
+        C.CDLL(str(path), mode=C.RTLD_GLOBAL | 2)  # RTLD_NOW
+
+
 def test_library_has_no_torch_dependency():
     from fullmag_gb300 import build
     out = subprocess.run(["ldd", str(build.build())], capture_output=True, text=True).stdout
