@@ -52,6 +52,8 @@ __device__ __forceinline__ void multiply_periodic(const float2 *K, size_t kc, bo
 
 // X[c][z][y<ny][kx] -> Y[c][z][ky<py][kx] (forward along y, zero rows pruned)
 __global__ void __launch_bounds__(kThreads) y_forward_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
@@ -83,6 +85,8 @@ __global__ void __launch_bounds__(kThreads) y_forward_kernel(const ColPass p) {
 
 // Y[c][z][ky][kx] -> X[c][z][y<ny][kx] (inverse along y, only physical rows kept)
 __global__ void __launch_bounds__(kThreads) y_inverse_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
@@ -131,6 +135,8 @@ __device__ __forceinline__ int ky_pair(int kya, int py, int &kyb) {
 // 3-D: for y-frequencies (ky, py-ky) and a tile of kx, forward z-transform of the
 // nz physical planes (zero-padded to pz), multiply by -N(k), inverse, keep nz planes.
 __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
     const int tx = p.tx, kx0 = blockIdx.x * tx, ncol = min(tx, g.nkx - kx0);
@@ -215,6 +221,8 @@ __global__ void __launch_bounds__(kThreads) z_convolve_kernel(const ColPass p) {
 // global memory, inner N2-point pass straight to global memory, one barrier.
 template <int N1, int N2>
 __global__ void __launch_bounds__(kThreads, 2) y_forward_fused_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     constexpr int N = N1 * N2, H1 = N1 / 2;
     constexpr int ls = skewed_len(N);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -254,6 +262,8 @@ __global__ void __launch_bounds__(kThreads, 2) y_forward_fused_kernel(const ColP
 // half-output outer pass straight to global memory, one barrier.
 template <int N1, int N2>
 __global__ void __launch_bounds__(kThreads, 2) y_inverse_fused_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     constexpr int N = N1 * N2, H1 = N1 / 2;
     constexpr int ls = skewed_len(N);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -303,6 +313,8 @@ __global__ void __launch_bounds__(kThreads, 2) y_inverse_fused_kernel(const ColP
 // straight to global memory.  Two barriers per tile, one buffer.
 template <int N1, int N2>
 __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve_fused_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     constexpr int N = N1 * N2, H1 = N1 / 2;
     constexpr int ls = skewed_len(N);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -405,6 +417,8 @@ __global__ void __launch_bounds__(kThreads, (N1 * N2 <= 128) ? 3 : 1) z_convolve
 // lane B repeats lane A and is not stored.
 template <int N1, int N2>
 __global__ void __launch_bounds__(3 * N2 * 8, 2) z_convolve_pair_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     constexpr int N = N1 * N2, H1 = N1 / 2, TX = 8;
     constexpr int ls = skewed_len(N);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -902,8 +916,16 @@ __device__ __forceinline__ void y_convolve_2d_general_body(const ColPass &p, con
     }
 }
 
-__global__ void __launch_bounds__(kThreads) yz_convolve_kernel(const ColPass p) { yz_convolve_body(p, blockIdx.x); }
-__global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p) { y_convolve_2d_body(p, blockIdx.x); }
+__global__ void __launch_bounds__(kThreads) yz_convolve_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
+    yz_convolve_body(p, blockIdx.x);
+}
+__global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
+    y_convolve_2d_body(p, blockIdx.x);
+}
 
 // One launch for many problems: work[blockIdx.x] = (problem, kx tile).  KIND (see
 // col_batched_kind): 0 thin film pruned, 1 fused y+z pruned, 2 thin film general,
@@ -998,7 +1020,9 @@ __device__ __forceinline__ void finalize_body(const float2 *__restrict__ partial
 }
 
 __global__ void __launch_bounds__(kFinThreads) finalize_stats_kernel(const float2 *__restrict__ partials, int nblocks,
-                                                                     double *__restrict__ out) {
+                                                                     double *__restrict__ out, int early) {
+    pdl_wait();
+    if (early) pdl_trigger();
     finalize_body(partials, nblocks, out);
 }
 
@@ -1036,9 +1060,8 @@ cudaError_t launch_y_fused(const ColPass &p, cudaStream_t s) {
     const void *fn = INV ? (const void *)y_inverse_fused_kernel<N1, N2> : (const void *)y_forward_fused_kernel<N1, N2>;
     cudaError_t e = ensure_smem(fn, sm);
     if (e != cudaSuccess) return e;
-    if (INV) y_inverse_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
-    else y_forward_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    if (INV) return launch_pdl(y_inverse_fused_kernel<N1, N2>, dim3(tiles(p), p.g.nz, 3), dim3(kThreads), sm, s, p);
+    return launch_pdl(y_forward_fused_kernel<N1, N2>, dim3(tiles(p), p.g.nz, 3), dim3(kThreads), sm, s, p);
 }
 // Radix split N = N1 x N2 of the two-level passes: split 0 is the default, split 1 the
 // alternative the autotuner times against it (512 has one split: a 64-point outer pass
@@ -1067,8 +1090,7 @@ cudaError_t launch_y_forward(const ColPass &p, cudaStream_t s) {
     const size_t sm = 2 * sizeof(float2) * (size_t)p.tx * skewed_len(p.g.py);
     cudaError_t e = ensure_smem((const void *)y_forward_kernel, sm);
     if (e != cudaSuccess) return e;
-    y_forward_kernel<<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(y_forward_kernel, dim3(tiles(p), p.g.nz, 3), dim3(kThreads), sm, s, p);
 }
 
 cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s) {
@@ -1076,8 +1098,7 @@ cudaError_t launch_y_inverse(const ColPass &p, cudaStream_t s) {
     const size_t sm = 2 * sizeof(float2) * (size_t)p.tx * skewed_len(p.g.py);
     cudaError_t e = ensure_smem((const void *)y_inverse_kernel, sm);
     if (e != cudaSuccess) return e;
-    y_inverse_kernel<<<dim3(tiles(p), p.g.nz, 3), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(y_inverse_kernel, dim3(tiles(p), p.g.nz, 3), dim3(kThreads), sm, s, p);
 }
 
 namespace {
@@ -1086,8 +1107,7 @@ cudaError_t launch_z_fused(const ColPass &p, cudaStream_t s) {
     const size_t sm = sizeof(float2) * (size_t)2 * 3 * p.tx * skewed_len(N1 * N2);
     cudaError_t e = ensure_smem((const void *)z_convolve_fused_kernel<N1, N2>, sm);
     if (e != cudaSuccess) return e;
-    z_convolve_fused_kernel<N1, N2><<<dim3(tiles(p), p.g.nky), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(z_convolve_fused_kernel<N1, N2>, dim3(tiles(p), p.g.nky), dim3(kThreads), sm, s, p);
 }
 // power-of-two pz with every physical plane in the lower half: the pruned fused kernel
 bool z_fused_ok(const Grid &g) {
@@ -1112,8 +1132,7 @@ cudaError_t launch_z_pair(const ColPass &p, cudaStream_t s) {
     const size_t sm = sizeof(float4) * (size_t)3 * 8 * skewed_len(N1 * N2);
     cudaError_t e = ensure_smem(fn, sm);
     if (e != cudaSuccess) return e;
-    z_convolve_pair_kernel<N1, N2><<<dim3(tiles(p), p.g.nky), 3 * N2 * 8, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(z_convolve_pair_kernel<N1, N2>, dim3(tiles(p), p.g.nky), dim3(3 * N2 * 8), sm, s, p);
 }
 }  // namespace
 
@@ -1139,8 +1158,7 @@ cudaError_t launch_z_convolve(const ColPass &p, cudaStream_t s) {
     const size_t sm = 2 * sizeof(float2) * (size_t)2 * 3 * p.tx * skewed_len(p.g.pz);
     cudaError_t e = ensure_smem((const void *)z_convolve_kernel, sm);
     if (e != cudaSuccess) return e;
-    z_convolve_kernel<<<dim3(tiles(p), p.g.nky), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(z_convolve_kernel, dim3(tiles(p), p.g.nky), dim3(kThreads), sm, s, p);
 }
 
 size_t yz_convolve_smem(const Grid &g, int tx) {
@@ -1155,8 +1173,7 @@ cudaError_t launch_yz_convolve(const ColPass &p, cudaStream_t s) {
     const size_t sm = yz_convolve_smem(p.g, p.tx);
     cudaError_t e = ensure_smem((const void *)yz_convolve_kernel, sm);
     if (e != cudaSuccess) return e;
-    yz_convolve_kernel<<<tiles(p), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(yz_convolve_kernel, dim3(tiles(p)), dim3(kThreads), sm, s, p);
 }
 
 int col_batched_kind(const Grid &g) {
@@ -1193,13 +1210,11 @@ cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s) {
     const size_t sm = y_convolve_2d_smem(p.g, p.tx);
     cudaError_t e = ensure_smem((const void *)y_convolve_2d_kernel, sm);
     if (e != cudaSuccess) return e;
-    y_convolve_2d_kernel<<<tiles(p), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(y_convolve_2d_kernel, dim3(tiles(p)), dim3(kThreads), sm, s, p);
 }
 
-cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s) {
-    finalize_stats_kernel<<<1, kFinThreads, 0, s>>>(partials, nblocks, out);
-    return cudaGetLastError();
+cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s, int early) {
+    return launch_pdl(finalize_stats_kernel, dim3(1), dim3(kFinThreads), 0, s, partials, nblocks, out, early);
 }
 
 namespace {

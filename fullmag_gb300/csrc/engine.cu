@@ -496,6 +496,9 @@ struct Engine {
     }
 
     bool use_gpu_newell = false;
+    // small fixed-step problems: each kernel lets the next one launch as soon as its own
+    // last CTAs have started (programmatic dependent launch, engine.h)
+    bool early_launch = false;
     // periodic boundary policy requested at create (bit 0 x, 1 y, 2 z) and the demag
     // image counts per axis (fdm_problem.rs:19-23,89-90)
     int per_req = 0;
@@ -535,6 +538,7 @@ struct Engine {
         p.xpost = xpost;
         p.rows = row_rows;
         p.hmap = hmap;
+        p.early = early_launch ? 1 : 0;
         return p;
     }
 
@@ -684,6 +688,7 @@ struct Engine {
         c.in = in;
         c.out = out;
         c.plan2 = plan_z;
+        c.early = early_launch ? 1 : 0;
         return c;
     }
 
@@ -772,12 +777,13 @@ struct Engine {
         if (rec_rows) return true;  // the batched round finalizes all problems at once
         launches += 1;
         kt_begin(KT_FIN);
-        const cudaError_t rc = launch_finalize_stats(partials, row_blocks, dstats, stream);
+        const cudaError_t rc = launch_finalize_stats(partials, row_blocks, dstats, stream, early_launch ? 1 : 0);
         kt_end();
         if (cuda_fail("finalize", rc)) return false;
         if (has_extra) {  // the extra pass before this evaluation left its per-CTA sums
             launches += 1;
-            if (cuda_fail("extra finalize", launch_extra_finalize(xpart, extra_field_blocks(g), dstats + kNumStats + 1, stream)))
+            if (cuda_fail("extra finalize",
+                          launch_extra_finalize(xpart, extra_field_blocks(g), dstats + kNumStats + 1, stream, early_launch ? 1 : 0)))
                 return false;
         }
         return !cuda_fail("stats copy",
@@ -1944,6 +1950,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
     g.nky = g.py / 2 + 1;
     g.nkz = g.pz / 2 + 1;
     grid_dividers(g);
+    early_launch = (integrator == FULLMAG_FDM_INTEGRATOR_HEUN || integrator == FULLMAG_FDM_INTEGRATOR_RK4) && g.n <= 65536;
 
     // ---- material constants ----
     const double mu0ms = kMu0 * ms;
@@ -1992,6 +1999,7 @@ bool Engine::setup(const fullmag_fdm_plan_desc *plan) {
 
     // DMI and magnetoelastic terms (api.cpp plan mapping; demag_fp32.cu:319-376,582-583)
     xf = ExtraField{};
+    xf.early = early_launch ? 1 : 0;
     xf.has_int = plan->has_interfacial_dmi ? 1 : 0;
     xf.has_bulk = plan->has_bulk_dmi ? 1 : 0;
     xf.has_mel = plan->has_magnetoelastic ? 1 : 0;
@@ -2369,31 +2377,39 @@ bool Engine::autotune() {
             return true;
         }
     }
+    // The fastest tile of one pass timed alone; with early launch (small fixed-step
+    // problems) the widest tile within 5 % of it: fewer CTAs of the next kernel are then
+    // resident and waiting beside the current one (measured on 256x64x1 RK4: 0.0645 ms/step
+    // with 65 thin-film CTAs against 0.0755 with 129, which timed alike on their own).
+    auto pick_tile = [&](const std::vector<std::pair<int, float>> &cand, int cur) {
+        if (cand.empty()) return cur;
+        float bt = 1e30f;
+        int best = cur;
+        for (const auto &c : cand)
+            if (c.second < bt) {
+                bt = c.second;
+                best = c.first;
+            }
+        if (early_launch)
+            for (const auto &c : cand)
+                if (c.second <= 1.05f * bt && c.first > best) best = c.first;
+        return best;
+    };
     if (demag) {
         if (g.thin) {
-            int best = tx_2d;
-            float bt = 1e30f;
+            std::vector<std::pair<int, float>> cand;
             for (int tx : {1, 2, 4, 8, 16}) {
                 if (tx > std::max(1, g.nkx) || y_convolve_2d_smem(g, tx) > 200u * 1024u) continue;
-                const float t = time_ms([&] { return launch_y_convolve_2d(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; });
-                if (t < bt) {
-                    bt = t;
-                    best = tx;
-                }
+                cand.emplace_back(tx, time_ms([&] { return launch_y_convolve_2d(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; }));
             }
-            tx_2d = best;
+            tx_2d = pick_tile(cand, tx_2d);
         } else if (use_yz) {
-            int best = tx_z;
-            float bt = 1e30f;
+            std::vector<std::pair<int, float>> cand;
             for (int tx : {1, 2, 4, 8}) {
                 if (tx > std::max(1, g.nkx) || yz_convolve_smem(g, tx) > 200u * 1024u) continue;
-                const float t = time_ms([&] { return launch_yz_convolve(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; });
-                if (t < bt) {
-                    bt = t;
-                    best = tx;
-                }
+                cand.emplace_back(tx, time_ms([&] { return launch_yz_convolve(col_pass(plan_y, tx, X, X), stream) == cudaSuccess; }));
             }
-            tx_z = best;
+            tx_z = pick_tile(cand, tx_z);
         } else {
             // tile widths and radix splits of the three column passes, each timed on its own
             // (power-of-two lengths 16..256 have a second split N1 x N2)

@@ -25,6 +25,35 @@
 
 namespace fm {
 
+// Programmatic dependent launch (sm_90 and later).  Every kernel of a step starts with
+// pdl_wait(): it returns once the grid it depends on has completed and its memory is
+// visible, so nothing it reads or writes can race the previous kernel.  With the pass's
+// `early` flag, pdl_trigger() right after lets the next kernel's CTAs be scheduled as
+// soon as this grid's last CTAs have started, so that kernel is resident and waiting
+// when this one ends instead of being launched after it.  The engine sets the flag for
+// small fixed-step problems, whose steps are a chain of sub-wave launches (measured:
+// 256x64x1 RK4 -12 %, 64x32x4 Heun -21 % per step); on the 256x256x64 volume (+2 %) and
+// the adaptive 512x128x1 film (+21 %) the early-resident CTAs cost more than they save.
+// Launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// <<<grid, block, smem, s>>>(args) with programmatic stream serialisation allowed
+template <typename... Exp, typename... Act>
+cudaError_t launch_pdl(void (*kernel)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Act &&...args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Act &&>(args)...);
+}
+
 constexpr int kNumStats = 9;  // e_ex e_d e_ext e_uni e_cub | max|Heff|^2 max|Hd|^2 max|k|^2 max err^2
 constexpr int kMaxTerms = 8;
 
@@ -111,6 +140,7 @@ struct RowPass {
     // observables
     float *h_ex_out, *h_d_out, *h_eff_out;  // NULL: not written
     int rows;                // rows per CTA
+    int early;               // let the next kernel launch early (pdl_trigger)
     // adjoint passes (launch_row_pass_adj only; see adjoint.cu for the equations); adj_mode
     // is a bit set, bit 2 runs before bit 1 at each cell:
     //   bit 2, after H_lin(lambda_H) (m_in = lambda_H, local terms off): lambda_y = adj_lam_m
@@ -142,6 +172,7 @@ struct ColPass {
     const double *skip_dt;   // batched rounds: the problem's step size; <= 0 skips its tiles
     int pipe;                // z pass: 1 = the packed ky-pair kernel (tile 8)
     int split;               // two-level passes: 0 the default radix split N1 x N2, 1 the alternative
+    int early;               // let the next kernel launch early (pdl_trigger)
 };
 
 // Launchers (kernels.cu)
@@ -231,11 +262,12 @@ struct ExtraField {
     float *h_ex_out;
     // thermal field (crates/fullmag-engine/src/fdm_fields.rs:818-896) or NULL
     const ThermalSlot *th;
+    int early;                 // let the next kernel launch early (pdl_trigger)
 };
 int extra_field_blocks(const Grid &g);
 cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s);
 // sums the per-CTA partials into out[0..4] (fixed order)
-cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s);
+cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s, int early = 0);
 
 // Adjoint (reverse-mode RK4): the final-combination pass (adjoint.cu); all fields SoA.
 // The local VJP and the stage update are the row pass's adjoint modes.
@@ -256,7 +288,7 @@ struct FinDesc {
 cudaError_t launch_row_pass_batched(const RowPass *ps, const int2 *work, int nwork, size_t smem, cudaStream_t s);
 cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, int kind, size_t smem, cudaStream_t s);
 cudaError_t launch_finalize_batched(const FinDesc *fd, int nproblems, double *out, cudaStream_t s);
-cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s);
+cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s, int early = 0);
 int row_pass_blocks(const RowPass &p);
 // Kernel of the batched column pass for a grid: 0 thin film pruned, 1 fused y+z pruned,
 // 2 thin film general, 3 fused y+z general.

@@ -97,6 +97,8 @@ __device__ __forceinline__ ExtraSums block_sum(ExtraSums v) {
 // kTh: thermal field.  The instances without them keep fewer registers.
 template <bool kNb, bool kRg, bool kTh>
 __global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(const ExtraField p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
     const Grid &g = p.g;
     const long long n = g.n;
     const float *m = p.m;
@@ -345,7 +347,9 @@ __global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(cons
 }
 
 __global__ void __launch_bounds__(kThreads) extra_finalize_kernel(const ExtraSums *__restrict__ partials, int nblocks,
-                                                                  double *__restrict__ out) {
+                                                                  double *__restrict__ out, int early) {
+    pdl_wait();
+    if (early) pdl_trigger();
     ExtraSums v{0.0, 0.0, 0.0, 0.0, 0.0};
     for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
         v.zee += partials[k].zee;
@@ -387,22 +391,19 @@ cudaError_t launch_extra_field(const ExtraField &p, cudaStream_t s) {
     const bool rg = p.region != nullptr, th = p.th != nullptr;
     const bool nb = p.has_int || p.has_bulk || (p.torques && p.has_zl);
     const dim3 grid(extra_field_blocks(p.g));
-    if (rg) {  // region exchange: the full instance (neighbours, with or without thermal)
-        if (th) extra_field_kernel<true, true, true><<<grid, kThreads, 0, s>>>(p);
-        else extra_field_kernel<true, true, false><<<grid, kThreads, 0, s>>>(p);
-    } else if (nb) {
-        if (th) extra_field_kernel<true, false, true><<<grid, kThreads, 0, s>>>(p);
-        else extra_field_kernel<true, false, false><<<grid, kThreads, 0, s>>>(p);
-    } else {
-        if (th) extra_field_kernel<false, false, true><<<grid, kThreads, 0, s>>>(p);
-        else extra_field_kernel<false, false, false><<<grid, kThreads, 0, s>>>(p);
-    }
-    return cudaGetLastError();
+    const dim3 block(kThreads);
+    if (rg)  // region exchange: the full instance (neighbours, with or without thermal)
+        return th ? launch_pdl(extra_field_kernel<true, true, true>, grid, block, 0, s, p)
+                  : launch_pdl(extra_field_kernel<true, true, false>, grid, block, 0, s, p);
+    if (nb)
+        return th ? launch_pdl(extra_field_kernel<true, false, true>, grid, block, 0, s, p)
+                  : launch_pdl(extra_field_kernel<true, false, false>, grid, block, 0, s, p);
+    return th ? launch_pdl(extra_field_kernel<false, false, true>, grid, block, 0, s, p)
+              : launch_pdl(extra_field_kernel<false, false, false>, grid, block, 0, s, p);
 }
 
-cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s) {
-    extra_finalize_kernel<<<1, kThreads, 0, s>>>(partials, nblocks, out);
-    return cudaGetLastError();
+cudaError_t launch_extra_finalize(const ExtraSums *partials, int nblocks, double *out, cudaStream_t s, int early) {
+    return launch_pdl(extra_finalize_kernel, dim3(1), dim3(kThreads), 0, s, partials, nblocks, out, early);
 }
 
 }  // namespace fm

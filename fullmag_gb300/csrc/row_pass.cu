@@ -853,7 +853,11 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 3) row_pass_kernel(const RowPass p) { row_pass_body<false>(p, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kThreads, 3) row_pass_kernel(const RowPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
+    row_pass_body<false>(p, blockIdx.x, gridDim.x);
+}
 __global__ void __launch_bounds__(kThreads) row_pass_adj_kernel(const RowPass p) { row_pass_body<true>(p, blockIdx.x, gridDim.x); }
 
 // One launch for many problems: work[blockIdx.x] = (problem, block within problem).
@@ -910,8 +914,7 @@ cudaError_t launch_row_pass(const RowPass &p, cudaStream_t s) {
     const size_t sm = row_pass_smem(p);
     cudaError_t e = ensure_smem((const void *)row_pass_kernel, sm);
     if (e != cudaSuccess) return e;
-    row_pass_kernel<<<row_pass_blocks(p), kThreads, sm, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(row_pass_kernel, dim3(row_pass_blocks(p)), dim3(kThreads), sm, s, p);
 }
 
 cudaError_t launch_row_pass_adj(const RowPass &p, cudaStream_t s) {
