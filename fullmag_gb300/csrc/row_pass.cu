@@ -463,7 +463,10 @@ __device__ __forceinline__ void cells_vec(const RowPass &p, int rows, int row0, 
 // Body of the row pass for CTA `bid` of `nblk`; shared by the single-problem kernel
 // and the batched kernel that walks a (problem, block) work table.  ADJ compiles the
 // adjoint modes (a separate kernel, so the forward kernel's registers are unaffected).
-template <bool ADJ>
+// XH = 512: the instance for x half-length 512 (px = 1024, e.g. 512-cell rows), whose
+// two-level x-transforms (32 x 16) hold 16 complex values a thread; compiled as a kernel
+// of its own so that its registers do not weigh on the other sizes.
+template <bool ADJ, int XH = 0>
 __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, const int nblk) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Grid &g = p.g;
@@ -481,9 +484,10 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
 
     // ---- (1) inverse x-transform of the demag spectrum ----
     float2 *hd = nullptr;
-    const bool fused_x = row_x_fused_ok(g);
+    const bool fused_x = XH == 512 || row_x_fused_ok(g);
     if (p.x_in && fused_x) {
-        row_inverse_x_fused(p, rows, row0, fa, fb);
+        if constexpr (XH == 512) row_inverse_x<32, 16>(p, rows, row0, fa, fb);
+        else row_inverse_x_fused(p, rows, row0, fa, fb);
         hd = fb;
     } else if (p.x_in) {
         // stage the spectrum rows in smem (batched loads), then form the half-length input
@@ -825,7 +829,8 @@ __device__ __forceinline__ void row_pass_body(const RowPass &p, const int bid, c
     // ---- (5) forward x-transform of the next stage input ----
     if (p.x_out && fused_x) {
         __syncthreads();  // every sample packed, every H_d sample of fb read
-        row_forward_x_fused(p, rows, row0, pack, fb);
+        if constexpr (XH == 512) row_forward_x<32, 16>(p, rows, row0, pack, fb);
+        else row_forward_x_fused(p, rows, row0, pack, fb);
     } else if (p.x_out) {
         // zero the padded half x in [nx, px) of every packed line
         float *pk = reinterpret_cast<float *>(pack);
@@ -857,6 +862,11 @@ __global__ void __launch_bounds__(kThreads, 3) row_pass_kernel(const RowPass p) 
     pdl_wait();
     if (p.early) pdl_trigger();
     row_pass_body<false>(p, blockIdx.x, gridDim.x);
+}
+__global__ void __launch_bounds__(kThreads, 2) row_pass_x512_kernel(const RowPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
+    row_pass_body<false, 512>(p, blockIdx.x, gridDim.x);
 }
 __global__ void __launch_bounds__(kThreads) row_pass_adj_kernel(const RowPass p) { row_pass_body<true>(p, blockIdx.x, gridDim.x); }
 
@@ -912,9 +922,11 @@ static cudaError_t ensure_smem(const void *fn, size_t bytes) {
 
 cudaError_t launch_row_pass(const RowPass &p, cudaStream_t s) {
     const size_t sm = row_pass_smem(p);
-    cudaError_t e = ensure_smem((const void *)row_pass_kernel, sm);
+    const bool x512 = p.g.half == 512 && p.g.nx <= 512;
+    const auto fn = x512 ? row_pass_x512_kernel : row_pass_kernel;
+    cudaError_t e = ensure_smem((const void *)fn, sm);
     if (e != cudaSuccess) return e;
-    return launch_pdl(row_pass_kernel, dim3(row_pass_blocks(p)), dim3(kThreads), sm, s, p);
+    return launch_pdl(fn, dim3(row_pass_blocks(p)), dim3(kThreads), sm, s, p);
 }
 
 cudaError_t launch_row_pass_adj(const RowPass &p, cudaStream_t s) {
