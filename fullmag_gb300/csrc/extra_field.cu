@@ -106,11 +106,11 @@ __global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(cons
     // since FP64 throughput is a small fraction of FP32 on this part
     enum { kZee, kDmi, kUni, kCub, kExch };
     float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    // one cell: its state (mx, my, mz) is loaded by the caller
+    auto cell = [&](const long long i, const float mx, const float my, const float mz) {
         float hx = 0.f, hy = 0.f, hz = 0.f;
         float rx = 0.f, ry = 0.f, rz = 0.f;  // region exchange (the H_EX observable)
         if (p.mask == nullptr || p.mask[i] != 0) {
-            const float mx = m[i], my = m[n + i], mz = m[2 * n + i];
             float ax = 0.f, ay = 0.f, az = 0.f;  // DMI + magnetoelastic
             if ((kNb || kRg) && (p.has_int || p.has_bulk || (kRg && p.region))) {
                 // neighbours with the Neumann clamp: a missing or inactive neighbour is the cell
@@ -337,7 +337,29 @@ __global__ void __launch_bounds__(kThreads, kRg ? 3 : 4) extra_field_kernel(cons
             p.h_ex_out[n + i] = ry;
             p.h_ex_out[2 * n + i] = rz;
         }
+    };
+    const long long T = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if constexpr (!kNb && !kRg && !kTh) {
+        // local terms only: four cells a thread strided by the grid, their state loads
+        // issued together ahead of the work (four times the bytes in flight of one cell per
+        // iteration; each load instruction still reads 32 consecutive cells of a warp).
+        // Measured on 256x256x64: magnetoelastic field 38.6 -> 31.7 us, spin-orbit torque
+        // 39.4 -> 32.8 us; the stencil and thermal instances keep one cell per iteration,
+        // where it measured slower (DMI +10 %, thermal +3 %).
+        for (; i + 3 * T < n; i += 4 * T) {
+            float v[4][3];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                v[j][0] = m[i + j * T];
+                v[j][1] = m[n + i + j * T];
+                v[j][2] = m[2 * n + i + j * T];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cell(i + j * T, v[j][0], v[j][1], v[j][2]);
+        }
     }
+    for (; i < n; i += T) cell(i, m[i], m[n + i], m[2 * n + i]);
     if (p.partials) {
         const ExtraSums t = block_sum(ExtraSums{(double)sh[kZee] + (double)sl[kZee], (double)sh[kDmi] + (double)sl[kDmi],
                                                 (double)sh[kUni] + (double)sl[kUni], (double)sh[kCub] + (double)sl[kCub],
