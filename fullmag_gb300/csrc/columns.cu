@@ -831,7 +831,8 @@ __device__ __forceinline__ void y_convolve_2d_fused_body(const ColPass &p, const
     }
 }
 
-// (py = 512 keeps the general path: its inner pass would hold 3 x 16 complex values)
+// (py = 512 takes y_convolve_2d_p512_kernel, a kernel of its own: its inner pass holds
+// 3 x 16 complex values a thread)
 __host__ __device__ __forceinline__ bool y2d_fused_ok(const Grid &g) {
     const int py = g.py;
     return g.per == 0 && (py == 16 || py == 32 || py == 64 || py == 128 || py == 256) && 2 * g.ny <= py;
@@ -925,6 +926,14 @@ __global__ void __launch_bounds__(kThreads) y_convolve_2d_kernel(const ColPass p
     pdl_wait();
     if (p.early) pdl_trigger();
     y_convolve_2d_body(p, blockIdx.x);
+}
+// py = 512 (films of 129..256 rows): the two-level 32 x 16 form, whose inner pass holds
+// 3 x 16 complex values a thread; a kernel of its own so that its registers do not weigh
+// on the other lengths
+__global__ void __launch_bounds__(kThreads, 2) y_convolve_2d_p512_kernel(const ColPass p) {
+    pdl_wait();
+    if (p.early) pdl_trigger();
+    y_convolve_2d_fused_body<32, 16>(p, blockIdx.x);
 }
 
 // One launch for many problems: work[blockIdx.x] = (problem, kx tile).  KIND (see
@@ -1183,7 +1192,8 @@ int col_batched_kind(const Grid &g) {
 
 size_t y_convolve_2d_smem(const Grid &g, int tx) {
     const size_t one = sizeof(float2) * (size_t)3 * tx * skewed_len(g.py);
-    return y2d_fused_ok(g) ? one : 2 * one;
+    const bool p512 = g.per == 0 && g.py == 512 && 2 * g.ny <= 512;
+    return (y2d_fused_ok(g) || p512) ? one : 2 * one;
 }
 
 cudaError_t launch_col_batched(const ColPass *ps, const int2 *work, int nwork, int kind, size_t smem, cudaStream_t s) {
@@ -1208,9 +1218,11 @@ cudaError_t launch_finalize_batched(const FinDesc *fd, int nproblems, double *ou
 
 cudaError_t launch_y_convolve_2d(const ColPass &p, cudaStream_t s) {
     const size_t sm = y_convolve_2d_smem(p.g, p.tx);
-    cudaError_t e = ensure_smem((const void *)y_convolve_2d_kernel, sm);
+    const bool p512 = p.g.per == 0 && p.g.py == 512 && 2 * p.g.ny <= 512;
+    const auto fn = p512 ? y_convolve_2d_p512_kernel : y_convolve_2d_kernel;
+    cudaError_t e = ensure_smem((const void *)fn, sm);
     if (e != cudaSuccess) return e;
-    return launch_pdl(y_convolve_2d_kernel, dim3(tiles(p)), dim3(kThreads), sm, s, p);
+    return launch_pdl(fn, dim3(tiles(p)), dim3(kThreads), sm, s, p);
 }
 
 cudaError_t launch_finalize_stats(const float2 *partials, int nblocks, double *out, cudaStream_t s, int early) {

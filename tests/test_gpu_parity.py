@@ -38,6 +38,8 @@ def make_pair(oracle, kw, integrator=_abi.INTEGRATOR_HEUN, thin=None, mask=None,
 CASES = {
     "cfg1_64x32x4": dict(nx=64, ny=32, nz=4),
     "thin_64x16x1": dict(nx=64, ny=16, nz=1, d=(3.90625e-9, 3.90625e-9, 3e-9)),
+    # py = 512: the thin-film pass's own 32 x 16 instance
+    "thin_16x256x1": dict(nx=16, ny=256, nz=1, d=(3e-9, 2.5e-9, 2e-9)),
     "odd_7x5x3": dict(nx=7, ny=5, nz=3, d=(3e-9, 2e-9, 2.5e-9)),
     "line_9x1x1": dict(nx=9, ny=1, nz=1),
     "single_1x1x1": dict(nx=1, ny=1, nz=1),
