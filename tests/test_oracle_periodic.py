@@ -3,7 +3,8 @@ the truncated image-sum tensor folded from the open tensor of the extended grid
 (crates/fullmag-engine/src/fdm_fft.rs:614-717, restated here in numpy), the unpadded
 FFT convolution against a direct real-space image sum, wrap-around exchange
 (fdm_fields.rs:109-160) on a spin wave that is an eigenvector of the periodic
-Laplacian, and the thin-film limits of the periodic demag field."""
+Laplacian, the thin-film limits of the periodic demag field, and the wrapped DMI and
+Zhang-Li stencils against numpy restatements."""
 import numpy as np
 import pytest
 
@@ -123,3 +124,68 @@ def test_periodic_film_limits(oracle):
     assert np.abs(h_in).max() < 0.01 * MS
     assert np.allclose(h_out[:, 2], -MS, rtol=0.01)
     assert np.abs(h_out[:, :2]).max() < 1e-6 * MS
+
+
+def _grid_fields(nx, ny, nz, arr):
+    """(n, 3) x-fastest -> (3, nz, ny, nx)."""
+    return arr.reshape(nz, ny, nx, 3).transpose(3, 0, 1, 2)
+
+
+def test_periodic_interfacial_dmi_wraps(oracle):
+    # central differences with the wrapped neighbour on periodic axes
+    # (interfacial_dmi_field, fdm_fields.rs:356-392); exchange, demag and Zeeman off so that
+    # H_eff is the DMI field alone
+    nx, ny, nz, d, D = 6, 5, 2, (2e-9, 3e-9, 2e-9), 3e-3
+    n = nx * ny * nz
+    m = random_unit(n, 21)
+    pr = oracle.Problem(nx=nx, ny=ny, nz=nz, dx=d[0], dy=d[1], dz=d[2], ms=MS, a_ex=A, alpha=0.5, m0=m,
+                        enable_exchange=False, enable_demag=False, dmi_d_interfacial=D, periodic=(1, 1, 0))
+    h = _grid_fields(nx, ny, nz, pr.fields()["h_eff"])
+    M = _grid_fields(nx, ny, nz, m)
+    ddx = (np.roll(M, -1, axis=3) - np.roll(M, 1, axis=3)) / (2 * d[0])
+    ddy = (np.roll(M, -1, axis=2) - np.roll(M, 1, axis=2)) / (2 * d[1])
+    pf = 2 * D / (MU0 * MS)
+    want = np.stack([pf * ddx[2], pf * ddy[2], -pf * (ddx[0] + ddy[1])])
+    assert np.allclose(h, want, rtol=1e-12, atol=1e-9 * np.abs(want).max())
+
+
+def test_periodic_zhang_li_upwind_wraps(oracle):
+    # the upwind derivative D = (u . grad) m takes the wrapped neighbour on a periodic axis
+    # (zhang_li_stt_torque, fdm_fields.rs:1253-1340); with every field off the right-hand
+    # side is the torque -m x (m x D) - beta m x D alone
+    nx, ny, nz, d = 7, 4, 3, (2e-9, 3e-9, 2.5e-9)
+    n = nx * ny * nz
+    m = random_unit(n, 23)
+    j, P, beta = (3e11, -2e11, 1e11), 0.6, 0.05
+    pr = oracle.Problem(nx=nx, ny=ny, nz=nz, dx=d[0], dy=d[1], dz=d[2], ms=MS, a_ex=A, alpha=0.5, m0=m,
+                        enable_exchange=False, enable_demag=False, current_density=j, stt_degree=P,
+                        stt_beta=beta, periodic=(1, 0, 1))
+    rhs = _grid_fields(nx, ny, nz, pr.fields()["rhs"])
+    M = _grid_fields(nx, ny, nz, m)
+    mu_b, e = 9.274009994e-24, 1.60217662e-19
+    b = P * mu_b / (e * MS * (1 + beta * beta))
+    u = [b * jj for jj in j]
+    Dv = np.zeros_like(M)
+    for a, (ax, per) in enumerate(((3, True), (2, False), (1, True))):
+        step = d[a]
+        if u[a] > 0:
+            prev = np.roll(M, 1, axis=ax)
+            diff = (M - prev) / step
+            if not per:  # open axis: no upwind neighbour at the first cell
+                idx = [slice(None)] * 4
+                idx[ax] = 0
+                diff[tuple(idx)] = 0.0
+        else:
+            nxt = np.roll(M, -1, axis=ax)
+            diff = (nxt - M) / step
+            if not per:
+                idx = [slice(None)] * 4
+                idx[ax] = -1
+                diff[tuple(idx)] = 0.0
+        Dv += u[a] * diff
+    mm = M.reshape(3, -1).T
+    DD = Dv.reshape(3, -1).T
+    c1 = np.cross(mm, DD)
+    c2 = np.cross(mm, c1)
+    want = (-c2 - beta * c1).T.reshape(M.shape)
+    assert np.allclose(rhs, want, rtol=1e-11, atol=1e-9 * np.abs(want).max())
