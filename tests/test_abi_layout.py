@@ -136,3 +136,37 @@ def test_header_matches_reference_layout(tmp_path):
     assert mine["constants"] == gold["constants"]
     assert set(gold["functions"]) <= set(functions)
     assert len(gold["functions"]) == 22
+
+
+def _plan(nx, ny, nz):
+    import numpy as np
+    from fullmag_gb300.backend import make_plan
+    m0 = np.tile([1.0, 0.0, 0.0], (nx * ny * nz, 1))
+    return make_plan(nx=nx, ny=ny, nz=nz, dx=2e-9, dy=2e-9, dz=2e-9, ms=8e5, a_ex=1.3e-11, alpha=0.5, m0=m0)
+
+
+@pytest.mark.parametrize("shape,periodic,images,message", [
+    ((8, 8, 2), (2, 0, 0), None, b"periodic[] entries must be 0 (open) or 1 (periodic)"),
+    ((8, 8, 2), (1, 0, 0), (5000, 0, 0), b"image_counts above 4096"),
+    ((9, 8, 2), (1, 0, 0), None, b"a periodic x axis needs an even number of cells"),
+])
+def test_periodic_create_refusals_without_gpu(shape, periodic, images, message):
+    # the periodic entry point validates its descriptor and the periodic geometry on the
+    # host, before any device work: a handle comes back with last_error set
+    from fullmag_gb300 import load_library
+    lib = load_library()
+    p, keep = _plan(*shape)
+    d = _abi.PeriodicityDesc()
+    for a, v in enumerate(periodic):
+        d.periodic[a] = v
+    if images is not None:
+        d.has_image_counts = 1
+        for a, v in enumerate(images):
+            d.image_counts[a] = v
+    h = lib.fullmag_fdm_backend_create_periodic(C.byref(p), C.byref(d))
+    try:
+        assert h
+        assert lib.fullmag_fdm_backend_last_error(h) == message
+    finally:
+        lib.fullmag_fdm_backend_destroy(h)
+    del keep
