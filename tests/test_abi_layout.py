@@ -170,3 +170,29 @@ def test_periodic_create_refusals_without_gpu(shape, periodic, images, message):
     finally:
         lib.fullmag_fdm_backend_destroy(h)
     del keep
+
+
+@pytest.mark.parametrize("edit,message", [
+    (lambda p: setattr(p, "initial_magnetization_len", 5), b"initial_magnetization_len mismatch: expected 384, got 5"),
+    (lambda p: setattr(p.grid, "dx", 0.0), b"cell sizes must be positive"),
+    (lambda p: setattr(p.material, "saturation_magnetisation", -1.0), b"saturation_magnetisation must be positive"),
+    (lambda p: setattr(p, "active_mask_len", 7), b"active_mask_len mismatch: expected 128, got 7"),
+])
+def test_create_refusals_without_gpu(edit, message):
+    # the plan validation of create runs on the host before any device work and reports
+    # through last_error on a non-NULL handle (api.cpp:170-180, 324-395)
+    import numpy as np
+    from fullmag_gb300 import load_library
+    lib = load_library()
+    p, keep = _plan(8, 8, 2)
+    mask = np.ones(8 * 8 * 2, dtype=np.uint8)
+    p.active_mask = mask.ctypes.data_as(C.POINTER(C.c_uint8))
+    p.active_mask_len = mask.size
+    edit(p)
+    h = lib.fullmag_fdm_backend_create(C.byref(p))
+    try:
+        assert h
+        assert lib.fullmag_fdm_backend_last_error(h) == message
+    finally:
+        lib.fullmag_fdm_backend_destroy(h)
+    del keep
