@@ -196,3 +196,43 @@ def test_create_refusals_without_gpu(edit, message):
     finally:
         lib.fullmag_fdm_backend_destroy(h)
     del keep
+
+
+@pytest.mark.parametrize("edit,periodic,message", [
+    (lambda p: (setattr(p, "has_interfacial_dmi", 1), setattr(p, "dmi_D_interfacial", 1e-3)), None,
+     b"DMI is not available with double-precision state (use SINGLE)"),
+    (lambda p: setattr(p, "temperature", 300.0), None, b"thermal noise is not available with double-precision state (use SINGLE)"),
+    (lambda p: None, (1, 0, 0), None),
+])
+def test_double_precision_refusals_without_gpu(edit, periodic, message):
+    # the double-precision path refuses the terms it does not carry before any device work;
+    # with periodic axes it refuses the boundary-correction tiers
+    import numpy as np
+    from fullmag_gb300 import load_library
+    lib = load_library()
+    p, keep = _plan(8, 8, 2)
+    p.precision = _abi.PRECISION_DOUBLE
+    edit(p)
+    if periodic is None:
+        h = lib.fullmag_fdm_backend_create(C.byref(p))
+    else:
+        n = 8 * 8 * 2
+        phi = np.ones(n)
+        p.boundary_correction = _abi.BOUNDARY_VOLUME
+        p.volume_fraction = phi.ctypes.data_as(C.POINTER(C.c_double))
+        p.volume_fraction_len = n
+        faces = [np.ones(n) for _ in range(6)]
+        for name, f in zip(("face_link_xp", "face_link_xm", "face_link_yp", "face_link_ym", "face_link_zp",
+                            "face_link_zm"), faces):
+            setattr(p, name, f.ctypes.data_as(C.POINTER(C.c_double)))
+        d = _abi.PeriodicityDesc()
+        for a, v in enumerate(periodic):
+            d.periodic[a] = v
+        h = lib.fullmag_fdm_backend_create_periodic(C.byref(p), C.byref(d))
+        message = b"boundary correction is not available with periodic boundaries"
+    try:
+        assert h
+        assert lib.fullmag_fdm_backend_last_error(h) == message
+    finally:
+        lib.fullmag_fdm_backend_destroy(h)
+    del keep
